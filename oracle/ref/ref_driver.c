@@ -1,0 +1,80 @@
+/*
+ * Driver around the reference GCGE CPU path (app_ccs backend + GCG), compiled
+ * together with the unmodified reference sources into oracle/_ref/.  Test
+ * infrastructure only: used to generate the golden fixtures and as the
+ * reference arm of the CPU baseline in this container.
+ *
+ * The call sequence is the one the reference's own front end uses
+ * (gcge.c:490-517): OPS_Create, backend Set, OPS_Setup, MultiVecCreateByMat
+ * for evec, GCGE_Create for the four multivector workspaces, dbl_ws/int_ws
+ * sized as in gcge.c:503-510 (= src/ops_eig_sol_gcg.c:1647-1651),
+ * EigenSolverSetup_GCG, GCGE_Setparameters, ops->EigenSolver.
+ * The backend is app_ccs (app/app_ccs.c:213-249), the reference's sparse CCS
+ * operator with int32 indices and FP64 values.
+ */
+#include <stdlib.h>
+#include <string.h>
+
+#include "ops.h"
+#include "app_ccs.h"
+#include "ops_eig_sol_gcg.h"
+
+int ref_gcg_solve(int n,
+                  const int *a_colptr, const int *a_rowind, const double *a_val,
+                  const int *b_colptr, const int *b_rowind, const double *b_val,
+                  int nev, int block_size, int nev_init, int nev_max, int max_iter,
+                  double abs_tol, double rel_tol, double gap_min, int auto_shift,
+                  const double *x0, int nev_given,
+                  double *eval_out, double *evec_out, int *nconv_out, int *niter_out)
+{
+    OPS *ops = NULL;
+    OPS_Create(&ops);
+    OPS_CCS_Set(ops);
+    OPS_Setup(ops);
+
+    CCSMAT A, B;
+    A.data = (double *)a_val; A.i_row = (int *)a_rowind; A.j_col = (int *)a_colptr;
+    A.nrows = n; A.ncols = n;
+    void *matB = NULL;
+    if (b_colptr != NULL) {
+        B.data = (double *)b_val; B.i_row = (int *)b_rowind; B.j_col = (int *)b_colptr;
+        B.nrows = n; B.ncols = n;
+        matB = &B;
+    }
+
+    double *eval = calloc((size_t)nev_max, sizeof(double));
+    void **evec = NULL;
+    ops->MultiVecCreateByMat(&evec, nev_max, &A, ops);
+    LAPACKVEC *ev = (LAPACKVEC *)evec;
+    if (nev_given > 0)
+        memcpy(ev->data, x0, sizeof(double) * (size_t)n * (size_t)nev_given);
+
+    srand(0);
+    void **mv_ws[4];
+    GCGE_Create(&A, nev_max, block_size, nev_init, mv_ws, NULL, NULL, ops);
+    int sizeV = nev_init + 2 * block_size;
+    int len_dbl = 2 * sizeV * sizeV + 10 * sizeV + (nev_max + 2 * block_size) + nev_max * block_size;
+    int len_int = 6 * sizeV + 2 * (block_size + 3);
+    double *dbl_ws = calloc((size_t)len_dbl, sizeof(double));
+    int *int_ws = calloc((size_t)len_int, sizeof(int));
+    srand(0);
+
+    double tol[2] = {abs_tol, rel_tol};
+    EigenSolverSetup_GCG(gap_min, nev_init, nev_max, block_size, tol, max_iter, 0, 0, 0,
+                         mv_ws, dbl_ws, int_ws, ops);
+    GCGE_Setparameters(gap_min, auto_shift, ops);
+    int nconv = nev;
+    ops->EigenSolver(&A, matB, eval, evec, nev_given, &nconv, ops);
+
+    memcpy(eval_out, eval, sizeof(double) * (size_t)nev_max);
+    memcpy(evec_out, ev->data, sizeof(double) * (size_t)n * (size_t)nev_max);
+    *nconv_out = nconv;
+    *niter_out = ((GCGSolver *)ops->eigen_solver_workspace)->numIter;
+
+    /* GCGE_Destroymvws frees dbl_ws/int_ws as well (src/ops_eig_sol_gcg.c:1919-1927). */
+    GCGE_Destroymvws(mv_ws, dbl_ws, int_ws, nev_max, block_size, ops);
+    ops->MultiVecDestroy(&evec, nev_max, ops);
+    free(eval);
+    OPS_Destroy(&ops);
+    return 0;
+}

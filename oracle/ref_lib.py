@@ -1,0 +1,65 @@
+"""ctypes binding of the reference GCGE CPU path compiled from its own sources
+(``oracle/ref/Makefile`` -> ``oracle/_ref/libgcge_ref.so``).
+
+TEST INFRASTRUCTURE ONLY.  The library exists only where the reference tree
+was present at build time; callers check :func:`available` first.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import time
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "_ref", "libgcge_ref.so")
+_lib = None
+
+
+def available() -> bool:
+    if not os.path.exists(LIB_PATH):
+        return False
+    try:
+        _load()
+        return True
+    except OSError:
+        return False
+
+
+def _load():
+    global _lib
+    if _lib is None:
+        _lib = ctypes.CDLL(LIB_PATH, mode=ctypes.RTLD_LOCAL)
+        _lib.ref_gcg_solve.restype = ctypes.c_int
+    return _lib
+
+
+def _ptr(a):
+    return None if a is None else a.ctypes.data_as(ctypes.c_void_p)
+
+
+def ref_solve(A, B, X0, nev, block_size, nev_init, nev_max, tol=(1e300, 1e-8), max_iter=500,
+              gap_min=1e-5, auto_shift=1):
+    """Run the reference GCG (app_ccs backend) on CSRMatrix inputs.
+
+    A and B are symmetric, so their CSR arrays are also their CCS arrays.
+    Returns (eval[nev_max], evec[n, nev_max], nconv, niter, seconds).
+    """
+    lib = _load()
+    n = A.n
+    X0 = np.asfortranarray(X0, dtype=np.float64)
+    ev = np.zeros(nev_max)
+    evec = np.zeros((n, nev_max), order="F")
+    nc = ctypes.c_int()
+    it = ctypes.c_int()
+    t = time.perf_counter()
+    lib.ref_gcg_solve(
+        ctypes.c_int(n), _ptr(A.indptr), _ptr(A.indices), _ptr(A.data),
+        _ptr(None if B is None else B.indptr), _ptr(None if B is None else B.indices),
+        _ptr(None if B is None else B.data),
+        ctypes.c_int(nev), ctypes.c_int(block_size), ctypes.c_int(nev_init), ctypes.c_int(nev_max),
+        ctypes.c_int(max_iter), ctypes.c_double(tol[0]), ctypes.c_double(tol[1]),
+        ctypes.c_double(gap_min), ctypes.c_int(auto_shift), _ptr(X0), ctypes.c_int(X0.shape[1]),
+        _ptr(ev), _ptr(evec), ctypes.byref(nc), ctypes.byref(it))
+    return ev, evec, nc.value, it.value, time.perf_counter() - t
