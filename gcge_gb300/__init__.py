@@ -1,0 +1,419 @@
+"""gcge_gb300 - GB300-native (sm_103a) GCG block eigensolver behind GCGE's
+OPS plugin surface.
+
+The product is the C-ABI shared library ``libgcge_cuda.so`` (declared in
+``include/gcge_ops.h`` and ``include/gcge_cuda.h``).  This module is the thin
+Python host side over it, mirroring the reference's call sequence
+(OPS_Create / OPS_CUDA_Set / OPS_Setup, MultiVecCreateByMat, GCGE_Create,
+EigenSolverSetup_GCG, GCGE_Setparameters, ops->EigenSolver; gcge.c:490-531),
+plus one-call helpers.  It needs no PyTorch: device memory, the stream and
+timing live in the library.  If the library is missing, every entry point
+raises - there is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import problems  # noqa: F401  (re-export)
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libgcge_cuda.so")
+
+GCGE_OK = 0
+GCGE_ERR_NOT_CONVERGED = 6
+PREC_FP64 = 0
+PREC_MIXED = 1
+
+# Every symbol include/*.h declares (checked by the CPU tests).
+EXPORTED_SYMBOLS = [
+    "OPS_Create", "OPS_Setup", "OPS_Destroy", "OPS_CUDA_Set",
+    "EigenSolverSetup_GCG", "EigenSolverCreateWorkspace_GCG", "EigenSolverDestroyWorkspace_GCG",
+    "EigenSolverSetParameters_GCG", "GCGE_Create", "GCGE_Setparameters", "GCGE_Destroymvws",
+    "ops_cuda_last_error", "ops_cuda_error_string", "ops_cuda_last_error_detail",
+    "CUDA_MatCreateFromCCS", "CUDA_MatDestroy",
+    "CUDA_MatNnz", "CUDA_MultiVecSetFromHost", "CUDA_MultiVecGetToHost", "CUDA_MultiVecSize",
+    "GCGE_SetPrecision", "GCGE_Solve", "GCGE_GetSolveInfo", "GCGE_Prepare", "GCGE_PreparedSolve",
+    "GCGE_PreparedDestroy", "GCGE_BenchSpMM", "GCGE_DenseEig", "GCGE_BlockPCG", "GCGE_BOrth",
+]
+
+_lib = None
+
+
+class GCGEError(RuntimeError):
+    def __init__(self, status: int, what: str = ""):
+        msg = _status_string(status) if _lib is not None else str(status)
+        detail = ""
+        if _lib is not None:
+            f = _lib.ops_cuda_last_error_detail
+            f.restype = ctypes.c_char_p
+            detail = (f() or b"").decode(errors="replace")
+        super().__init__(f"{what}: status {status} ({msg}) {detail}")
+        self.status = status
+
+
+def _status_string(s: int) -> str:
+    f = _lib.ops_cuda_error_string
+    f.restype = ctypes.c_char_p
+    return f(ctypes.c_int(s)).decode()
+
+
+class SolveInfo(ctypes.Structure):
+    _fields_ = [("nconv", ctypes.c_int), ("niter", ctypes.c_int), ("status", ctypes.c_int),
+                ("pcg_iters", ctypes.c_int), ("spmm_calls", ctypes.c_int),
+                ("kernel_launches", ctypes.c_int), ("seconds", ctypes.c_double),
+                ("phase_ms", ctypes.c_double * 10)]
+
+    PHASES = ("checkconv", "compP", "compRR", "rr_matW", "eig", "compRV", "compW", "linsol",
+              "compX", "initX")
+
+    def as_dict(self) -> dict:
+        d = {k: getattr(self, k) for k in ("nconv", "niter", "status", "pcg_iters", "spmm_calls",
+                                           "kernel_launches", "seconds")}
+        d["phase_ms"] = {p: self.phase_ms[i] for i, p in enumerate(self.PHASES)}
+        return d
+
+
+def lib_path() -> str:
+    return LIB_PATH
+
+
+def load(build_if_missing: bool = False) -> ctypes.CDLL:
+    """Load libgcge_cuda.so (RTLD_GLOBAL is not needed: one library)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        if build_if_missing:
+            from .build import build
+            build()
+        else:
+            raise ImportError(f"{LIB_PATH} is missing: run gcge_gb300.build.build() (nvcc, sm_103a)")
+    lib = ctypes.CDLL(LIB_PATH)
+    for name in ("CUDA_MatCreateFromCCS", "CUDA_MultiVecSetFromHost", "CUDA_MultiVecGetToHost",
+                 "GCGE_Solve", "GCGE_Prepare", "GCGE_PreparedSolve", "GCGE_SetPrecision",
+                 "GCGE_GetSolveInfo", "GCGE_BenchSpMM", "ops_cuda_last_error", "CUDA_MultiVecSize",
+                 "CUDA_MatNnz", "GCGE_DenseEig", "GCGE_BlockPCG", "GCGE_BOrth"):
+        getattr(lib, name).restype = ctypes.c_int
+    _lib = lib
+    return lib
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data_as(ctypes.c_void_p)
+
+
+def _csr_args(M):
+    if M is None:
+        return None, None, None
+    return (np.ascontiguousarray(M.indptr, dtype=np.int32),
+            np.ascontiguousarray(M.indices, dtype=np.int32),
+            np.ascontiguousarray(M.data, dtype=np.float64))
+
+
+@dataclass
+class SolveResult:
+    eval: np.ndarray
+    evec: np.ndarray | None
+    nconv: int
+    niter: int
+    status: int
+    info: dict = field(default_factory=dict)
+
+
+def solve(A, B, nev, block_size, nev_init, nev_max, X0=None, tol=(1e300, 1e-8), max_iter=500,
+          gap_min=1e-5, auto_shift=1, precision=PREC_FP64, want_evec=True) -> SolveResult:
+    """One GCG solve through GCGE_Solve.  A, B: problems.CSRMatrix (symmetric,
+    so CSR arrays == CCS arrays); B None = identity.  X0 (n x k) seeds the basis."""
+    lib = load()
+    n = A.n
+    a = _csr_args(A)
+    b = _csr_args(B)
+    X0 = None if X0 is None else np.asfortranarray(X0, dtype=np.float64)
+    ng = 0 if X0 is None else X0.shape[1]
+    ev = np.zeros(nev_max)
+    evec = np.zeros((n, nev_max), order="F") if want_evec else None
+    info = SolveInfo()
+    t = (ctypes.c_double * 2)(*tol)
+    st = lib.GCGE_Solve(ctypes.c_int(n), _p(a[0]), _p(a[1]), _p(a[2]), _p(b[0]), _p(b[1]), _p(b[2]),
+                        ctypes.c_int(nev), ctypes.c_int(block_size), ctypes.c_int(nev_init),
+                        ctypes.c_int(nev_max), ctypes.c_int(max_iter), t, ctypes.c_double(gap_min),
+                        ctypes.c_int(auto_shift), ctypes.c_int(precision), _p(X0), ctypes.c_int(ng),
+                        _p(ev), _p(evec), ctypes.byref(info))
+    if st not in (GCGE_OK, GCGE_ERR_NOT_CONVERGED):
+        raise GCGEError(st, "GCGE_Solve")
+    return SolveResult(ev, evec, info.nconv, info.niter, st, info.as_dict())
+
+
+class Prepared:
+    """A problem resident in HBM: matrices, initial block and solver state.
+    ``solve()`` times device work only (inputs already on the GPU)."""
+
+    def __init__(self, A, B, nev, block_size, nev_init, nev_max, X0=None, tol=(1e300, 1e-8),
+                 max_iter=500, gap_min=1e-5, auto_shift=1, precision=PREC_FP64):
+        lib = load()
+        self.lib = lib
+        self.n, self.nev_max = A.n, nev_max
+        a = _csr_args(A)
+        b = _csr_args(B)
+        X0 = None if X0 is None else np.asfortranarray(X0, dtype=np.float64)
+        ng = 0 if X0 is None else X0.shape[1]
+        self.handle = ctypes.c_void_p()
+        t = (ctypes.c_double * 2)(*tol)
+        st = lib.GCGE_Prepare(ctypes.byref(self.handle), ctypes.c_int(A.n), _p(a[0]), _p(a[1]),
+                              _p(a[2]), _p(b[0]), _p(b[1]), _p(b[2]), ctypes.c_int(nev),
+                              ctypes.c_int(block_size), ctypes.c_int(nev_init),
+                              ctypes.c_int(nev_max), ctypes.c_int(max_iter), t,
+                              ctypes.c_double(gap_min), ctypes.c_int(auto_shift),
+                              ctypes.c_int(precision), _p(X0), ctypes.c_int(ng))
+        if st != GCGE_OK:
+            raise GCGEError(st, "GCGE_Prepare")
+
+    def solve(self, want_evec=False) -> SolveResult:
+        ev = np.zeros(self.nev_max)
+        evec = np.zeros((self.n, self.nev_max), order="F") if want_evec else None
+        info = SolveInfo()
+        st = self.lib.GCGE_PreparedSolve(self.handle, _p(ev), _p(evec), ctypes.byref(info))
+        if st not in (GCGE_OK, GCGE_ERR_NOT_CONVERGED):
+            raise GCGEError(st, "GCGE_PreparedSolve")
+        return SolveResult(ev, evec, info.nconv, info.niter, st, info.as_dict())
+
+    def close(self):
+        if self.handle:
+            self.lib.GCGE_PreparedDestroy(ctypes.byref(self.handle))
+            self.handle = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+# ---------------------------------------------------------------------------
+# OPS vtable access, for callers that drive the backend slot by slot
+# ---------------------------------------------------------------------------
+_OPS_FIELDS = [
+    "Printf", "GetWtime", "GetOptionFromCommandLine", "MatView", "MatAxpby", "VecCreateByMat",
+    "VecCreateByVec", "VecDestroy", "VecView", "VecInnerProd", "VecLocalInnerProd",
+    "VecSetRandomValue", "VecAxpby", "MatDotVec", "MatTransDotVec", "MultiVecCreateByMat",
+    "MultiVecCreateByVec", "MultiVecCreateByMultiVec", "MultiVecDestroy", "GetVecFromMultiVec",
+    "RestoreVecForMultiVec", "MultiVecView", "MultiVecLocalInnerProd", "MultiVecInnerProd",
+    "MultiVecSetRandomValue", "MultiVecAxpby", "MultiVecLinearComb", "MatDotMultiVec",
+    "MatTransDotMultiVec", "MultiVecQtAP", "lapack_ops", "DenseMatQtAP", "DenseMatOrth",
+    "LinearSolver", "linear_solver_workspace", "MultiLinearSolver",
+    "multi_linear_solver_workspace", "MultiVecOrth", "orth_workspace", "MultiGridCreate",
+    "MultiGridDestroy", "VecFromItoJ", "MultiVecFromItoJ", "EigenSolver",
+    "eigen_solver_workspace", "app_ops",
+]
+
+
+class OPSStruct(ctypes.Structure):
+    """Layout of struct OPS_ (src/ops.h:43-152): 46 pointer-sized members."""
+    _fields_ = [(f, ctypes.c_void_p) for f in _OPS_FIELDS]
+
+
+_I2 = ctypes.c_int * 2
+_VP = ctypes.c_void_p
+_FT = {
+    "MultiVecCreateByMat": ctypes.CFUNCTYPE(None, ctypes.POINTER(_VP), ctypes.c_int, _VP, _VP),
+    "MultiVecDestroy": ctypes.CFUNCTYPE(None, ctypes.POINTER(_VP), ctypes.c_int, _VP),
+    "MultiVecAxpby": ctypes.CFUNCTYPE(None, ctypes.c_double, _VP, ctypes.c_double, _VP, _I2, _I2, _VP),
+    "MultiVecLinearComb": ctypes.CFUNCTYPE(None, _VP, _VP, ctypes.c_int, _I2, _I2,
+                                           ctypes.POINTER(ctypes.c_double), ctypes.c_int,
+                                           ctypes.POINTER(ctypes.c_double), ctypes.c_int, _VP),
+    "MultiVecInnerProd": ctypes.CFUNCTYPE(None, ctypes.c_char, _VP, _VP, ctypes.c_int, _I2, _I2,
+                                          ctypes.POINTER(ctypes.c_double), ctypes.c_int, _VP),
+    "MatDotMultiVec": ctypes.CFUNCTYPE(None, _VP, _VP, _VP, _I2, _I2, _VP),
+    "MultiVecQtAP": ctypes.CFUNCTYPE(None, ctypes.c_char, ctypes.c_char, _VP, _VP, _VP,
+                                     ctypes.c_int, _I2, _I2, ctypes.POINTER(ctypes.c_double),
+                                     ctypes.c_int, _VP, _VP),
+    "MultiVecSetRandomValue": ctypes.CFUNCTYPE(None, _VP, ctypes.c_int, ctypes.c_int, _VP),
+}
+
+
+class CudaOps:
+    """OPS filled by OPS_CUDA_Set, with numpy-friendly wrappers of its slots
+    (the same slot names and argument meaning as the reference's OPS)."""
+
+    def __init__(self):
+        lib = load()
+        self.lib = lib
+        self.ptr = ctypes.POINTER(OPSStruct)()
+        lib.OPS_Create(ctypes.byref(self.ptr))
+        lib.OPS_CUDA_Set(self.ptr)
+        lib.OPS_Setup(self.ptr)
+        self._mats, self._mvs = [], []
+
+    def _fn(self, name):
+        return ctypes.cast(getattr(self.ptr.contents, name), _FT[name])
+
+    def check(self, what=""):
+        st = self.lib.ops_cuda_last_error()
+        if st != GCGE_OK:
+            raise GCGEError(st, what)
+
+    def mat(self, M):
+        h = ctypes.c_void_p()
+        a = _csr_args(M)
+        st = self.lib.CUDA_MatCreateFromCCS(ctypes.byref(h), ctypes.c_int(M.n), ctypes.c_int(M.n),
+                                            _p(a[0]), _p(a[1]), _p(a[2]))
+        if st != GCGE_OK:
+            raise GCGEError(st, "CUDA_MatCreateFromCCS")
+        self._mats.append(h)
+        return h
+
+    def multivec(self, mat, ncols, host=None):
+        h = _VP()
+        self._fn("MultiVecCreateByMat")(ctypes.byref(h), ncols, mat, ctypes.cast(self.ptr, _VP))
+        self.check("MultiVecCreateByMat")
+        if host is not None:
+            self.upload(h, host)
+        self._mvs.append((h, ncols))
+        return h
+
+    def upload(self, mv, host, start=0):
+        host = np.asfortranarray(host, dtype=np.float64)
+        st = self.lib.CUDA_MultiVecSetFromHost(mv, start, start + host.shape[1], _p(host),
+                                               host.shape[0])
+        if st != GCGE_OK:
+            raise GCGEError(st, "CUDA_MultiVecSetFromHost")
+
+    def download(self, mv, start, end):
+        nr, nc = ctypes.c_int(), ctypes.c_int()
+        self.lib.CUDA_MultiVecSize(mv, ctypes.byref(nr), ctypes.byref(nc))
+        out = np.zeros((nr.value, end - start), order="F")
+        st = self.lib.CUDA_MultiVecGetToHost(mv, start, end, _p(out), nr.value)
+        if st != GCGE_OK:
+            raise GCGEError(st, "CUDA_MultiVecGetToHost")
+        return out
+
+    # slots -------------------------------------------------------------
+    def axpby(self, alpha, x, beta, y, start, end):
+        self._fn("MultiVecAxpby")(alpha, x, beta, y, _I2(*start), _I2(*end), ctypes.cast(self.ptr, _VP))
+        self.check("MultiVecAxpby")
+
+    def linear_comb(self, x, y, start, end, coef=None, ldc=0, beta=None, incb=0):
+        c = None if coef is None else np.asfortranarray(coef, dtype=np.float64)
+        b = None if beta is None else np.ascontiguousarray(beta, dtype=np.float64)
+        cp = None if c is None else c.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+        bp = None if b is None else b.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+        self._fn("MultiVecLinearComb")(x, y, 0, _I2(*start), _I2(*end), cp, ldc, bp, incb,
+                                       ctypes.cast(self.ptr, _VP))
+        self.check("MultiVecLinearComb")
+
+    def inner_prod(self, mode, x, y, start, end, ldip=None):
+        nr, nc = end[0] - start[0], end[1] - start[1]
+        if mode == "D":
+            out = np.zeros(nc)
+            ld = 1
+        else:
+            ld = ldip or nr
+            out = np.zeros((ld, nc), order="F")
+        self._fn("MultiVecInnerProd")(mode.encode(), x, y, 0, _I2(*start), _I2(*end),
+                                      out.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), ld,
+                                      ctypes.cast(self.ptr, _VP))
+        self.check("MultiVecInnerProd")
+        return out
+
+    def mat_dot(self, mat, x, y, start, end):
+        self._fn("MatDotMultiVec")(mat, x, y, _I2(*start), _I2(*end), ctypes.cast(self.ptr, _VP))
+        self.check("MatDotMultiVec")
+
+    def qtap(self, ntsA, mode, Q, A, P, start, end, ws, ld=None):
+        nr, nc = end[0] - start[0], end[1] - start[1]
+        shape = (nc, nr) if mode == "T" else (nr, nc)
+        ld = ld or shape[0]
+        out = np.zeros((ld, shape[1]), order="F")
+        self._fn("MultiVecQtAP")(ntsA.encode(), mode.encode(), Q, A, P, 0, _I2(*start), _I2(*end),
+                                 out.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), ld, ws,
+                                 ctypes.cast(self.ptr, _VP))
+        self.check("MultiVecQtAP")
+        return out
+
+    def set_random(self, x, start, end):
+        self._fn("MultiVecSetRandomValue")(x, start, end, ctypes.cast(self.ptr, _VP))
+        self.check("MultiVecSetRandomValue")
+
+    def close(self):
+        for h, nc in self._mvs:
+            self._fn("MultiVecDestroy")(ctypes.byref(h), nc, ctypes.cast(self.ptr, _VP))
+        for h in self._mats:
+            self.lib.CUDA_MatDestroy(ctypes.byref(h))
+        self._mvs, self._mats = [], []
+        if self.ptr:
+            self.lib.OPS_Destroy(ctypes.byref(self.ptr))
+
+
+def bench_spmm(A, k: int, fp32: bool, reps: int = 20):
+    """Average ms per SpMM launch of k columns and its algorithmic bytes."""
+    lib = load()
+    ops = CudaOps()
+    try:
+        h = ops.mat(A)
+        ms, by = ctypes.c_double(), ctypes.c_double()
+        st = lib.GCGE_BenchSpMM(h, ctypes.c_int(k), ctypes.c_int(1 if fp32 else 0), ctypes.c_int(reps),
+                                ctypes.byref(ms), ctypes.byref(by))
+        if st != GCGE_OK:
+            raise GCGEError(st, "GCGE_BenchSpMM")
+        return ms.value, by.value
+    finally:
+        ops.close()
+
+
+def dense_eig(M: np.ndarray):
+    """Eigen-decomposition of a symmetric matrix with the solver's dense
+    eigensolver (FP32 Jacobi + FP64 refinement on the GPU)."""
+    lib = load()
+    M = np.asfortranarray(M, dtype=np.float64)
+    s = M.shape[0]
+    ev = np.zeros(s)
+    Z = np.zeros((s, s), order="F")
+    st = lib.GCGE_DenseEig(ctypes.c_int(s), _p(M), ctypes.c_int(s), _p(ev), _p(Z), ctypes.c_int(s))
+    if st != GCGE_OK:
+        raise GCGEError(st, "GCGE_DenseEig")
+    return ev, Z
+
+
+def block_pcg(A, B, sigma, b, x0, max_iter=30, rate=1e-2, tol=1e-14, fp32=False):
+    """Block CG on (A + sigma B) x = b through GCGE_BlockPCG; returns (x, iters)."""
+    ops = CudaOps()
+    try:
+        hA = ops.mat(A)
+        hB = ops.mat(B) if B is not None else None
+        k = b.shape[1]
+        hb = ops.multivec(hA, k, b)
+        hx = ops.multivec(hA, k, x0)
+        it = ctypes.c_int()
+        st = ops.lib.GCGE_BlockPCG(hA, hB, ctypes.c_double(sigma), hb, hx, ctypes.c_int(k),
+                                   ctypes.c_int(max_iter), ctypes.c_double(rate),
+                                   ctypes.c_double(tol), ctypes.c_int(1 if fp32 else 0),
+                                   ctypes.byref(it))
+        if st != GCGE_OK:
+            raise GCGEError(st, "GCGE_BlockPCG")
+        return ops.download(hx, 0, k), it.value
+    finally:
+        ops.close()
+
+
+def b_orth(B, X, start, n=None, zero_tol=2 * np.finfo(float).eps, max_reorth=2, A_for_size=None):
+    """B-orthonormalise columns [start, end) of X against [0, start) via
+    GCGE_BOrth; returns the orthonormalised block (columns [0, new_end))."""
+    ops = CudaOps()
+    try:
+        M = B if B is not None else A_for_size
+        hB = ops.mat(B) if B is not None else None
+        hM = hB if hB is not None else ops.mat(M)
+        k = X.shape[1]
+        hx = ops.multivec(hM, k, X)
+        end = ctypes.c_int(k)
+        st = ops.lib.GCGE_BOrth(hB, hx, ctypes.c_int(start), ctypes.byref(end),
+                                ctypes.c_double(zero_tol), ctypes.c_int(max_reorth))
+        if st != GCGE_OK:
+            raise GCGEError(st, "GCGE_BOrth")
+        return ops.download(hx, 0, end.value)
+    finally:
+        ops.close()

@@ -1,0 +1,206 @@
+// Shared definitions of the GB300 GCGE library: status handling, device
+// buffers, multivector / sparse-matrix objects and kernel launcher prototypes.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <cstdio>
+#include <string>
+#include <vector>
+
+#include "../../include/gcge_cuda.h"
+
+namespace gcge {
+
+// ---------------------------------------------------------------- status
+void set_error(int status, const char *where);
+int take_error();
+const char *status_string(int s);
+
+struct CudaError {
+    int status;
+    std::string where;
+};
+
+// Throws CudaError on failure; every C-ABI entry point catches it and turns it
+// into a status code, so no exception crosses the ABI.
+#define GCGE_CUDA(call)                                                              \
+    do {                                                                             \
+        cudaError_t e_ = (call);                                                     \
+        if (e_ != cudaSuccess) {                                                     \
+            throw ::gcge::CudaError{GCGE_ERR_CUDA, std::string(#call) + ": " +         \
+                                                       cudaGetErrorString(e_)};       \
+        }                                                                            \
+    } while (0)
+#define GCGE_CHECK_LAUNCH() GCGE_CUDA(cudaGetLastError())
+#define GCGE_REQUIRE(cond, status, msg)                                              \
+    do {                                                                             \
+        if (!(cond)) throw ::gcge::CudaError{(status), std::string(msg)};            \
+    } while (0)
+
+// Count of kernels launched by the library (per process); the solver reports
+// the difference over a solve.
+extern unsigned long long g_kernel_launches;
+inline void count_launch(int k = 1) { g_kernel_launches += (unsigned long long)k; }
+
+// ---------------------------------------------------------------- buffers
+template <typename T>
+struct DevBuf {
+    T *p = nullptr;
+    size_t n = 0;
+    DevBuf() = default;
+    DevBuf(const DevBuf &) = delete;
+    DevBuf &operator=(const DevBuf &) = delete;
+    ~DevBuf() { release(); }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        n = 0;
+    }
+    void alloc(size_t count) {
+        if (count <= n && p) return;
+        release();
+        if (count == 0) return;
+        cudaError_t e = cudaMalloc((void **)&p, count * sizeof(T));
+        if (e != cudaSuccess) {
+            p = nullptr;
+            throw CudaError{GCGE_ERR_ALLOC, std::string("cudaMalloc: ") + cudaGetErrorString(e)};
+        }
+        n = count;
+    }
+    T *get() const { return p; }
+};
+
+template <typename T>
+struct PinnedBuf {
+    T *p = nullptr;
+    size_t n = 0;
+    PinnedBuf() = default;
+    PinnedBuf(const PinnedBuf &) = delete;
+    PinnedBuf &operator=(const PinnedBuf &) = delete;
+    ~PinnedBuf() {
+        if (p) cudaFreeHost(p);
+    }
+    void alloc(size_t count) {
+        if (count <= n && p) return;
+        if (p) cudaFreeHost(p);
+        p = nullptr;
+        n = 0;
+        if (count == 0) return;
+        GCGE_CUDA(cudaMallocHost((void **)&p, count * sizeof(T)));
+        n = count;
+    }
+};
+
+// ---------------------------------------------------------------- objects
+constexpr uint32_t kMultiVecMagic = 0x4D564755u;  // multivector
+constexpr uint32_t kMatMagic = 0x4D544755u;       // sparse matrix
+
+// Column-major multivector in HBM: column c starts at data + c * ld.
+// ld is nrows rounded up to 32 elements so every column is 256-byte aligned.
+struct MultiVec {
+    uint32_t magic = kMultiVecMagic;
+    int nrows = 0, ncols = 0, ld = 0;
+    double *data = nullptr;
+    bool owns = true;
+};
+
+// SELL-32 (sliced ELLPACK, slice height 32 = one warp) sparsity pattern with
+// one or more value arrays in the same padded order.  Entry e of row r lives
+// at slice_ptr[r / 32] + e * 32 + r % 32; padding entries repeat the row's own
+// column index with a zero value, so every index is in range.
+struct SellPattern {
+    int n = 0;
+    int nslices = 0;
+    long long nnz = 0;      // true nonzeros
+    long long padded = 0;   // stored entries
+    DevBuf<long long> slice_ptr;
+    DevBuf<int> col;
+};
+
+struct SparseMat {
+    uint32_t magic = kMatMagic;
+    unsigned long long serial = 0;  // unique per created matrix
+    int n = 0;
+    long long nnz = 0;
+    // host CSR copy (symmetric matrix: CSR == CCS)
+    std::vector<int> h_ptr, h_ind;
+    std::vector<double> h_val;
+    SellPattern pat;
+    DevBuf<double> val;      // FP64 values in SELL order
+};
+
+MultiVec *as_mv(void *h);
+SparseMat *as_mat(void *h);
+
+// SELL-32 construction from host CSR arrays (row indices sorted or not).
+// Every input value array is laid out in the padded SELL order; the pattern
+// (slice pointers, column indices) is returned on the host for upload.
+void sell_from_csr(int n, const int *ptr, const int *ind, const std::vector<const double *> &vals,
+                   SellPattern &pat, std::vector<std::vector<double>> &out_vals,
+                   std::vector<int> &h_col, std::vector<long long> &h_sp);
+void upload_sell(SellPattern &pat, const std::vector<int> &h_col, const std::vector<long long> &h_sp,
+                 cudaStream_t st);
+
+// ---------------------------------------------------------------- launchers
+// Sparse (spmm.cu).  X, Y column-major with leading dimensions; k columns.
+template <typename T>
+void spmm(const SellPattern &pat, const T *val, const T *X, int ldx, T *Y, int ldy, int k,
+          cudaStream_t st);
+// Y = M X and partial dots sum_i X[i,c] * Y[i,c] into partial[block * kmax + c];
+// returns the number of blocks (partials to reduce).
+template <typename T>
+int spmm_dot(const SellPattern &pat, const T *val, const T *X, int ldx, T *Y, int ldy, int k,
+             const int *active, double *partial, int kmax, cudaStream_t st);
+// partial[block*kmax+c] = sum over the block's rows of r^2 with r = (A - lam_c B) x_c
+int residual_norms(const SellPattern &pat, const double *a, const double *b, const double *X,
+                   int ldx, const double *lam, int k, double *partial, int kmax, cudaStream_t st);
+int spmm_blocks(const SellPattern &pat);
+
+// Dense (dense.cu).
+void axpby(int n, int ncols, double alpha, const double *X, int ldx, double beta, double *Y,
+           int ldy, cudaStream_t st);
+void axpby_f32(int n, int ncols, float alpha, const float *X, int ldx, float beta, float *Y,
+               int ldy, cudaStream_t st);
+// Y(:, j) = alpha sum_l X(:, l) C(l, j) + beta_j Y(:, j); beta == nullptr -> 0,
+// incb == 0 -> scalar *beta.  C on the device.
+void lincomb(int n, int k, int m, const double *X, int ldx, const double *C, int ldc, double *Y,
+             int ldy, const double *beta_dev, int incb, cudaStream_t st, double alpha = 1.0);
+// C(m x w) = Q^T P over n rows; result written to C (device, ldc).
+void gram(int n, int m, int w, const double *Q, int ldq, const double *P, int ldp, double *C,
+          int ldc, double *scratch, size_t scratch_elems, cudaStream_t st);
+size_t gram_scratch_elems(int n, int m, int w);
+// per-column dots out[c] = X(:,c) . Y(:,c)
+void coldot(int n, int k, const double *X, int ldx, const double *Y, int ldy, double *out,
+            double *scratch, size_t scratch_elems, cudaStream_t st);
+// out[c] = sum_b partial[b * kmax + c]  (fixed order, deterministic)
+void reduce_partials(const double *partial, int nblocks, int kmax, int k, double *out,
+                     cudaStream_t st);
+void scale_columns(int n, int k, double *X, int ldx, const double *s, cudaStream_t st);
+void copy_f64_to_f32(int n, int k, const double *X, int ldx, float *Y, int ldy, cudaStream_t st);
+void copy_f32_to_f64(int n, int k, const float *X, int ldx, double *Y, int ldy, cudaStream_t st);
+// Y += X (FP32 correction accumulated into an FP64 block)
+void add_f32_to_f64(int n, int k, const float *X, int ldx, double *Y, int ldy, cudaStream_t st);
+void fill_uniform(int n, int k, double *X, int ldx, unsigned long long seed, cudaStream_t st);
+void gather_columns(int n, int k, const double *X, int ldx, const int *idx, double *Y, int ldy,
+                    cudaStream_t st);
+void set_identity(int n, double *X, int ldx, cudaStream_t st);
+void fill_value(size_t count, double *X, double v, cudaStream_t st);
+void scale_columns_strided(int n, int m, double *Y, int ldy, const double *s, int inc,
+                           cudaStream_t st);
+// max |C(i,j)| over an m x w block (device) -> *out (device)
+void absmax(int m, int w, const double *C, int ldc, double *out, cudaStream_t st);
+// rows with mask[i] != 0 of an m x k block set to zero
+void zero_rows(int m, int k, double *X, int ldx, const int *mask, cudaStream_t st);
+// Y(i, j) = X(j, i) for an m x k block (X m x k -> Y k x m)
+void transpose_copy(int m, int k, const double *X, int ldx, double *Y, int ldy, cudaStream_t st);
+// y = a + sigma b over count entries, in double or float
+void shift_values(size_t count, const double *a, const double *b, double sigma, double *y64,
+                  float *y32, cudaStream_t st);
+void copy_cols(int n, int k, const double *X, int ldx, double *Y, int ldy, cudaStream_t st);
+// Stream shared by every library call (created on first use).
+cudaStream_t lib_stream();
+
+
+}  // namespace gcge

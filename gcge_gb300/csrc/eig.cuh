@@ -1,0 +1,28 @@
+// Dense symmetric eigensolver of the Rayleigh-Ritz step (eig.cu).
+#pragma once
+#include "common.cuh"
+
+namespace gcge {
+
+struct EigWork {
+    int cap = 0;
+    int max_rounds = 0;
+    DevBuf<double> G, W, S, C, X, X2, lam, delta, gscr;
+    DevBuf<float2> log;
+    DevBuf<int> info;
+    PinnedBuf<double> h_S, h_C, h_lam, h_info;
+    double last_delta = 0, last_orth = 0;
+    int last_rounds = 0, last_sweeps = 0, last_steps = 0;
+    void reserve(int smax);
+};
+
+size_t jacobi_smem_bytes(int s);
+int jacobi_max_dim();
+
+// Eigenpairs of the symmetric s x s matrix M (device, leading dim ld):
+// ascending eigenvalues to eval_host, orthonormal eigenvectors to Z
+// (device, ldz).  refine_steps Ogita-Aishima steps follow the FP32 Jacobi.
+int sym_eig(EigWork &wk, int s, const double *M, int ld, double *eval_host, double *Z, int ldz,
+            int refine_steps, cudaStream_t st);
+
+}  // namespace gcge

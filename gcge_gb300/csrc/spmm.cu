@@ -1,0 +1,259 @@
+// Sparse kernels on SELL-32 matrices: SpMM over a block of columns, SpMM with
+// a fused per-column dot product (block-PCG p^T w), and the fused residual
+// norm ||(A - lambda_c B) x_c||^2 of CheckConvergence.
+//
+// Layout: one warp owns one 32-row slice; lane l owns row 32*slice + l and
+// walks the slice's entries e = 0..width-1 at slice_ptr + e*32 + l, so each
+// step of the warp reads 32 consecutive column indices / values (one 128-byte
+// line for int32/fp32, two for fp64).  The dense block X is column-major; for
+// a fixed stencil offset the 32 lanes read 32 consecutive x[j] of a column.
+// Every column's accumulator stays in registers, so the matrix is streamed
+// once for all k columns (reference: one column at a time, app/app_ccs.c:120-131).
+#include <algorithm>
+#include <numeric>
+
+#include "common.cuh"
+
+namespace gcge {
+
+constexpr int kSpmmThreads = 128;  // 4 slices per block
+
+int spmm_blocks(const SellPattern &pat) {
+    return (pat.nslices + (kSpmmThreads / 32) - 1) / (kSpmmThreads / 32);
+}
+
+// Host-side SELL construction.  Returns the padded value arrays in host memory
+// (one per input value array) so callers can upload them or derive others.
+void sell_from_csr(int n, const int *ptr, const int *ind, const std::vector<const double *> &vals,
+                   SellPattern &pat, std::vector<std::vector<double>> &out_vals,
+                   std::vector<int> &h_col, std::vector<long long> &h_sp) {
+    const int ns = (n + 31) / 32;
+    h_sp.assign(ns + 1, 0);
+    long long nnz = 0;
+    for (int s = 0; s < ns; ++s) {
+        int w = 0;
+        for (int l = 0; l < 32; ++l) {
+            int r = s * 32 + l;
+            if (r < n) w = std::max(w, ptr[r + 1] - ptr[r]);
+        }
+        h_sp[s + 1] = h_sp[s] + (long long)w * 32;
+    }
+    nnz = ptr[n];
+    const long long padded = h_sp[ns];
+    h_col.assign(padded, 0);
+    out_vals.assign(vals.size(), std::vector<double>(padded, 0.0));
+    for (int s = 0; s < ns; ++s) {
+        const long long base = h_sp[s];
+        const int w = (int)((h_sp[s + 1] - base) / 32);
+        for (int l = 0; l < 32; ++l) {
+            const int r = s * 32 + l;
+            const int rr = r < n ? r : n - 1;
+            const int len = r < n ? ptr[r + 1] - ptr[r] : 0;
+            for (int e = 0; e < w; ++e) {
+                const long long pos = base + (long long)e * 32 + l;
+                if (e < len) {
+                    h_col[pos] = ind[ptr[r] + e];
+                    for (size_t v = 0; v < vals.size(); ++v) out_vals[v][pos] = vals[v][ptr[r] + e];
+                } else {
+                    h_col[pos] = rr;  // padding: own row, zero value
+                }
+            }
+        }
+    }
+    pat.n = n;
+    pat.nslices = ns;
+    pat.nnz = nnz;
+    pat.padded = padded;
+}
+
+void upload_sell(SellPattern &pat, const std::vector<int> &h_col, const std::vector<long long> &h_sp,
+                 cudaStream_t st) {
+    pat.slice_ptr.alloc(h_sp.size());
+    pat.col.alloc(std::max<size_t>(h_col.size(), 1));
+    GCGE_CUDA(cudaMemcpyAsync(pat.slice_ptr.p, h_sp.data(), h_sp.size() * sizeof(long long),
+                              cudaMemcpyHostToDevice, st));
+    if (!h_col.empty())
+        GCGE_CUDA(cudaMemcpyAsync(pat.col.p, h_col.data(), h_col.size() * sizeof(int),
+                                  cudaMemcpyHostToDevice, st));
+}
+
+// ---------------------------------------------------------------- kernels
+template <typename T, int K>
+__global__ void __launch_bounds__(kSpmmThreads)
+k_spmm(const long long *__restrict__ sp, const int *__restrict__ col, const T *__restrict__ val,
+       int n, int nslices, const T *__restrict__ X, int ldx, T *__restrict__ Y, int ldy, int k) {
+    const int slice = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (slice >= nslices) return;
+    const long long beg = sp[slice], end = sp[slice + 1];
+    T acc[K];
+#pragma unroll
+    for (int c = 0; c < K; ++c) acc[c] = T(0);
+    for (long long e = beg + lane; e < end; e += 32) {
+        const int j = __ldg(col + e);
+        const T a = __ldg(val + e);
+        const T *xj = X + j;
+#pragma unroll
+        for (int c = 0; c < K; ++c)
+            if (c < k) acc[c] = fma(a, __ldg(xj + (size_t)c * ldx), acc[c]);
+    }
+    const int row = slice * 32 + lane;
+    if (row < n) {
+#pragma unroll
+        for (int c = 0; c < K; ++c)
+            if (c < k) Y[row + (size_t)c * ldy] = acc[c];
+    }
+}
+
+template <typename T, int K>
+__global__ void __launch_bounds__(kSpmmThreads)
+k_spmm_dot(const long long *__restrict__ sp, const int *__restrict__ col, const T *__restrict__ val,
+           int n, int nslices, const T *__restrict__ X, int ldx, T *__restrict__ Y, int ldy, int k,
+           const int *__restrict__ active, double *__restrict__ partial, int kmax) {
+    __shared__ double red[kSpmmThreads / 32][K];
+    const int slice = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    bool act[K];
+#pragma unroll
+    for (int c = 0; c < K; ++c) act[c] = (c < k) && (active == nullptr || active[c] != 0);
+    T acc[K];
+#pragma unroll
+    for (int c = 0; c < K; ++c) acc[c] = T(0);
+    const int row = slice * 32 + lane;
+    if (slice < nslices) {
+        const long long beg = sp[slice], end = sp[slice + 1];
+        for (long long e = beg + lane; e < end; e += 32) {
+            const int j = __ldg(col + e);
+            const T a = __ldg(val + e);
+            const T *xj = X + j;
+#pragma unroll
+            for (int c = 0; c < K; ++c)
+                if (act[c]) acc[c] = fma(a, __ldg(xj + (size_t)c * ldx), acc[c]);
+        }
+    }
+#pragma unroll
+    for (int c = 0; c < K; ++c) {
+        T v = T(0);
+        if (row < n && act[c]) {
+            Y[row + (size_t)c * ldy] = acc[c];
+            v = X[row + (size_t)c * ldx] * acc[c];
+        }
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+        if (lane == 0) red[warp][c] = (double)v;
+    }
+    __syncthreads();
+    for (int c = threadIdx.x; c < K; c += blockDim.x) {
+        double s = 0.0;
+#pragma unroll
+        for (int w = 0; w < kSpmmThreads / 32; ++w) s += red[w][c];
+        if (c < kmax) partial[(size_t)blockIdx.x * kmax + c] = s;
+    }
+}
+
+template <int K>
+__global__ void __launch_bounds__(kSpmmThreads)
+k_residual(const long long *__restrict__ sp, const int *__restrict__ col,
+           const double *__restrict__ a, const double *__restrict__ b, int n, int nslices,
+           const double *__restrict__ X, int ldx, const double *__restrict__ lam, int k,
+           double *__restrict__ partial, int kmax) {
+    __shared__ double red[kSpmmThreads / 32][K];
+    __shared__ double slam[K];
+    const int slice = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int c = threadIdx.x; c < K; c += blockDim.x) slam[c] = c < k ? lam[c] : 0.0;
+    __syncthreads();
+    double acc[K];
+#pragma unroll
+    for (int c = 0; c < K; ++c) acc[c] = 0.0;
+    const int row = slice * 32 + lane;
+    if (slice < nslices) {
+        const long long beg = sp[slice], end = sp[slice + 1];
+        for (long long e = beg + lane; e < end; e += 32) {
+            const int j = __ldg(col + e);
+            const double av = __ldg(a + e), bv = __ldg(b + e);
+            const double *xj = X + j;
+#pragma unroll
+            for (int c = 0; c < K; ++c)
+                if (c < k) acc[c] = fma(fma(-slam[c], bv, av), __ldg(xj + (size_t)c * ldx), acc[c]);
+        }
+    }
+#pragma unroll
+    for (int c = 0; c < K; ++c) {
+        double v = (row < n && c < k) ? acc[c] * acc[c] : 0.0;
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+        if (lane == 0) red[warp][c] = v;
+    }
+    __syncthreads();
+    for (int c = threadIdx.x; c < K; c += blockDim.x) {
+        double s = 0.0;
+#pragma unroll
+        for (int w = 0; w < kSpmmThreads / 32; ++w) s += red[w][c];
+        if (c < kmax) partial[(size_t)blockIdx.x * kmax + c] = s;
+    }
+}
+
+// ---------------------------------------------------------------- dispatch
+#define GCGE_K_DISPATCH(kk, BODY)                          \
+    do {                                                   \
+        if ((kk) <= 4) { constexpr int KT = 4; BODY; }        \
+        else if ((kk) <= 8) { constexpr int KT = 8; BODY; }   \
+        else if ((kk) <= 16) { constexpr int KT = 16; BODY; } \
+        else if ((kk) <= 24) { constexpr int KT = 24; BODY; } \
+        else if ((kk) <= 32) { constexpr int KT = 32; BODY; } \
+        else { constexpr int KT = 40; BODY; }                 \
+    } while (0)
+
+constexpr int kMaxChunk = 40;
+
+template <typename T>
+void spmm(const SellPattern &pat, const T *val, const T *X, int ldx, T *Y, int ldy, int k,
+          cudaStream_t st) {
+    if (k <= 0 || pat.n == 0) return;
+    const int blocks = spmm_blocks(pat);
+    for (int c0 = 0; c0 < k; c0 += kMaxChunk) {
+        const int kc = std::min(kMaxChunk, k - c0);
+        GCGE_K_DISPATCH(kc, (k_spmm<T, KT><<<blocks, kSpmmThreads, 0, st>>>(
+                                pat.slice_ptr.p, pat.col.p, val, pat.n, pat.nslices,
+                                X + (size_t)c0 * ldx, ldx, Y + (size_t)c0 * ldy, ldy, kc)));
+        GCGE_CHECK_LAUNCH();
+        count_launch();
+    }
+}
+
+template <typename T>
+int spmm_dot(const SellPattern &pat, const T *val, const T *X, int ldx, T *Y, int ldy, int k,
+             const int *active, double *partial, int kmax, cudaStream_t st) {
+    GCGE_REQUIRE(k <= kMaxChunk && k <= kmax, GCGE_ERR_ARG, "spmm_dot: too many columns");
+    const int blocks = spmm_blocks(pat);
+    if (k <= 0) return 0;
+    GCGE_K_DISPATCH(k, (k_spmm_dot<T, KT><<<blocks, kSpmmThreads, 0, st>>>(
+                           pat.slice_ptr.p, pat.col.p, val, pat.n, pat.nslices, X, ldx, Y, ldy,
+                           k, active, partial, kmax)));
+    GCGE_CHECK_LAUNCH();
+    count_launch();
+    return blocks;
+}
+
+int residual_norms(const SellPattern &pat, const double *a, const double *b, const double *X,
+                   int ldx, const double *lam, int k, double *partial, int kmax, cudaStream_t st) {
+    GCGE_REQUIRE(k <= kMaxChunk && k <= kmax, GCGE_ERR_ARG, "residual_norms: too many columns");
+    const int blocks = spmm_blocks(pat);
+    if (k <= 0) return 0;
+    GCGE_K_DISPATCH(k, (k_residual<KT><<<blocks, kSpmmThreads, 0, st>>>(
+                           pat.slice_ptr.p, pat.col.p, a, b, pat.n, pat.nslices, X, ldx, lam, k,
+                           partial, kmax)));
+    GCGE_CHECK_LAUNCH();
+    count_launch();
+    return blocks;
+}
+
+template void spmm<double>(const SellPattern &, const double *, const double *, int, double *,
+                           int, int, cudaStream_t);
+template void spmm<float>(const SellPattern &, const float *, const float *, int, float *, int,
+                          int, cudaStream_t);
+template int spmm_dot<double>(const SellPattern &, const double *, const double *, int, double *,
+                              int, int, const int *, double *, int, cudaStream_t);
+template int spmm_dot<float>(const SellPattern &, const float *, const float *, int, float *, int,
+                             int, const int *, double *, int, cudaStream_t);
+
+}  // namespace gcge

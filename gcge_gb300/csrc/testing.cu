@@ -1,0 +1,95 @@
+// Component entry points: the dense eigensolver, the block-PCG inner solve
+// and the B-orthonormalisation, each callable on its own through the C ABI so
+// they can be checked against the CPU oracle in isolation.
+#include <cstring>
+
+#include "gcg.cuh"
+
+using namespace gcge;
+
+extern "C" {
+
+int GCGE_DenseEig(int s, const double *M, int ldm, double *eval, double *Z, int ldz) {
+    try {
+        GCGE_REQUIRE(s >= 1 && M && eval && Z && ldm >= s && ldz >= s, GCGE_ERR_ARG,
+                     "GCGE_DenseEig: arguments");
+        cudaStream_t st = lib_stream();
+        EigWork wk;
+        wk.reserve(s);
+        DevBuf<double> dM, dZ;
+        dM.alloc((size_t)s * s);
+        dZ.alloc((size_t)s * s);
+        GCGE_CUDA(cudaMemcpy2DAsync(dM.p, sizeof(double) * s, M, sizeof(double) * ldm,
+                                    sizeof(double) * s, s, cudaMemcpyHostToDevice, st));
+        sym_eig(wk, s, dM.p, s, eval, dZ.p, s, 8, st);
+        GCGE_CUDA(cudaMemcpy2DAsync(Z, sizeof(double) * ldz, dZ.p, sizeof(double) * s,
+                                    sizeof(double) * s, s, cudaMemcpyDeviceToHost, st));
+        GCGE_CUDA(cudaStreamSynchronize(st));
+        return GCGE_OK;
+    } catch (const CudaError &e) {
+        set_error(e.status, e.where.c_str());
+        take_error();
+        return e.status;
+    }
+}
+
+int GCGE_BlockPCG(void *A, void *B, double sigma, void **b, void **x, int k, int max_iter,
+                  double rate, double tol, int fp32, int *iters) {
+    try {
+        SparseMat *Am = as_mat(A);
+        SparseMat *Bm = B ? as_mat(B) : nullptr;
+        MultiVec *bv = as_mv(b), *xv = as_mv(x);
+        GCGE_REQUIRE(Am && (!B || Bm) && bv && xv, GCGE_ERR_HANDLE, "GCGE_BlockPCG: handles");
+        GCGE_REQUIRE(k >= 1 && k <= kPcgMaxCols && k <= bv->ncols && k <= xv->ncols, GCGE_ERR_ARG,
+                     "GCGE_BlockPCG: k");
+        cudaStream_t st = lib_stream();
+        SolverCtx c;
+        prepare_union(c, Am, Bm, st);
+        c.reserve(Am->n, k, k, k, spmm_blocks(c.upat));
+        shift_values(c.upat.padded, c.ua.p, c.ub.p, sigma, fp32 ? nullptr : c.us64.p,
+                     fp32 ? c.us32.p : nullptr, st);
+        const int n = Am->n, ld = c.ld;
+        int it = 0;
+        if (!fp32) {
+            it = block_pcg<double>(c.pcg, c.upat, c.us64.p, bv->data, bv->ld, xv->data, xv->ld,
+                                   c.r64.p, c.p64.p, c.w64.p, ld, k, max_iter, rate, tol, false, st);
+        } else {
+            DevBuf<float> x32, b32, r32, p32, w32;
+            for (auto *bb : {&x32, &b32, &r32, &p32, &w32}) bb->alloc((size_t)ld * k);
+            copy_f64_to_f32(n, k, xv->data, xv->ld, x32.p, ld, st);
+            copy_f64_to_f32(n, k, bv->data, bv->ld, b32.p, ld, st);
+            it = block_pcg<float>(c.pcg, c.upat, c.us32.p, b32.p, ld, x32.p, ld, r32.p, p32.p,
+                                  w32.p, ld, k, max_iter, rate, tol, false, st);
+            copy_f32_to_f64(n, k, x32.p, ld, xv->data, xv->ld, st);
+        }
+        GCGE_CUDA(cudaStreamSynchronize(st));
+        if (iters) *iters = it;
+        return GCGE_OK;
+    } catch (const CudaError &e) {
+        set_error(e.status, e.where.c_str());
+        take_error();
+        return e.status;
+    }
+}
+
+int GCGE_BOrth(void *B, void **x, int start, int *end, double zero_tol, int max_reorth) {
+    try {
+        SparseMat *Bm = B ? as_mat(B) : nullptr;
+        MultiVec *xv = as_mv(x);
+        GCGE_REQUIRE((!B || Bm) && xv && end, GCGE_ERR_HANDLE, "GCGE_BOrth: handles");
+        GCGE_REQUIRE(start >= 0 && *end >= start && *end <= xv->ncols, GCGE_ERR_ARG,
+                     "GCGE_BOrth: range");
+        SolverCtx c;
+        c.reserve(xv->nrows, xv->ncols, xv->ncols, 1, 1);
+        *end = borth(c, Bm, xv->data, xv->ld, xv->nrows, start, *end, Bm != nullptr, zero_tol,
+                     max_reorth, nullptr);
+        GCGE_CUDA(cudaStreamSynchronize(lib_stream()));
+        return GCGE_OK;
+    } catch (const CudaError &e) {
+        set_error(e.status, e.where.c_str());
+        take_error();
+        return e.status;
+    }
+}
+
+}  // extern "C"

@@ -1,0 +1,151 @@
+/*
+ * gcge_cuda.h - CUDA (sm_103a) backend and solver entry points of the GB300
+ * GCGE library (libgcge_cuda.so).  Plain C ABI: pointers, sizes, status codes.
+ *
+ * Drop-in map (reference interface each entry replaces):
+ *   OPS_CUDA_Set                 <- OPS_CCS_Set            app/app_ccs.c:213-249
+ *   CUDA_MatCreateFromCCS        <- filling a CCSMAT        app/app_ccs.h:20-24
+ *   CUDA_MultiVecSetFromHost /
+ *   CUDA_MultiVecGetToHost       <- direct LAPACKVEC.data access (app/app_lapack.h:17-20);
+ *                                   device multivectors are opaque
+ *   GCGE_Solve                   <- the EigenSolverSetup_GCG + GCGE_Setparameters +
+ *                                   ops->EigenSolver sequence of gcge.c:490-531
+ *                                   (the reference has no single GCGE_Solve symbol)
+ * OPS slots filled by OPS_CUDA_Set (semantics of app_ccs + app_lapack):
+ *   MatDotMultiVec, MatTransDotMultiVec   app/app_ccs.c:50-150 (mat NULL -> copy)
+ *   MultiVecAxpby                         app/app_lapack.c:334-395
+ *   MultiVecLinearComb                    app/app_lapack.c:463-534
+ *   MultiVecInnerProd / LocalInnerProd    app/app_lapack.c:299-321 + DenseMatQtAP :64-183
+ *   MultiVecQtAP                          src/ops_multi_vec.c:351-411 (fused on device)
+ *   MultiVecCreateByMat/ByVec/ByMultiVec, MultiVecDestroy, MultiVecView,
+ *   MultiVecSetRandomValue, Get/RestoreVecFromMultiVec, Vec* single-vector ops
+ *                                         app/app_lapack.c:230-650
+ */
+#ifndef GCGE_CUDA_H
+#define GCGE_CUDA_H
+
+#include <stddef.h>
+#include "gcge_ops.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Status codes returned by every int-valued entry point and recorded as the
+ * sticky status of the void OPS slots. */
+enum {
+    GCGE_OK = 0,
+    GCGE_ERR_CUDA = 1,        /* a CUDA runtime call failed */
+    GCGE_ERR_ARG = 2,         /* invalid argument (size, range, NULL) */
+    GCGE_ERR_ALLOC = 3,       /* device or host allocation failed */
+    GCGE_ERR_HANDLE = 4,      /* handle is not a CUDA matrix / multivector */
+    GCGE_ERR_NUMERIC = 5,     /* NaN/Inf detected in residuals or projections */
+    GCGE_ERR_NOT_CONVERGED = 6, /* numIterMax reached before nev pairs converged */
+    GCGE_ERR_NO_DEVICE = 7,   /* no CUDA device visible */
+    GCGE_ERR_TOO_LARGE = 8    /* projected problem exceeds the dense-solver capacity */
+};
+
+/* Sticky error of the OPS slots and setup calls on this thread (0 = none);
+ * reading it clears it. */
+int ops_cuda_last_error(void);
+const char *ops_cuda_error_string(int status);
+/* Text of the most recent error recorded by any entry point (where it was
+ * raised and the CUDA message, if any); not cleared by ops_cuda_last_error. */
+const char *ops_cuda_last_error_detail(void);
+
+/* ---- backend --------------------------------------------------------- */
+void OPS_CUDA_Set(struct OPS_ *ops);
+
+/* Device matrix from host CCS arrays of an n x n matrix (int32 indices, FP64
+ * values; j_col[n+1], i_row[nnz], data[nnz]).  The data are copied to HBM.
+ * Like app_ccs, MatTransDotMultiVec assumes the matrix is symmetric
+ * (app/app_ccs.c:140-150). */
+int CUDA_MatCreateFromCCS(void **mat, int nrows, int ncols, const int *j_col, const int *i_row,
+                          const double *data);
+void CUDA_MatDestroy(void **mat);
+int CUDA_MatNnz(void *mat, long long *nnz);
+
+/* Copy columns [start, end) between a device multivector and a host
+ * column-major array with leading dimension ldh >= nrows. */
+int CUDA_MultiVecSetFromHost(void **mv, int start, int end, const double *host, int ldh);
+int CUDA_MultiVecGetToHost(void **mv, int start, int end, double *host, int ldh);
+int CUDA_MultiVecSize(void **mv, int *nrows, int *ncols);
+
+/* ---- GCG solve -------------------------------------------------------- */
+enum { GCGE_PREC_FP64 = 0, GCGE_PREC_MIXED = 1 };
+
+/* Precision of the GPU GCG installed on this ops (default GCGE_PREC_FP64).
+ * MIXED runs the block-PCG inner solve and its SpMM with FP32 values, int32
+ * indices and FP32 accumulation; residuals, B-orthogonalisation, Rayleigh-Ritz
+ * and the dense eigensolve stay FP64. */
+int GCGE_SetPrecision(struct OPS_ *ops, int precision);
+
+typedef struct gcge_solve_info {
+    int nconv;          /* locked (converged) pairs, may exceed nev */
+    int niter;          /* outer GCG iterations */
+    int status;         /* GCGE_OK / GCGE_ERR_NOT_CONVERGED / ... */
+    int pcg_iters;      /* total inner block-PCG iterations */
+    int spmm_calls;     /* SpMM launches */
+    int kernel_launches;/* all kernels launched by the solve */
+    double seconds;     /* wall time of the solve on the host clock */
+    double phase_ms[10];/* checkconv, compP, compRR, rr_matW, eig, compRV, compW, linsol,
+                           compX, initX (CUDA events on the solver stream) */
+} gcge_solve_info;
+
+/* One-call solve of A x = lambda B x for the nev smallest pairs from host
+ * CCS arrays (B may be NULL = identity).  X0 (n x nev_given, column-major,
+ * may be NULL when nev_given = 0) seeds the first columns of the basis.
+ * tol = {abs, rel}; convergence is ||A x - lambda B x||_2 <= tol[0] and
+ * <= |lambda| tol[1] with x B-normalised (src/ops_eig_sol_gcg.c:239-240).
+ * gap_min and auto_shift are the GCGE_Setparameters arguments.
+ * eval[nev_max], evec[n x nev_max] (column-major) receive the solver's
+ * eval/evec arrays; info may be NULL. */
+int GCGE_Solve(int n, const int *a_colptr, const int *a_rowind, const double *a_val,
+               const int *b_colptr, const int *b_rowind, const double *b_val, int nev,
+               int block_size, int nev_init, int nev_max, int max_iter, const double tol[2],
+               double gap_min, int auto_shift, int precision, const double *X0, int nev_given,
+               double *eval, double *evec, gcge_solve_info *info);
+
+/* Statistics of the last ops->EigenSolver call on this ops. */
+int GCGE_GetSolveInfo(struct OPS_ *ops, gcge_solve_info *info);
+
+/* ---- device-resident benchmarking helpers ------------------------------
+ * A prepared problem keeps A, B, the initial block and all solver state in
+ * HBM so repeated solves time only the device work. */
+typedef struct gcge_prepared gcge_prepared;
+int GCGE_Prepare(gcge_prepared **prep, int n, const int *a_colptr, const int *a_rowind,
+                 const double *a_val, const int *b_colptr, const int *b_rowind,
+                 const double *b_val, int nev, int block_size, int nev_init, int nev_max,
+                 int max_iter, const double tol[2], double gap_min, int auto_shift,
+                 int precision, const double *X0, int nev_given);
+/* Solve with device-resident inputs; eval (host, nev_max) is copied back,
+ * eigenvectors stay on the device unless evec is non-NULL. */
+int GCGE_PreparedSolve(gcge_prepared *prep, double *eval, double *evec, gcge_solve_info *info);
+void GCGE_PreparedDestroy(gcge_prepared **prep);
+
+/* ---- kernel-level entry points used by the measurement harness ---------
+ * SpMM of k columns, Y = M X, on device buffers owned by the library.
+ * Timed with CUDA events on the library stream; returns average ms/launch. */
+int GCGE_BenchSpMM(void *mat, int k, int fp32, int reps, double *ms_per_launch,
+                   double *bytes_per_launch);
+
+/* ---- component entry points (each step of the solver on its own) -------
+ * Dense symmetric eigensolve of the Rayleigh-Ritz step (replaces dsyevx,
+ * src/ops_eig_sol_gcg.c:1145-1150): host M (s x s, ldm) -> ascending eval[s]
+ * and orthonormal eigenvectors Z (s x s, ldz). */
+int GCGE_DenseEig(int s, const double *M, int ldm, double *eval, double *Z, int ldz);
+/* Block CG on (A + sigma B) x = b for columns [0, k) of device multivectors
+ * b and x (x holds the initial guess), with the stopping rule of BlockPCG
+ * (src/ops_lin_sol.c:383-394, absolute tolerance); fp32 selects the mixed
+ * precision path. */
+int GCGE_BlockPCG(void *A, void *B, double sigma, void **b, void **x, int k, int max_iter,
+                  double rate, double tol, int fp32, int *iters);
+/* B-orthonormalise columns [start, *end) of x against [0, start) (B NULL =
+ * identity), as MultiVecOrth does (src/ops_orth.c:203-394); *end shrinks by
+ * the number of dependent columns dropped. */
+int GCGE_BOrth(void *B, void **x, int start, int *end, double zero_tol, int max_reorth);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* GCGE_CUDA_H */

@@ -1,0 +1,170 @@
+/*
+ * gcge_ops.h - the OPS plugin surface of GCGE, as exported by the GB300
+ * library (libgcge_cuda.so).
+ *
+ * `struct OPS_` reproduces the reference's vtable member for member
+ * (src/ops.h:43-152) so that code written against the reference's OPS can
+ * fill it with the CUDA backend (OPS_CUDA_Set, see gcge_cuda.h) and call the
+ * GPU GCG through the same entry points.  `GCGSolver` reproduces
+ * src/ops_eig_sol_gcg.h:21-52 so that callers that read
+ * ((GCGSolver *)ops->eigen_solver_workspace)->numIter (gcge.c:523) keep
+ * working.  Both layouts are ABI contracts and must not be reordered.
+ *
+ * All functions keep the reference's signatures: they return void, take
+ * half-open column ranges start[2]/end[2] ([0] = source x, [1] = destination
+ * y), host coefficient arrays (column-major, leading dimension ldc/ldIP) and
+ * opaque matrix/multivector handles.  Errors are recorded in a sticky status
+ * (ops_cuda_last_error(), gcge_cuda.h) instead of assert().
+ */
+#ifndef GCGE_OPS_H
+#define GCGE_OPS_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* src/ops.h:43-152 */
+typedef struct OPS_ {
+    void   (*Printf)(const char *fmt, ...);
+    double (*GetWtime)(void);
+    int    (*GetOptionFromCommandLine)(const char *name, char type, void *data,
+                                       int argc, char *argv[], struct OPS_ *ops);
+    /* mat */
+    void (*MatView)(void *mat, struct OPS_ *ops);
+    void (*MatAxpby)(double alpha, void *matX, double beta, void *matY, struct OPS_ *ops);
+    /* vec */
+    void (*VecCreateByMat)(void **des_vec, void *src_mat, struct OPS_ *ops);
+    void (*VecCreateByVec)(void **des_vec, void *src_vec, struct OPS_ *ops);
+    void (*VecDestroy)(void **des_vec, struct OPS_ *ops);
+    void (*VecView)(void *x, struct OPS_ *ops);
+    void (*VecInnerProd)(void *x, void *y, double *inner_prod, struct OPS_ *ops);
+    void (*VecLocalInnerProd)(void *x, void *y, double *inner_prod, struct OPS_ *ops);
+    void (*VecSetRandomValue)(void *x, struct OPS_ *ops);
+    void (*VecAxpby)(double alpha, void *x, double beta, void *y, struct OPS_ *ops);
+    void (*MatDotVec)(void *mat, void *x, void *y, struct OPS_ *ops);
+    void (*MatTransDotVec)(void *mat, void *x, void *y, struct OPS_ *ops);
+    /* multi-vec */
+    void (*MultiVecCreateByMat)(void ***multi_vec, int num_vec, void *src_mat, struct OPS_ *ops);
+    void (*MultiVecCreateByVec)(void ***multi_vec, int num_vec, void *src_vec, struct OPS_ *ops);
+    void (*MultiVecCreateByMultiVec)(void ***multi_vec, int num_vec, void **src_mv, struct OPS_ *ops);
+    void (*MultiVecDestroy)(void ***multi_vec, int num_vec, struct OPS_ *ops);
+    void (*GetVecFromMultiVec)(void **multi_vec, int col, void **vec, struct OPS_ *ops);
+    void (*RestoreVecForMultiVec)(void **multi_vec, int col, void **vec, struct OPS_ *ops);
+    void (*MultiVecView)(void **x, int start, int end, struct OPS_ *ops);
+    void (*MultiVecLocalInnerProd)(char nsdIP, void **x, void **y, int is_vec, int *start,
+                                   int *end, double *inner_prod, int ldIP, struct OPS_ *ops);
+    void (*MultiVecInnerProd)(char nsdIP, void **x, void **y, int is_vec, int *start, int *end,
+                              double *inner_prod, int ldIP, struct OPS_ *ops);
+    void (*MultiVecSetRandomValue)(void **multi_vec, int start, int end, struct OPS_ *ops);
+    void (*MultiVecAxpby)(double alpha, void **x, double beta, void **y, int *start, int *end,
+                          struct OPS_ *ops);
+    void (*MultiVecLinearComb)(void **x, void **y, int is_vec, int *start, int *end,
+                               double *coef, int ldc, double *beta, int incb, struct OPS_ *ops);
+    void (*MatDotMultiVec)(void *mat, void **x, void **y, int *start, int *end, struct OPS_ *ops);
+    void (*MatTransDotMultiVec)(void *mat, void **x, void **y, int *start, int *end,
+                                struct OPS_ *ops);
+    void (*MultiVecQtAP)(char ntsA, char ntsdQAP, void **mvQ, void *matA, void **mvP, int is_vec,
+                         int *start, int *end, double *qAp, int ldQAP, void **mv_ws,
+                         struct OPS_ *ops);
+    /* dense matrix ops */
+    struct OPS_ *lapack_ops;
+    void (*DenseMatQtAP)(char ntluA, char nsdC, int nrowsA, int ncolsA, int nrowsC, int ncolsC,
+                         double alpha, double *matQ, int ldQ, double *matA, int ldA,
+                         double *matP, int ldP, double beta, double *matC, int ldC,
+                         double *dbl_ws);
+    void (*DenseMatOrth)(double *mat, int nrows, int ldm, int start, int *end,
+                         double orth_zero_tol, double *dbl_ws, int length, int *int_ws);
+    /* linear solver */
+    void (*LinearSolver)(void *mat, void *b, void *x, struct OPS_ *ops);
+    void *linear_solver_workspace;
+    void (*MultiLinearSolver)(void *mat, void **b, void **x, int *start, int *end,
+                              struct OPS_ *ops);
+    void *multi_linear_solver_workspace;
+    /* orthonormal */
+    void (*MultiVecOrth)(void **x, int start_x, int *end_x, void *B, struct OPS_ *ops);
+    void *orth_workspace;
+    /* multigrid */
+    void (*MultiGridCreate)(void ***A_array, void ***B_array, void ***P_array, int *num_levels,
+                            void *A, void *B, struct OPS_ *ops);
+    void (*MultiGridDestroy)(void ***A_array, void ***B_array, void ***P_array, int *num_levels,
+                             struct OPS_ *ops);
+    void (*VecFromItoJ)(void **P_array, int level_i, int level_j, void *vec_i, void *vec_j,
+                        void **vec_ws, struct OPS_ *ops);
+    void (*MultiVecFromItoJ)(void **P_array, int level_i, int level_j, void **multi_vec_i,
+                             void **multi_vec_j, int *startIJ, int *endIJ, void ***multi_vec_ws,
+                             struct OPS_ *ops);
+    /* eigen solver */
+    void (*EigenSolver)(void *A, void *B, double *eval, void **evec, int nevGiven, int *nevConv,
+                        struct OPS_ *ops);
+    void *eigen_solver_workspace;
+    struct OPS_ *app_ops;
+} OPS;
+
+/* src/ops_eig_sol_gcg.h:21-52 */
+typedef struct GCGSolver_ {
+    void *A; void *B; double sigma;
+    double *eval; void **evec;
+    int nevMax; double gapMin;
+    int nevInit; int nevGiven; int nevConv;
+    int block_size; double tol[2]; int numIterMax;
+    int numIter; int sizeV;
+    void **mv_ws[4]; double *dbl_ws; int *int_ws;
+    int length_dbl_ws;
+    int print; int printtime;
+    int user_defined_multi_linear_solver;
+    int check_conv_max_num;
+    char initX_orth_method[8]; int initX_orth_block_size;
+    int initX_orth_max_reorth; double initX_orth_zero_tol;
+    char compP_orth_method[8]; int compP_orth_block_size;
+    int compP_orth_max_reorth; double compP_orth_zero_tol;
+    char compW_orth_method[8]; int compW_orth_block_size;
+    int compW_orth_max_reorth; double compW_orth_zero_tol;
+    int compW_cg_max_iter; double compW_cg_rate;
+    double compW_cg_tol; char compW_cg_tol_type[8];
+    int compW_cg_auto_shift; double compW_cg_shift;
+    int compW_cg_order;
+    int compRR_min_num; double compRR_min_gap;
+    double compRR_tol;
+} GCGSolver;
+
+/* OPS lifetime: src/ops.c:26-149.  OPS_Setup fills Printf/GetWtime/
+ * GetOptionFromCommandLine defaults; the GPU GCG needs no lapack_ops. */
+void OPS_Create(OPS **ops);
+void OPS_Setup(OPS *ops);
+void OPS_Destroy(OPS **ops);
+
+/* GCG entry points: src/ops_eig_sol_gcg.c:1565-1628 (Setup), :1684-1741
+ * (SetParameters), :1865-1877 (GCGE_Create), :1878-1918 (GCGE_Setparameters),
+ * :1919-1927 (GCGE_Destroymvws), :1630-1680 (workspace create/destroy).
+ * EigenSolverSetup_GCG installs the GPU GCG as ops->EigenSolver; the
+ * multivector workspaces must come from a CUDA-backed ops (OPS_CUDA_Set).
+ * dbl_ws / int_ws are accepted for signature compatibility; the GPU solver
+ * keeps its small dense state in its own per-ops context. */
+void EigenSolverSetup_GCG(double gapMin, int nevInit, int nevMax, int block_size, double tol[2],
+                          int numIterMax, int print, int printtime,
+                          int user_defined_multi_linear_solver, void **mv_ws[4], double *dbl_ws,
+                          int *int_ws, struct OPS_ *ops);
+void EigenSolverCreateWorkspace_GCG(int nevInit, int nevMax, int block_size, void *mat,
+                                    void ***mv_ws, double **dbl_ws, int **int_ws,
+                                    struct OPS_ *ops);
+void EigenSolverDestroyWorkspace_GCG(int nevInit, int nevMax, int block_size, void *mat,
+                                     void ***mv_ws, double **dbl_ws, int **int_ws,
+                                     struct OPS_ *ops);
+void EigenSolverSetParameters_GCG(
+    int check_conv_max_num, const char *initX_orth_method, int initX_orth_block_size,
+    int initX_orth_max_reorth, double initX_orth_zero_tol, const char *compP_orth_method,
+    int compP_orth_block_size, int compP_orth_max_reorth, double compP_orth_zero_tol,
+    const char *compW_orth_method, int compW_orth_block_size, int compW_orth_max_reorth,
+    double compW_orth_zero_tol, int compW_cg_max_iter, double compW_cg_rate, double compW_cg_tol,
+    const char *compW_cg_tol_type, int compW_cg_auto_shift, int compRR_min_num,
+    double compRR_min_gap, double compRR_tol, struct OPS_ *ops);
+void GCGE_Create(void *A, int nevMax, int block_size, int nevInit, void ***gcg_mv_ws,
+                 double *dbl_ws, int *int_ws, struct OPS_ *ops);
+void GCGE_Setparameters(double gapMin, int shift, struct OPS_ *ops);
+void GCGE_Destroymvws(void ***gcg_mv_ws, double *dbl_ws, int *int_ws, int nevMax, int block_size,
+                      struct OPS_ *ops);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* GCGE_OPS_H */

@@ -1,0 +1,64 @@
+import json
+import os
+import sys
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+GOLDEN_DIR = os.path.join(ROOT, "tests", "golden")
+
+
+def pytest_configure(config):
+    config.addinivalue_line("markers", "gpu: needs a CUDA GPU (GB300, sm_103a)")
+
+
+@pytest.fixture(scope="session")
+def golden():
+    with open(os.path.join(GOLDEN_DIR, "golden.json")) as f:
+        return json.load(f)
+
+
+@pytest.fixture(scope="session")
+def golden_vectors():
+    return dict(np.load(os.path.join(GOLDEN_DIR, "golden_vectors.npz")))
+
+
+def build_case(name):
+    """The generator call of each golden case (mirrors tests/golden/make_golden.py)."""
+    sys.path.insert(0, os.path.join(ROOT, "tests", "golden"))
+    from make_golden import cases
+    builder = cases()[name][0]
+    return builder()
+
+
+@pytest.fixture(scope="session")
+def gpu_lib():
+    import gcge_gb300 as G
+    G.load()
+    return G
+
+
+def cluster_subspace_angle(evals, V1, V2, B=None, rel_gap=1e-6):
+    """Largest principal angle (radians) between V1 and V2 over clusters of
+    nearly equal eigenvalues (subspaces are compared cluster by cluster, so
+    degenerate eigenvalues do not need matching eigenvectors).  Columns are
+    B-orthonormal; the angle is measured in the B inner product."""
+    k = V1.shape[1]
+    worst = 0.0
+    i = 0
+    BV2 = V2 if B is None else B @ V2
+    while i < k:
+        j = i + 1
+        while j < k and abs(evals[j] - evals[j - 1]) <= rel_gap * abs(evals[j]):
+            j += 1
+        if j == k and i > 0 and j - i > 0:
+            pass
+        C = V1[:, i:j].T @ BV2[:, i:j]
+        s = np.linalg.svd(C, compute_uv=False)
+        worst = max(worst, float(np.arccos(np.clip(s.min(), -1.0, 1.0))))
+        i = j
+    return worst

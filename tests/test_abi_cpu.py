@@ -1,0 +1,100 @@
+"""C-ABI checks that need no GPU: the library loads and exports every entry
+point the headers declare, and the OPS / GCGSolver layouts match the
+reference's (so reference-side code can fill and read them)."""
+import ctypes
+import os
+import re
+import shutil
+import subprocess
+
+import pytest
+
+import gcge_gb300 as G
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+INC = os.path.join(ROOT, "include")
+
+
+def header_functions():
+    names = set()
+    for h in ("gcge_ops.h", "gcge_cuda.h"):
+        txt = open(os.path.join(INC, h)).read()
+        txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+        txt = re.sub(r"typedef struct OPS_ \{.*?\} OPS;", "", txt, flags=re.S)
+        txt = re.sub(r"typedef struct GCGSolver_ \{.*?\} GCGSolver;", "", txt, flags=re.S)
+        for m in re.finditer(r"^\s*(?:const\s+)?[A-Za-z_][\w\s\*]*?\b([A-Za-z_]\w*)\s*\(", txt, re.M):
+            name = m.group(1)
+            if name not in ("if", "while", "sizeof", "defined"):
+                names.add(name)
+    return sorted(names)
+
+
+@pytest.fixture(scope="module")
+def lib():
+    if not os.path.exists(G.lib_path()):
+        from gcge_gb300.build import build
+        build()
+    return G.load()
+
+
+def test_every_declared_symbol_is_exported(lib):
+    declared = header_functions()
+    assert len(declared) >= 30
+    missing = [n for n in declared if not hasattr(lib, n)]
+    assert missing == []
+    assert set(declared) <= set(G.EXPORTED_SYMBOLS) | {"OPS_Create", "OPS_Setup", "OPS_Destroy"}
+
+
+def test_status_strings(lib):
+    f = lib.ops_cuda_error_string
+    f.restype = ctypes.c_char_p
+    assert f(0) == b"ok"
+    assert b"converged" in f(6)
+
+
+def test_ops_create_and_cuda_set_without_gpu(lib):
+    ops = ctypes.POINTER(G.OPSStruct)()
+    lib.OPS_Create(ctypes.byref(ops))
+    lib.OPS_CUDA_Set(ops)
+    lib.OPS_Setup(ops)
+    o = ops.contents
+    for slot in ("MatDotMultiVec", "MultiVecAxpby", "MultiVecLinearComb", "MultiVecInnerProd",
+                 "MultiVecQtAP", "MultiVecCreateByMat", "MultiVecDestroy", "Printf", "GetWtime"):
+        assert getattr(o, slot), slot
+    assert o.MatAxpby is None and o.EigenSolver is None
+    lib.OPS_Destroy(ctypes.byref(ops))
+
+
+LAYOUT_PROBE = r"""
+#include <stdio.h>
+#include <stddef.h>
+#include HEADER
+int main(void) {
+    printf("%zu %zu %zu %zu %zu %zu %zu %zu\n", sizeof(OPS), offsetof(OPS, MultiVecQtAP),
+           offsetof(OPS, EigenSolver), offsetof(OPS, app_ops), sizeof(GCGSolver),
+           offsetof(GCGSolver, numIter), offsetof(GCGSolver, compW_cg_tol_type),
+           offsetof(GCGSolver, compRR_tol));
+    return 0;
+}
+"""
+
+
+def _probe(tmp_path, header, incs):
+    src = tmp_path / "probe.c"
+    src.write_text(LAYOUT_PROBE.replace("HEADER", header))
+    exe = tmp_path / "probe"
+    cmd = ["gcc", "-w", str(src), "-o", str(exe)] + [f"-I{d}" for d in incs]
+    subprocess.run(cmd, check=True, capture_output=True)
+    return subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.split()
+
+
+@pytest.mark.skipif(shutil.which("gcc") is None, reason="gcc not available")
+def test_layout_matches_reference_headers(tmp_path):
+    ours = _probe(tmp_path, '"gcge_ops.h"', [INC])
+    assert int(ours[0]) == 46 * 8 and int(ours[3]) == 45 * 8
+    ref_src = "/root/reference/src"
+    if not os.path.isdir(ref_src):
+        pytest.skip("reference headers not mounted here")
+    ref = _probe(tmp_path, '"ops_eig_sol_gcg.h"',
+                 [os.path.join(ROOT, "oracle", "ref"), ref_src, "/root/reference/app"])
+    assert ours == ref

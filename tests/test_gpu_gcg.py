@@ -1,0 +1,98 @@
+"""End-to-end parity of the GPU GCG with the reference GCGE CPU path on the
+same seeded inputs: eigenvalues within 1e-10 relative of the reference's
+(golden fixtures made by its own C sources), eigenvector subspaces within
+1e-6 rad per cluster, every residual under the requested tolerance."""
+import numpy as np
+import pytest
+
+from conftest import build_case, cluster_subspace_angle
+from gcge_gb300 import problems as P
+from oracle.gcg_oracle import gcg_solve, residuals
+
+pytestmark = pytest.mark.gpu
+
+CASES = ["laplace2d_24x24_nev8", "laplace2d_24x24_noshift", "laplace2d_20x20_abstol",
+         "laplace2d_128x128_nev20_bs20", "laplace2d_128x128_nev20_rule", "laplace3d_mass_16",
+         "laplace3d_mass_24", "vardiff3d_12", "aniso2d_40x30_eps10_diagB", "rgg_2000_deg10"]
+
+
+def run_gpu(G, case, g, precision=0):
+    A, B = build_case(case)
+    X0 = P.initial_block(A.n, g["nev_init"], seed=g["x0_seed"])
+    r = G.solve(A, B, g["nev"], g["block_size"], g["nev_init"], g["nev_max"], X0=X0,
+                tol=tuple(g["tol"]), max_iter=g["max_iter"], gap_min=g["gap_min"],
+                auto_shift=g["auto_shift"], precision=precision)
+    return A, B, r
+
+
+@pytest.mark.parametrize("case", CASES)
+def test_gcg_matches_reference(gpu_lib, golden, golden_vectors, case):
+    g = golden[case]
+    A, B, r = run_gpu(gpu_lib, case, g)
+    nev = g["nev"]
+    ref = np.array(g["eval"][:nev])
+    assert r.status == gpu_lib.GCGE_OK
+    assert r.nconv >= nev
+    rel = np.abs(r.eval[:nev] - ref) / np.abs(ref)
+    assert rel.max() < 1e-10, rel.max()
+    Bs = None if B is None else B.to_scipy()
+    res, relres = residuals(A.to_scipy(), Bs, r.eval[:nev], r.evec[:, :nev])
+    tol0, tol1 = g["tol"]
+    assert np.all(res <= tol0 * 1.001) and np.all(relres <= tol1 * 1.001)
+    if case in golden_vectors:
+        ang = cluster_subspace_angle(r.eval[:nev], r.evec[:, :nev], golden_vectors[case], Bs)
+        assert ang < 1e-6, ang
+    # B-orthonormal eigenvectors
+    V = r.evec[:, :nev]
+    BV = V if Bs is None else Bs @ V
+    assert np.abs(V.T @ BV - np.eye(nev)).max() < 1e-9
+    # iteration count close to the reference's
+    assert abs(r.niter - g["niter"]) <= max(4, g["niter"] // 4), (r.niter, g["niter"])
+
+
+def test_analytic_spectrum_config1(gpu_lib, golden):
+    g = golden["laplace2d_128x128_nev20_bs20"]
+    A, B, r = run_gpu(gpu_lib, "laplace2d_128x128_nev20_bs20", g)
+    k = np.arange(1, 129)
+    lam1 = 2 - 2 * np.cos(k * np.pi / 129)
+    exact = np.sort((lam1[:, None] + lam1[None, :]).ravel())[:20]
+    assert np.max(np.abs(r.eval[:20] - exact) / exact) < 1e-10
+
+
+@pytest.mark.parametrize("case", ["laplace3d_mass_16", "vardiff3d_12", "laplace2d_128x128_nev20_bs20"])
+def test_mixed_precision_same_eigenvalues(gpu_lib, golden, case):
+    """FP32 inner solve, FP64 everything else: same eigenvalues, same tolerance."""
+    g = golden[case]
+    A, B, r = run_gpu(gpu_lib, case, g, precision=gpu_lib.PREC_MIXED)
+    nev = g["nev"]
+    ref = np.array(g["eval"][:nev])
+    assert r.status == gpu_lib.GCGE_OK and r.nconv >= nev
+    assert np.max(np.abs(r.eval[:nev] - ref) / np.abs(ref)) < 1e-10
+    res, relres = residuals(A.to_scipy(), None if B is None else B.to_scipy(), r.eval[:nev],
+                            r.evec[:, :nev])
+    assert np.all(relres <= g["tol"][1] * 1.001)
+
+
+def test_matches_live_oracle_on_unseen_input(gpu_lib):
+    """A problem the fixtures do not hold, against the oracle run here."""
+    A = P.aniso2d(33, 21, 2.5)
+    B = P.diag_matrix(0.5 + 1.5 * P.splitmix_uniform(42, A.n, 0))
+    X0 = P.initial_block(A.n, 12, seed=3)
+    r = gpu_lib.solve(A, B, 10, 4, 12, 22, X0=X0)
+    o = gcg_solve(A.to_scipy(), B.to_scipy(), X0, 10, 4, 12, 22)
+    assert r.nconv >= 10 and o.nconv >= 10
+    assert np.max(np.abs(r.eval[:10] - o.eval[:10]) / o.eval[:10]) < 1e-10
+
+
+def test_prepared_solve_is_repeatable(gpu_lib):
+    c = P.config1()
+    X0 = P.initial_block(c["A"].n, 40, seed=1)
+    prep = gpu_lib.Prepared(c["A"], None, 20, 20, 40, 40, X0=X0)
+    try:
+        r1 = prep.solve(want_evec=True)
+        r2 = prep.solve(want_evec=True)
+    finally:
+        prep.close()
+    assert np.array_equal(r1.eval, r2.eval) and r1.niter == r2.niter
+    assert np.array_equal(r1.evec, r2.evec)
+    assert r1.info["kernel_launches"] > 0 and r1.info["spmm_calls"] > 0

@@ -1,0 +1,85 @@
+"""The CPU oracle (numpy restatement of the reference GCG) pinned against the
+golden fixtures produced by the reference's own C sources, and against the
+analytic Dirichlet spectrum."""
+import numpy as np
+import pytest
+
+from conftest import build_case
+from gcge_gb300 import problems as P
+from oracle import ref_lib
+from oracle.gcg_oracle import GCGOracle, GCGParams, gcg_solve, residuals
+
+FAST_CASES = ["laplace2d_24x24_nev8", "laplace2d_24x24_noshift", "laplace2d_20x20_abstol",
+              "vardiff3d_12", "aniso2d_40x30_eps10_diagB", "rgg_2000_deg10"]
+
+
+def run_oracle(case, g):
+    A, B = build_case(case)
+    X0 = P.initial_block(A.n, g["nev_init"], seed=g["x0_seed"])
+    return A, B, gcg_solve(A.to_scipy(), None if B is None else B.to_scipy(), X0, g["nev"],
+                           g["block_size"], g["nev_init"], g["nev_max"], tol=tuple(g["tol"]),
+                           max_iter=g["max_iter"], gap_min=g["gap_min"], auto_shift=g["auto_shift"])
+
+
+@pytest.mark.parametrize("case", FAST_CASES)
+def test_oracle_matches_reference_fixture(case, golden):
+    g = golden[case]
+    A, B, r = run_oracle(case, g)
+    nev = g["nev"]
+    ref = np.array(g["eval"][:nev])
+    assert r.nconv >= nev
+    # same algorithm: eigenvalues agree far below the solver tolerance
+    assert np.max(np.abs(r.eval[:nev] - ref) / np.abs(ref)) < 1e-10
+    # iteration counts agree up to summation-order effects
+    assert abs(r.niter - g["niter"]) <= max(3, g["niter"] // 5)
+    res, rel = residuals(A.to_scipy(), None if B is None else B.to_scipy(), r.eval[:nev],
+                         r.evec[:, :nev])
+    tol0, tol1 = g["tol"]
+    assert np.all((res <= tol0 * 1.0001) & (rel <= tol1 * 1.0001))
+
+
+def test_oracle_analytic_laplace2d():
+    A = P.laplace2d(24, 24)
+    X0 = P.initial_block(A.n, 12, seed=1)
+    r = gcg_solve(A.to_scipy(), None, X0, 8, 4, 12, 20)
+    k = np.arange(1, 25)
+    lam1 = 2 - 2 * np.cos(k * np.pi / 25)
+    exact = np.sort((lam1[:, None] + lam1[None, :]).ravel())[:8]
+    assert np.max(np.abs(r.eval[:8] - exact) / exact) < 1e-11
+
+
+def test_oracle_mgs_orthonormalises():
+    A = P.laplace2d(10, 10).to_scipy()
+    Bd = P.diag_matrix(np.linspace(0.5, 2.0, 100)).to_scipy()
+    o = GCGOracle(A, Bd, GCGParams(nev_init=6, nev_max=6, block_size=2))
+    rng = np.random.default_rng(3)
+    X = np.asfortranarray(rng.standard_normal((100, 8)))
+    X[:, 5] = 0.0                        # a zero column is dropped (src/ops_orth.c:64-74)
+    end = o.mgs(X, 0, 8, Bd)
+    assert end == 7
+    G = X[:, :end].T @ (Bd @ X[:, :end])
+    assert np.abs(G - np.eye(end)).max() < 1e-12
+
+
+def test_oracle_block_pcg_stops_at_rate():
+    A = P.laplace2d(16, 16).to_scipy()
+    o = GCGOracle(A, None, GCGParams(nev_init=4, nev_max=4, block_size=4))
+    o.sigma = 0.3
+    rng = np.random.default_rng(4)
+    b = np.asfortranarray(rng.standard_normal((256, 3)))
+    x = np.zeros((256, 3), order="F")
+    it = o.block_pcg(b, x)
+    r = b - (A @ x + 0.3 * x)
+    assert it <= 30
+    assert np.all(np.linalg.norm(r, axis=0) <= 1e-2 * np.linalg.norm(b, axis=0) * 1.0001)
+
+
+@pytest.mark.skipif(not ref_lib.available(), reason="reference build (oracle/_ref) not present")
+def test_oracle_matches_live_reference_on_new_input():
+    A = P.aniso2d(17, 23, 3.0)
+    B = P.diag_matrix(0.5 + 1.5 * P.splitmix_uniform(99, A.n, 0))
+    X0 = P.initial_block(A.n, 9, seed=7)
+    ev, evec, nc, it, _ = ref_lib.ref_solve(A, B, X0, 10, 3, 9, 19)
+    r = gcg_solve(A.to_scipy(), B.to_scipy(), X0, 10, 3, 9, 19)
+    assert nc >= 10 and r.nconv >= 10
+    assert np.max(np.abs(ev[:10] - r.eval[:10]) / np.abs(ev[:10])) < 1e-10
