@@ -1,0 +1,349 @@
+#!/usr/bin/env python
+"""Benchmark of the GB300 GCG eigensolver on the generalized 3D workload.
+
+Workload (the generalized problem the headline metric is quoted on): A = (1/h^2)
+7-point Dirichlet Laplacian on a 64^3 grid (h = 1/65), B = M x M x M with the
+1D consistent mass M = h tridiag(1/6, 4/6, 1/6) (27 nonzeros per row),
+n = 262144; the nev = 100 smallest pairs, block size 20, nevInit 60,
+nevMax 160 (the reference front end's block rule), convergence
+||A x - lambda B x|| <= 1e-8 |lambda|, seeded Gaussian initial block.  All
+data are generated (problems.py); no dataset is involved.
+
+One step = one complete GCG solve.  Metric: converged requested eigenpairs per
+second (nev / solve time).  `value` is the mixed-precision solver (FP32
+block-PCG inner solve, everything else FP64) with inputs resident in HBM,
+timed with CUDA events on the library stream; `fp64_value` is the plain FP64
+GPU GCG on the same inputs; `e2e` is the same metric through GCGE_Solve from
+host CCS arrays (matrix upload, SELL build, solve, eigenvector download).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+N > 1 (torchrun): every rank solves its own replica on its own GPU (a single
+problem is not split across GPUs); value = all ranks' pairs / max time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+
+METRIC = "converged eigenpairs/s @1e-8 resid: mixed vs FP64 GCG, 1 GB300; p50/p99 latency"
+UNIT = "eigenpairs/s"
+WORKLOAD = dict(workload="laplace3d_7pt_64^3 + kron consistent mass (generalized), nev=100",
+                n=262144, nnz_A=1810432, nnz_B=6859000, nev=100, block_size=20, nev_init=60,
+                nev_max=160, tol="rel 1e-8", x0="seeded Gaussian n x 60 (seed 1)",
+                l2="working set (V 419 MB + matrices 106 MB) larger than the 129 MB L2")
+PEAK_FALLBACK_GBS = 6800.0
+# Iterations the full solve needs at this workload: measured with the GPU
+# FP64 path (54, same algorithm and initial block); the reference CPU arm and
+# the CPU baseline time a bounded number of outer iterations and scale by it.
+FULL_SOLVE_ITERS = 54
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--cpu-iters", type=int, default=2,
+                    help="outer iterations of the CPU sample (baseline / reference arm)")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--threads", type=int, default=0,
+                    help="host threads of the CPU reference arm (0 = all)")
+    ap.add_argument("--size", type=int, default=64, help="grid size k (k^3 unknowns)")
+    ap.add_argument("--solve-once", choices=["mixed", "fp64"], default=None,
+                    help="prepare the workload and run one solve (for profiler captures)")
+    return ap.parse_args()
+
+
+# ------------------------------------------------------------------ dist
+class Dist:
+    def __init__(self):
+        self.world = int(os.environ.get("WORLD_SIZE", "1"))
+        self.rank = int(os.environ.get("RANK", "0"))
+        self.local = int(os.environ.get("LOCAL_RANK", "0"))
+        self.pg = None
+        if self.world > 1:
+            import torch.distributed as dist
+            dist.init_process_group("gloo", init_method="env://")
+            self.pg = dist
+
+    def barrier(self):
+        if self.pg:
+            self.pg.barrier()
+
+    def max(self, v: float) -> float:
+        if not self.pg:
+            return v
+        import torch
+        t = torch.tensor([v], dtype=torch.float64)
+        self.pg.all_reduce(t, op=self.pg.ReduceOp.MAX)
+        return float(t.item())
+
+    def sum(self, v: float) -> float:
+        if not self.pg:
+            return v
+        import torch
+        t = torch.tensor([v], dtype=torch.float64)
+        self.pg.all_reduce(t, op=self.pg.ReduceOp.SUM)
+        return float(t.item())
+
+    def close(self):
+        if self.pg:
+            self.pg.destroy_process_group()
+
+
+# ------------------------------------------------------------------ clocks
+class Clocks:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        os.unlink(self.path)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ------------------------------------------------------------------ helpers
+def measured_peak_gbs():
+    try:
+        with open(os.path.join(HERE, "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except Exception:
+        return PEAK_FALLBACK_GBS, "fallback"
+
+
+def ncu_traffic_per_launch():
+    """DRAM bytes per PCG SpMM launch from the committed ncu summary, if any."""
+    p = os.path.join(HERE, "profiles", "pcg_spmm_fp32_laplace3d_mass_64.json")
+    try:
+        with open(p) as f:
+            return float(json.load(f)["dram_bytes_per_launch"])
+    except Exception:
+        return None
+
+
+def build_workload(k):
+    from gcge_gb300 import problems as P
+    c = P.config2(k)
+    X0 = P.initial_block(c["A"].n, c["nev_init"], seed=1)
+    return c, X0
+
+
+def cpu_sample(c, X0, iters, threads):
+    """The CPU oracle (numpy restatement of the reference GCG) on the same
+    workload for `iters` outer iterations.  Returns the estimated seconds of a
+    full solve: set-up (InitializeX, first Rayleigh-Ritz) + FULL_SOLVE_ITERS x
+    the mean measured outer-iteration time, and the sampled seconds."""
+    from oracle.gcg_oracle import GCGOracle, GCGParams
+    p = GCGParams(nev_init=c["nev_init"], nev_max=c["nev_max"], block_size=c["block_size"],
+                  num_iter_max=iters)
+    o = GCGOracle(c["A"].to_scipy(), c["B"].to_scipy(), p)
+    r = o.solve(X0, c["nev"])
+    m = r.marks
+    setup = m[1] - m[0]
+    per_iter = (m[-1] - m[1]) / max(1, len(m) - 2)
+    return setup + FULL_SOLVE_ITERS * per_iter, m[-1] - m[0]
+
+
+# ------------------------------------------------------------------ arms
+def run_reference(args, d: Dist):
+    if d.rank != 0:
+        return
+    threads = args.threads or os.cpu_count() or 1
+    c, X0 = build_workload(args.size)
+    cw, X0w = build_workload(12)
+    for _ in range(args.warmup):
+        cpu_sample(cw, X0w, 1, threads)
+    runs = [cpu_sample(c, X0, args.cpu_iters, threads) for _ in range(args.steps)]
+    per_solve = statistics.mean(r[0] for r in runs)
+    sampled = statistics.mean(r[1] for r in runs)
+    value = c["nev"] / per_solve
+    sample = (f"numpy/scipy restatement of the reference GCG (oracle/gcg_oracle.py; the reference's "
+              f"own C build is not available on this host): set-up + {args.cpu_iters} outer "
+              f"iterations of this workload ({sampled:.1f} s sampled per step), extrapolated to "
+              f"set-up + {FULL_SOLVE_ITERS} iterations")
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": per_solve * 1000,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic", "impl": "reference", "config": WORKLOAD,
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                             "sample": sample},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args, d: Dist):
+    os.environ.setdefault("CUDA_VISIBLE_DEVICES", str(d.local))
+    import gcge_gb300 as G
+    G.load(build_if_missing=True)
+    c, X0 = build_workload(args.size)
+    A, B, nev = c["A"], c["B"], c["nev"]
+    kw = dict(nev=nev, block_size=c["block_size"], nev_init=c["nev_init"], nev_max=c["nev_max"],
+              X0=X0)
+    prep_mixed = G.Prepared(A, B, precision=G.PREC_MIXED, **kw)
+    prep_fp64 = G.Prepared(A, B, precision=G.PREC_FP64, **kw)
+
+    def timed(prep, steps):
+        infos, pairs = [], 0
+        d.barrier()
+        with G.DeviceTimer() as tm:
+            for _ in range(steps):
+                r = prep.solve()
+                infos.append(r.info)
+                pairs += min(r.nconv, nev) if r.status == G.GCGE_OK else 0
+        return tm.ms / 1000.0, pairs, infos
+
+    for _ in range(args.warmup):
+        prep_mixed.solve()
+    prep_fp64.solve()
+    clocks = Clocks(d.local)
+    clocks.start()
+    t_mixed, pairs_mixed, infos = timed(prep_mixed, args.steps)
+    clk = clocks.stop()
+    t_fp64, pairs_fp64, infos64 = timed(prep_fp64, max(1, args.steps // 2))
+    t_mixed_max = d.max(t_mixed)
+    value = d.sum(pairs_mixed) / t_mixed_max
+    fp64_value = d.sum(pairs_fp64) / d.max(t_fp64)
+
+    # end to end through GCGE_Solve from host arrays
+    e2e_steps = max(1, args.steps // 2)
+    d.barrier()
+    t0 = time.perf_counter()
+    e2e_pairs = 0
+    for _ in range(e2e_steps):
+        r = G.solve(A, B, precision=G.PREC_MIXED, **kw)
+        e2e_pairs += min(r.nconv, nev) if r.status == G.GCGE_OK else 0
+    t_e2e = d.max(time.perf_counter() - t0)
+    e2e_value = d.sum(e2e_pairs) / t_e2e
+    h2d = (A.indptr.nbytes + A.indices.nbytes + A.data.nbytes + B.indptr.nbytes + B.indices.nbytes
+           + B.data.nbytes + X0.nbytes)
+    d2h = 8 * c["nev_max"] * (1 + A.n)
+
+    spmm_ms = sum(i["pcg_spmm_ms"] for i in infos)
+    spmm_bytes = sum(i["pcg_spmm_bytes"] for i in infos)
+    spmm_launches = sum(i["pcg_spmm_launches"] for i in infos)
+    peak, peak_kind = measured_peak_gbs()
+    achieved = spmm_bytes / (spmm_ms / 1000.0) / 1e9 if spmm_ms > 0 else None
+    traffic = ncu_traffic_per_launch()
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": t_mixed_max / args.steps * 1000.0,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64 outer / f32 inner PCG (mixed)", "data": "synthetic (generated, seeded)",
+        "config": dict(WORKLOAD, precision="mixed", parallelism=f"replicas x{d.world}"),
+        "fp64_value": fp64_value, "mixed_over_fp64": value / fp64_value if fp64_value else None,
+        "fp64_ms_per_step": t_fp64 / max(1, args.steps // 2) * 1000.0,
+        "niter": [i["niter"] for i in infos], "nconv": [i["nconv"] for i in infos],
+        "phase_ms_last_step": infos[-1]["phase_ms"], "phase_ms_fp64": infos64[-1]["phase_ms"],
+        "gpu_launches": sum(i["kernel_launches"] for i in infos),
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": int(d2h), "steps": e2e_steps},
+        "roofline": {"kernel": "k_spmm_dot<float> (block-PCG SpMM, union pattern of A and B)",
+                     "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": (achieved / peak) if achieved else None, "peak_kind": peak_kind,
+                     "traffic": traffic,
+                     "bytes_per_launch": spmm_bytes / max(1, spmm_launches),
+                     "ms_per_launch": spmm_ms / max(1, spmm_launches), "launches": spmm_launches},
+        "clocks": clk,
+    }
+    prep_mixed.close()
+    prep_fp64.close()
+    if d.rank == 0 and d.world == 1 and not args.no_cpu_baseline:
+        # single-threaded CPU oracle in a child process (BLAS threads fixed at start-up)
+        env = dict(os.environ, OPENBLAS_NUM_THREADS="1", OMP_NUM_THREADS="1")
+        cmd = [sys.executable, os.path.abspath(__file__), "--impl", "reference", "--steps", "1",
+               "--warmup", "0", "--threads", "1", "--cpu-iters", str(args.cpu_iters),
+               "--size", str(args.size)]
+        try:
+            out = subprocess.run(cmd, env=env, capture_output=True, text=True, timeout=900).stdout
+            ref = json.loads([ln for ln in out.splitlines() if ln.startswith("{")][-1])
+            line["cpu_baseline"] = dict(ref["cpu_baseline"])
+        except Exception as e:  # reported, not fatal
+            line["cpu_baseline"] = {"value": None, "unit": UNIT, "cores": 1, "kind": "port",
+                                    "sample": f"failed: {e}"}
+    if d.rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+def solve_once(args):
+    import gcge_gb300 as G
+    G.load(build_if_missing=True)
+    c, X0 = build_workload(args.size)
+    prep = G.Prepared(c["A"], c["B"], c["nev"], c["block_size"], c["nev_init"], c["nev_max"], X0=X0,
+                      precision=G.PREC_MIXED if args.solve_once == "mixed" else G.PREC_FP64)
+    r = prep.solve()
+    prep.close()
+    print(json.dumps({"nconv": r.nconv, "niter": r.niter, "status": r.status,
+                      "kernel_launches": r.info["kernel_launches"]}))
+    return 0 if r.status == G.GCGE_OK else 1
+
+
+def main():
+    args = parse()
+    if args.solve_once:
+        sys.exit(solve_once(args))
+    if args.impl == "reference":
+        threads = args.threads or os.cpu_count() or 1
+        os.environ["OPENBLAS_NUM_THREADS"] = str(threads)
+        os.environ["OMP_NUM_THREADS"] = str(threads)
+    d = Dist()
+    try:
+        if args.impl == "reference":
+            run_reference(args, d)
+        else:
+            run_ours(args, d)
+    finally:
+        d.close()
+
+
+if __name__ == "__main__":
+    main()

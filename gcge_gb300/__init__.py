@@ -38,6 +38,7 @@ EXPORTED_SYMBOLS = [
     "CUDA_MatNnz", "CUDA_MultiVecSetFromHost", "CUDA_MultiVecGetToHost", "CUDA_MultiVecSize",
     "GCGE_SetPrecision", "GCGE_Solve", "GCGE_GetSolveInfo", "GCGE_Prepare", "GCGE_PreparedSolve",
     "GCGE_PreparedDestroy", "GCGE_BenchSpMM", "GCGE_DenseEig", "GCGE_BlockPCG", "GCGE_BOrth",
+    "GCGE_TimerStart", "GCGE_TimerStop",
 ]
 
 _lib = None
@@ -65,14 +66,16 @@ class SolveInfo(ctypes.Structure):
     _fields_ = [("nconv", ctypes.c_int), ("niter", ctypes.c_int), ("status", ctypes.c_int),
                 ("pcg_iters", ctypes.c_int), ("spmm_calls", ctypes.c_int),
                 ("kernel_launches", ctypes.c_int), ("seconds", ctypes.c_double),
-                ("phase_ms", ctypes.c_double * 10)]
+                ("phase_ms", ctypes.c_double * 10), ("pcg_spmm_launches", ctypes.c_int),
+                ("pcg_spmm_ms", ctypes.c_double), ("pcg_spmm_bytes", ctypes.c_double)]
 
     PHASES = ("checkconv", "compP", "compRR", "rr_matW", "eig", "compRV", "compW", "linsol",
               "compX", "initX")
 
     def as_dict(self) -> dict:
         d = {k: getattr(self, k) for k in ("nconv", "niter", "status", "pcg_iters", "spmm_calls",
-                                           "kernel_launches", "seconds")}
+                                           "kernel_launches", "seconds", "pcg_spmm_launches",
+                                           "pcg_spmm_ms", "pcg_spmm_bytes")}
         d["phase_ms"] = {p: self.phase_ms[i] for i, p in enumerate(self.PHASES)}
         return d
 
@@ -96,8 +99,10 @@ def load(build_if_missing: bool = False) -> ctypes.CDLL:
     for name in ("CUDA_MatCreateFromCCS", "CUDA_MultiVecSetFromHost", "CUDA_MultiVecGetToHost",
                  "GCGE_Solve", "GCGE_Prepare", "GCGE_PreparedSolve", "GCGE_SetPrecision",
                  "GCGE_GetSolveInfo", "GCGE_BenchSpMM", "ops_cuda_last_error", "CUDA_MultiVecSize",
-                 "CUDA_MatNnz", "GCGE_DenseEig", "GCGE_BlockPCG", "GCGE_BOrth"):
+                 "CUDA_MatNnz", "GCGE_DenseEig", "GCGE_BlockPCG", "GCGE_BOrth",
+                 "GCGE_TimerStart"):
         getattr(lib, name).restype = ctypes.c_int
+    lib.GCGE_TimerStop.restype = ctypes.c_double
     _lib = lib
     return lib
 
@@ -417,3 +422,17 @@ def b_orth(B, X, start, n=None, zero_tol=2 * np.finfo(float).eps, max_reorth=2, 
         return ops.download(hx, 0, end.value)
     finally:
         ops.close()
+
+
+class DeviceTimer:
+    """CUDA events on the library stream around a region (GCGE_TimerStart/Stop)."""
+
+    def __enter__(self):
+        st = load().GCGE_TimerStart()
+        if st != GCGE_OK:
+            raise GCGEError(st, "GCGE_TimerStart")
+        return self
+
+    def __exit__(self, *exc):
+        self.ms = load().GCGE_TimerStop()
+        return False

@@ -917,6 +917,30 @@ int GCGE_Solve(int n, const int *a_colptr, const int *a_rowind, const double *a_
     return st;
 }
 
+static cudaEvent_t g_t0 = nullptr, g_t1 = nullptr;
+int GCGE_TimerStart(void) {
+    GCGE_TRY_RET({
+        if (!g_t0) {
+            GCGE_CUDA(cudaEventCreate(&g_t0));
+            GCGE_CUDA(cudaEventCreate(&g_t1));
+        }
+        GCGE_CUDA(cudaEventRecord(g_t0, lib_stream()));
+    });
+}
+double GCGE_TimerStop(void) {
+    try {
+        GCGE_REQUIRE(g_t0 != nullptr, GCGE_ERR_ARG, "GCGE_TimerStop without GCGE_TimerStart");
+        GCGE_CUDA(cudaEventRecord(g_t1, lib_stream()));
+        GCGE_CUDA(cudaEventSynchronize(g_t1));
+        float ms = 0.f;
+        GCGE_CUDA(cudaEventElapsedTime(&ms, g_t0, g_t1));
+        return ms;
+    } catch (const CudaError &e) {
+        set_error(e.status, e.where.c_str());
+        return -1.0;
+    }
+}
+
 int GCGE_BenchSpMM(void *mat, int k, int fp32, int reps, double *ms_per_launch,
                    double *bytes_per_launch) {
     GCGE_TRY_RET({

@@ -733,7 +733,11 @@ void gcg_eigensolver(void *Ah, void *Bh, double *eval, void **evec, int nevGiven
         c->pub.nevGiven = nevGiven;
         GCGE_REQUIRE(V->ld == R->ld, GCGE_ERR_ARG, "EigenSolver: leading dimensions differ");
         GcgRun run(*c, A, B, V, R);
+        c->pcg.timing_reset();
         const int status = run.run(eval, nevGiven, nevConv);
+        c->info.pcg_spmm_ms = c->pcg.timing_collect_ms();
+        c->info.pcg_spmm_launches = c->pcg.spmm_launches;
+        c->info.pcg_spmm_bytes = c->pcg.spmm_bytes;
         c->info.nconv = *nevConv;
         c->info.niter = c->pub.numIter;
         c->info.status = status;

@@ -165,6 +165,25 @@ static int chunks_for(int n, int k) {
     return std::max(1, std::min((n + 1023) / 1024, (4 * sms + k - 1) / k));
 }
 
+void PcgWork::timing_reset() {
+    ev_used = 0;
+    spmm_bytes = 0.0;
+    spmm_launches = 0;
+}
+double PcgWork::timing_collect_ms() {
+    double ms = 0.0;
+    for (size_t i = 0; i + 1 < ev_used; i += 2) {
+        float t = 0.f;
+        if (cudaEventSynchronize(ev[i + 1]) == cudaSuccess &&
+            cudaEventElapsedTime(&t, ev[i], ev[i + 1]) == cudaSuccess)
+            ms += t;
+    }
+    return ms;
+}
+PcgWork::~PcgWork() {
+    for (auto e : ev) cudaEventDestroy(e);
+}
+
 void PcgWork::reserve(int n, int kmax_, int spmm_nblocks) {
     kmax = kmax_;
     const size_t need = std::max((size_t)spmm_nblocks, (size_t)chunks_for(n, 1)) * kmax;
@@ -214,8 +233,25 @@ int block_pcg(PcgWork &wk, const SellPattern &pat, const T *sval, const T *Bv, i
         if (wk.h_sc.p->nactive == 0) break;
         k_pcg_p<T><<<pgrid, 256, 0, st>>>(n, k, R, P, ld, wk.sc.p);
         GCGE_CHECK_LAUNCH();
+        const bool timed = wk.ev_used + 2 <= 65536;
+        if (timed) {
+            while (wk.ev.size() < wk.ev_used + 2) {
+                cudaEvent_t e;
+                GCGE_CUDA(cudaEventCreate(&e));
+                wk.ev.push_back(e);
+            }
+            GCGE_CUDA(cudaEventRecord(wk.ev[wk.ev_used], st));
+        }
         const int nb = spmm_dot<T>(pat, sval, P, ld, W, ld, k, &wk.sc.p->active[0], wk.part.p,
                                    wk.kmax, st);
+        if (timed) {
+            GCGE_CUDA(cudaEventRecord(wk.ev[wk.ev_used + 1], st));
+            wk.ev_used += 2;
+        }
+        // algorithmic bytes: matrix once, active columns of p read once, of w written once
+        wk.spmm_bytes += (double)pat.nnz * (sizeof(T) + 4) + 4.0 * (n + 1) +
+                         2.0 * n * wk.h_sc.p->nactive * sizeof(T);
+        wk.spmm_launches++;
         k_pcg_alpha<<<1, 1024, 0, st>>>(k, wk.part.p, nb, wk.kmax, wk.sc.p);
         GCGE_CHECK_LAUNCH();
         k_pcg_xr<T><<<cgrid, 256, 0, st>>>(n, k, X, ldx, R, P, W, ld, wk.sc.p, wk.part.p, wk.kmax,

@@ -21,7 +21,15 @@ struct PcgWork {
     DevBuf<double> part;
     DevBuf<PcgScalars> sc;
     PinnedBuf<PcgScalars> h_sc;
+    // per-launch timing of the SpMM inside the iterations (event pairs)
+    std::vector<cudaEvent_t> ev;
+    size_t ev_used = 0;
+    double spmm_bytes = 0.0;
+    int spmm_launches = 0;
     void reserve(int n, int kmax, int spmm_nblocks);
+    void timing_reset();
+    double timing_collect_ms();  // synchronises, sums the recorded intervals
+    ~PcgWork();
 };
 
 // Solve S x = b column-wise (S on the SELL pattern `pat` with values sval)

@@ -90,6 +90,10 @@ typedef struct gcge_solve_info {
     double seconds;     /* wall time of the solve on the host clock */
     double phase_ms[10];/* checkconv, compP, compRR, rr_matW, eig, compRV, compW, linsol,
                            compX, initX (CUDA events on the solver stream) */
+    int pcg_spmm_launches;   /* SpMM launches inside the block-PCG iterations */
+    double pcg_spmm_ms;      /* their summed device time (CUDA events around each launch) */
+    double pcg_spmm_bytes;   /* their summed algorithmic bytes: nnz (v + 4) + 4 (n + 1)
+                                + 2 n k_active v, v = value size (8 FP64, 4 mixed) */
 } gcge_solve_info;
 
 /* One-call solve of A x = lambda B x for the nev smallest pairs from host
@@ -128,6 +132,12 @@ void GCGE_PreparedDestroy(gcge_prepared **prep);
  * Timed with CUDA events on the library stream; returns average ms/launch. */
 int GCGE_BenchSpMM(void *mat, int k, int fp32, int reps, double *ms_per_launch,
                    double *bytes_per_launch);
+
+/* CUDA-event timer on the library stream: GCGE_TimerStart records the start
+ * event; GCGE_TimerStop records the stop event, waits for it and returns the
+ * elapsed milliseconds (negative on error). */
+int GCGE_TimerStart(void);
+double GCGE_TimerStop(void);
 
 /* ---- component entry points (each step of the solver on its own) -------
  * Dense symmetric eigensolve of the Rayleigh-Ritz step (replaces dsyevx,

@@ -58,6 +58,7 @@ class GCGResult:
     nconv: int
     niter: int
     times: dict = field(default_factory=dict)
+    marks: list = field(default_factory=list)  # wall clock at solve start and each loop top
 
 
 class GCGOracle:
@@ -422,6 +423,7 @@ class GCGOracle:
         self.ss_evec = None
         offsetP = [0] * (bs + 3)
         offsetW = [0] * (bs + 3)
+        marks = [time.perf_counter()]
         t = time.perf_counter()
         self.initialize_x(V, ritz_vec, nev_given)
         self.times["initX"] += time.perf_counter() - t
@@ -439,6 +441,7 @@ class GCGOracle:
         num_iter_max = p.num_iter_max
         num_iter = 0
         while True:
+            marks.append(time.perf_counter())
             num_check = 0 if num_iter <= 0 else (
                 self.sizeN if self.startN + self.sizeN < self.endX else self.endX - self.startN)
             num_check = min(num_check, p.check_conv_max_num)
@@ -496,7 +499,9 @@ class GCGOracle:
         niter = num_iter + (p.num_iter_max - num_iter_max)
         ev = np.zeros(nev_max)
         ev[:self.sizeX] = self.ss_eval[:self.sizeX]
-        return GCGResult(eval=ev, evec=ritz_vec, nconv=nevc, niter=niter, times=dict(self.times))
+        marks.append(time.perf_counter())
+        return GCGResult(eval=ev, evec=ritz_vec, nconv=nevc, niter=niter, times=dict(self.times),
+                         marks=marks)
 
 
 def gcg_solve(A, B, X0, nev, block_size, nev_init, nev_max, tol=(1e300, 1e-8),
