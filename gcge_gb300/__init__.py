@@ -38,7 +38,7 @@ EXPORTED_SYMBOLS = [
     "CUDA_MatNnz", "CUDA_MultiVecSetFromHost", "CUDA_MultiVecGetToHost", "CUDA_MultiVecSize",
     "GCGE_SetPrecision", "GCGE_Solve", "GCGE_GetSolveInfo", "GCGE_Prepare", "GCGE_PreparedSolve",
     "GCGE_PreparedDestroy", "GCGE_BenchSpMM", "GCGE_DenseEig", "GCGE_BlockPCG", "GCGE_BOrth",
-    "GCGE_TimerStart", "GCGE_TimerStop",
+    "GCGE_TimerStart", "GCGE_TimerStop", "GCGE_GramNoAlloc",
 ]
 
 _lib = None
@@ -100,7 +100,7 @@ def load(build_if_missing: bool = False) -> ctypes.CDLL:
                  "GCGE_Solve", "GCGE_Prepare", "GCGE_PreparedSolve", "GCGE_SetPrecision",
                  "GCGE_GetSolveInfo", "GCGE_BenchSpMM", "ops_cuda_last_error", "CUDA_MultiVecSize",
                  "CUDA_MatNnz", "GCGE_DenseEig", "GCGE_BlockPCG", "GCGE_BOrth",
-                 "GCGE_TimerStart"):
+                 "GCGE_TimerStart", "GCGE_GramNoAlloc"):
         getattr(lib, name).restype = ctypes.c_int
     lib.GCGE_TimerStop.restype = ctypes.c_double
     _lib = lib

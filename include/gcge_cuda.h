@@ -155,6 +155,23 @@ int GCGE_BlockPCG(void *A, void *B, double sigma, void **b, void **x, int k, int
  * the number of dependent columns dropped. */
 int GCGE_BOrth(void *B, void **x, int start, int *end, double zero_tol, int max_reorth);
 
+/* ---- allocation-free Gram product ---------------------------------------
+ * No counterpart in the reference: an addition for callers that may not
+ * allocate device memory (their memory belongs to another allocator or a
+ * pre-sized pool, or they run latency-critical loops where an allocation's
+ * device synchronisation is not acceptable).
+ * C (m x w, ldc) = Q^T P for device arrays Q (n x m, ldq) and P (n x w, ldp),
+ * column-major, launched on `stream` (a cudaStream_t; NULL = default stream).
+ * Calls no cudaMalloc/cudaFree: the split-K partial sums live in a 4 MiB
+ * device array fixed in the library, so m * w <= 524288 (larger requests
+ * return GCGE_ERR_TOO_LARGE).  The array's device address is looked up by
+ * the first call on each device (make that call before any stream capture);
+ * all calls on a device share the array, so calls that overlap on the GPU
+ * race - order them on one stream. */
+#define GCGE_NOALLOC_SCRATCH_BYTES (4u << 20)
+int GCGE_GramNoAlloc(int n, int m, int w, const double *Q, int ldq, const double *P, int ldp,
+                     double *C, int ldc, void *stream);
+
 #ifdef __cplusplus
 }
 #endif
