@@ -71,8 +71,8 @@ void SolverCtx::reserve(int n_, int nev_max, int nev_init, int bs, int spmm_nblo
     if (bs > cap_bs || (size_t)ld * bs > bbuf.n) {
         bbuf.alloc((size_t)ld * bs);
         r64.alloc((size_t)ld * bs);
-        p64.alloc((size_t)ld * bs);
-        w64.alloc((size_t)ld * bs);
+        const size_t nr = (size_t)n_ * rows_width(std::min(bs, 40), 8);
+        for (auto *b : {&xr64, &br64, &rr64, &pr64, &wr64}) b->alloc(nr);
         cap_bs = bs;
     }
     if (smax > cap_s) {
@@ -460,22 +460,27 @@ struct GcgRun {
         const bool rel = std::strcmp(g.compW_cg_tol_type, "rel") == 0;
         int it;
         if (!mixed) {
-            it = block_pcg<double>(c.pcg, c.upat, c.us64.p, c.bbuf.p, ld, colp(V, startW), ld,
-                                   c.r64.p, c.p64.p, c.w64.p, ld, bsz, g.compW_cg_max_iter,
-                                   g.compW_cg_rate, g.compW_cg_tol, rel, st);
+            const int kp = rows_width(bsz, 8);
+            col_to_rows<double, double>(n, bsz, kp, colp(V, startW), ld, c.xr64.p, st);
+            col_to_rows<double, double>(n, bsz, kp, c.bbuf.p, ld, c.br64.p, st);
+            it = block_pcg_rows<double>(c.pcg, c.upat, c.us64.p, c.br64.p, c.xr64.p, c.rr64.p,
+                                        c.pr64.p, c.wr64.p, kp, bsz, g.compW_cg_max_iter,
+                                        g.compW_cg_rate, g.compW_cg_tol, rel, st);
+            rows_to_col<double, double>(n, bsz, kp, c.xr64.p, colp(V, startW), ld, false, st);
         } else {
             // CG from x0 on S x = b is CG from 0 on S d = b - S x0: the residual
             // is formed in FP64 (it is a difference of nearly equal vectors once
             // the Ritz vectors converge), the correction d is iterated in FP32,
             // and x = x0 + d is accumulated in FP64.
+            const int kp = rows_width(bsz, 4);
             spmm<double>(c.upat, c.us64.p, colp(V, startW), ld, c.r64.p, ld, bsz, st);
             axpby(n, bsz, 1.0, c.bbuf.p, ld, -1.0, c.r64.p, ld, st);
-            copy_f64_to_f32(n, bsz, c.r64.p, ld, c.b32.p, ld, st);
-            GCGE_CUDA(cudaMemsetAsync(c.x32.p, 0, sizeof(float) * (size_t)ld * bsz, st));
-            it = block_pcg<float>(c.pcg, c.upat, c.us32.p, c.b32.p, ld, c.x32.p, ld, c.r32.p,
-                                  c.p32.p, c.w32.p, ld, bsz, g.compW_cg_max_iter, g.compW_cg_rate,
-                                  g.compW_cg_tol, rel, st);
-            add_f32_to_f64(n, bsz, c.x32.p, ld, colp(V, startW), ld, st);
+            col_to_rows<double, float>(n, bsz, kp, c.r64.p, ld, c.br32.p, st);
+            GCGE_CUDA(cudaMemsetAsync(c.xr32.p, 0, sizeof(float) * (size_t)n * kp, st));
+            it = block_pcg_rows<float>(c.pcg, c.upat, c.us32.p, c.br32.p, c.xr32.p, c.rr32.p,
+                                       c.pr32.p, c.wr32.p, kp, bsz, g.compW_cg_max_iter,
+                                       g.compW_cg_rate, g.compW_cg_tol, rel, st);
+            rows_to_col<float, double>(n, bsz, kp, c.xr32.p, colp(V, startW), ld, true, st);
             spmm_calls++;
         }
         pcg_iters += it;
@@ -556,7 +561,7 @@ struct GcgRun {
         GCGE_REQUIRE(nevMax >= *nevConvIO + bs || nevMax >= bs, GCGE_ERR_ARG, "nevMax too small");
         GCGE_REQUIRE(V->ncols >= nevMax + 2 * bs && ritz->ncols >= nevMax, GCGE_ERR_ARG,
                      "workspace multivectors too small");
-        GCGE_REQUIRE(bs <= kPcgMaxCols && bs >= 1, GCGE_ERR_ARG, "block_size out of range");
+        GCGE_REQUIRE(bs <= 40 && bs >= 1, GCGE_ERR_ARG, "block_size out of range (1..40)");
         GCGE_REQUIRE(nevMax + 2 * bs <= n, GCGE_ERR_ARG, "nevMax + 2*block_size exceeds n");
         GCGE_REQUIRE(nevGiven >= 0, GCGE_ERR_ARG, "nevGiven < 0");
         int numIterMax = g.numIterMax;
@@ -719,12 +724,8 @@ void gcg_eigensolver(void *Ah, void *Bh, double *eval, void **evec, int nevGiven
         prepare_union(*c, A, B, st);
         c->reserve(A->n, c->pub.nevMax, c->pub.nevInit, c->pub.block_size, spmm_blocks(c->upat));
         if (c->precision == GCGE_PREC_MIXED) {
-            const size_t nb = (size_t)round32(A->n) * c->pub.block_size;
-            c->x32.alloc(nb);
-            c->b32.alloc(nb);
-            c->r32.alloc(nb);
-            c->p32.alloc(nb);
-            c->w32.alloc(nb);
+            const size_t nb = (size_t)A->n * rows_width(std::min(c->pub.block_size, 40), 4);
+            for (auto *b : {&c->xr32, &c->br32, &c->rr32, &c->pr32, &c->wr32}) b->alloc(nb);
         }
         c->pub.A = Ah;
         c->pub.B = Bh;

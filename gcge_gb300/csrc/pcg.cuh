@@ -33,11 +33,17 @@ struct PcgWork {
 };
 
 // Solve S x = b column-wise (S on the SELL pattern `pat` with values sval)
-// starting from x; R, P, W are n x k work blocks with leading dimension ld.
-// Returns the number of iterations run (<= max_iter).
+// starting from x.  B, X, R, P, W are row-interleaved n x kp blocks (row i at
+// i*kp, padding columns zero).  Returns the number of iterations run.
 template <typename T>
-int block_pcg(PcgWork &wk, const SellPattern &pat, const T *sval, const T *B, int ldb, T *X,
-              int ldx, T *R, T *P, T *W, int ld, int k, int max_iter, double rate, double tol,
-              bool rel_tol, cudaStream_t st);
+int block_pcg_rows(PcgWork &wk, const SellPattern &pat, const T *sval, const T *B, T *X, T *R,
+                   T *P, T *W, int kp, int k, int max_iter, double rate, double tol, bool rel_tol,
+                   cudaStream_t st);
+
+// Column-major (ld) <-> row-interleaved (kp) block conversions.
+template <typename S, typename T>
+void col_to_rows(int n, int k, int kp, const S *X, int ldx, T *Y, cudaStream_t st);
+template <typename T, typename D>
+void rows_to_col(int n, int k, int kp, const T *X, D *Y, int ldy, bool add, cudaStream_t st);
 
 }  // namespace gcge

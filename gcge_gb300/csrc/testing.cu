@@ -40,7 +40,7 @@ int GCGE_BlockPCG(void *A, void *B, double sigma, void **b, void **x, int k, int
         SparseMat *Bm = B ? as_mat(B) : nullptr;
         MultiVec *bv = as_mv(b), *xv = as_mv(x);
         GCGE_REQUIRE(Am && (!B || Bm) && bv && xv, GCGE_ERR_HANDLE, "GCGE_BlockPCG: handles");
-        GCGE_REQUIRE(k >= 1 && k <= kPcgMaxCols && k <= bv->ncols && k <= xv->ncols, GCGE_ERR_ARG,
+        GCGE_REQUIRE(k >= 1 && k <= 40 && k <= bv->ncols && k <= xv->ncols, GCGE_ERR_ARG,
                      "GCGE_BlockPCG: k");
         cudaStream_t st = lib_stream();
         SolverCtx c;
@@ -48,19 +48,24 @@ int GCGE_BlockPCG(void *A, void *B, double sigma, void **b, void **x, int k, int
         c.reserve(Am->n, k, k, k, spmm_blocks(c.upat));
         shift_values(c.upat.padded, c.ua.p, c.ub.p, sigma, fp32 ? nullptr : c.us64.p,
                      fp32 ? c.us32.p : nullptr, st);
-        const int n = Am->n, ld = c.ld;
+        const int n = Am->n;
         int it = 0;
         if (!fp32) {
-            it = block_pcg<double>(c.pcg, c.upat, c.us64.p, bv->data, bv->ld, xv->data, xv->ld,
-                                   c.r64.p, c.p64.p, c.w64.p, ld, k, max_iter, rate, tol, false, st);
+            const int kp = rows_width(k, 8);
+            col_to_rows<double, double>(n, k, kp, xv->data, xv->ld, c.xr64.p, st);
+            col_to_rows<double, double>(n, k, kp, bv->data, bv->ld, c.br64.p, st);
+            it = block_pcg_rows<double>(c.pcg, c.upat, c.us64.p, c.br64.p, c.xr64.p, c.rr64.p,
+                                        c.pr64.p, c.wr64.p, kp, k, max_iter, rate, tol, false, st);
+            rows_to_col<double, double>(n, k, kp, c.xr64.p, xv->data, xv->ld, false, st);
         } else {
+            const int kp = rows_width(k, 4);
             DevBuf<float> x32, b32, r32, p32, w32;
-            for (auto *bb : {&x32, &b32, &r32, &p32, &w32}) bb->alloc((size_t)ld * k);
-            copy_f64_to_f32(n, k, xv->data, xv->ld, x32.p, ld, st);
-            copy_f64_to_f32(n, k, bv->data, bv->ld, b32.p, ld, st);
-            it = block_pcg<float>(c.pcg, c.upat, c.us32.p, b32.p, ld, x32.p, ld, r32.p, p32.p,
-                                  w32.p, ld, k, max_iter, rate, tol, false, st);
-            copy_f32_to_f64(n, k, x32.p, ld, xv->data, xv->ld, st);
+            for (auto *bb : {&x32, &b32, &r32, &p32, &w32}) bb->alloc((size_t)n * kp);
+            col_to_rows<double, float>(n, k, kp, xv->data, xv->ld, x32.p, st);
+            col_to_rows<double, float>(n, k, kp, bv->data, bv->ld, b32.p, st);
+            it = block_pcg_rows<float>(c.pcg, c.upat, c.us32.p, b32.p, x32.p, r32.p, p32.p, w32.p,
+                                       kp, k, max_iter, rate, tol, false, st);
+            rows_to_col<float, double>(n, k, kp, x32.p, xv->data, xv->ld, false, st);
         }
         GCGE_CUDA(cudaStreamSynchronize(st));
         if (iters) *iters = it;
