@@ -162,8 +162,8 @@ def measured_peak_gbs():
 
 
 def ncu_traffic_per_launch():
-    """DRAM bytes per PCG SpMM launch from the committed ncu summary, if any."""
-    p = os.path.join(HERE, "profiles", "pcg_spmm_fp32_laplace3d_mass_64.json")
+    """DRAM bytes per block-PCG kernel launch from the committed ncu summary, if any."""
+    p = os.path.join(HERE, "profiles", "block_pcg_fp32_laplace3d_mass_64.json")
     try:
         with open(p) as f:
             return float(json.load(f)["dram_bytes_per_launch"])
@@ -270,9 +270,13 @@ def run_ours(args, d: Dist):
 
     spmm_ms = sum(i["pcg_spmm_ms"] for i in infos)
     spmm_bytes = sum(i["pcg_spmm_bytes"] for i in infos)
-    spmm_launches = sum(i["pcg_spmm_launches"] for i in infos)
+    spmm_phases = sum(i["pcg_spmm_launches"] for i in infos)
+    pcg_ms = sum(i["pcg_kernel_ms"] for i in infos)
+    pcg_bytes = sum(i["pcg_kernel_bytes"] for i in infos)
+    pcg_launches = sum(i["pcg_kernel_launches"] for i in infos)
     peak, peak_kind = measured_peak_gbs()
-    achieved = spmm_bytes / (spmm_ms / 1000.0) / 1e9 if spmm_ms > 0 else None
+    achieved = pcg_bytes / (pcg_ms / 1000.0) / 1e9 if pcg_ms > 0 else None
+    spmm_achieved = spmm_bytes / (spmm_ms / 1000.0) / 1e9 if spmm_ms > 0 else None
     traffic = ncu_traffic_per_launch()
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
@@ -287,12 +291,18 @@ def run_ours(args, d: Dist):
         "gpu_launches": sum(i["kernel_launches"] for i in infos),
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h), "steps": e2e_steps},
-        "roofline": {"kernel": "k_spmm_dot<float> (block-PCG SpMM, union pattern of A and B)",
+        "roofline": {"kernel": "k_block_pcg<float,20> (persistent block PCG of the W step: "
+                               "p update, SpMM on the union pattern of A and B, x/r update)",
                      "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": (achieved / peak) if achieved else None, "peak_kind": peak_kind,
                      "traffic": traffic,
-                     "bytes_per_launch": spmm_bytes / max(1, spmm_launches),
-                     "ms_per_launch": spmm_ms / max(1, spmm_launches), "launches": spmm_launches},
+                     "bytes_per_launch": pcg_bytes / max(1, pcg_launches),
+                     "ms_per_launch": pcg_ms / max(1, pcg_launches), "launches": pcg_launches,
+                     "spmm_phase": {"achieved": spmm_achieved,
+                                    "frac": (spmm_achieved / peak) if spmm_achieved else None,
+                                    "bytes_per_phase": spmm_bytes / max(1, spmm_phases),
+                                    "ms_per_phase": spmm_ms / max(1, spmm_phases),
+                                    "phases": spmm_phases}},
         "clocks": clk,
     }
     prep_mixed.close()

@@ -67,7 +67,9 @@ class SolveInfo(ctypes.Structure):
                 ("pcg_iters", ctypes.c_int), ("spmm_calls", ctypes.c_int),
                 ("kernel_launches", ctypes.c_int), ("seconds", ctypes.c_double),
                 ("phase_ms", ctypes.c_double * 10), ("pcg_spmm_launches", ctypes.c_int),
-                ("pcg_spmm_ms", ctypes.c_double), ("pcg_spmm_bytes", ctypes.c_double)]
+                ("pcg_spmm_ms", ctypes.c_double), ("pcg_spmm_bytes", ctypes.c_double),
+                ("pcg_kernel_launches", ctypes.c_int), ("pcg_kernel_ms", ctypes.c_double),
+                ("pcg_kernel_bytes", ctypes.c_double)]
 
     PHASES = ("checkconv", "compP", "compRR", "rr_matW", "eig", "compRV", "compW", "linsol",
               "compX", "initX")
@@ -75,7 +77,9 @@ class SolveInfo(ctypes.Structure):
     def as_dict(self) -> dict:
         d = {k: getattr(self, k) for k in ("nconv", "niter", "status", "pcg_iters", "spmm_calls",
                                            "kernel_launches", "seconds", "pcg_spmm_launches",
-                                           "pcg_spmm_ms", "pcg_spmm_bytes")}
+                                           "pcg_spmm_ms", "pcg_spmm_bytes",
+                                           "pcg_kernel_launches", "pcg_kernel_ms",
+                                           "pcg_kernel_bytes")}
         d["phase_ms"] = {p: self.phase_ms[i] for i, p in enumerate(self.PHASES)}
         return d
 

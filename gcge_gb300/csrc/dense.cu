@@ -150,11 +150,23 @@ void lincomb(int n, int k, int m, const double *X, int ldx, const double *C, int
         }
         return;
     }
-    const long long big_blocks = (long long)((n + 63) / 64) * ((m + 31) / 32);
+    // column tile fitted to m (multiple of 4 up to 32) so thin products waste
+    // no FMA lanes; 64-row tiles for tall outputs, 16 x 16 tiles for small ones
+    const int tn = m >= 32 ? 32 : ((m + 3) / 4) * 4;
+    const long long big_blocks = (long long)((n + 63) / 64) * ((m + tn - 1) / tn);
     if (big_blocks >= 2LL * num_sms()) {
-        dim3 grid((n + 63) / 64, (m + 31) / 32);
-        k_lincomb<64, 32, 16, 256><<<grid, 256, 0, st>>>(n, k, m, X, ldx, C, ldc, Y, ldy, beta_dev,
-                                                         incb, alpha);
+        dim3 grid((n + 63) / 64, (m + tn - 1) / tn);
+        switch (tn) {
+#define GCGE_LC_CASE(W)                                                                         \
+    case W:                                                                                    \
+        k_lincomb<64, W, 16, 256><<<grid, 256, 0, st>>>(n, k, m, X, ldx, C, ldc, Y, ldy, beta_dev, \
+                                                        incb, alpha);                          \
+        break;
+            GCGE_LC_CASE(4) GCGE_LC_CASE(8) GCGE_LC_CASE(12) GCGE_LC_CASE(16) GCGE_LC_CASE(20)
+            GCGE_LC_CASE(24) GCGE_LC_CASE(28) GCGE_LC_CASE(32)
+#undef GCGE_LC_CASE
+            default: break;
+        }
     } else {
         dim3 grid((n + 15) / 16, (m + 15) / 16);
         k_lincomb<16, 16, 16, 64><<<grid, 64, 0, st>>>(n, k, m, X, ldx, C, ldc, Y, ldy, beta_dev,
@@ -165,44 +177,65 @@ void lincomb(int n, int k, int m, const double *X, int ldx, const double *C, int
 }
 
 // ---------------------------------------------------------------- Q^T P
-// Block (chunk, mt, wt) accumulates the 32 x 32 tile (mt, wt) of Q^T P over
-// its row chunk; thread t owns row a = t % 32 of the tile and 4 columns.
+// Block (chunk, mt, wt) accumulates the 32 x TW tile (mt, wt) of Q^T P over
+// its row chunk; thread t owns row a = t % 32 of the tile and TW/8 columns.
 constexpr int kGT = 32;
-__global__ void __launch_bounds__(256)
-k_gram(int n, int m, int w, const double *__restrict__ Q, int ldq, const double *__restrict__ P,
-       int ldp, double *__restrict__ part, int rows_per_chunk) {
+template <int TW>
+__device__ __forceinline__ void gram_tile(int n, int m, int w, const double *__restrict__ Q, int ldq,
+                                          const double *__restrict__ P, int ldp,
+                                          double *__restrict__ part, int rows_per_chunk) {
+    constexpr int CPT = TW / 8;
     __shared__ double Qs[kGT][kGT + 1];
-    __shared__ double Ps[kGT][kGT + 1];
+    __shared__ double Ps[kGT][TW + 1];
     const int t = threadIdx.x;
-    const int a = t % kGT, g = t / kGT;  // 8 groups x 4 columns
+    const int a = t % kGT, g = t / kGT;  // 8 groups x CPT columns
     const int chunk = blockIdx.x;
-    const int a0 = blockIdx.y * kGT, b0 = blockIdx.z * kGT;
+    const int a0 = blockIdx.y * kGT, b0 = blockIdx.z * TW;
     const int r_begin = chunk * rows_per_chunk;
     const int r_end = min(n, r_begin + rows_per_chunk);
-    double acc[4] = {0.0, 0.0, 0.0, 0.0};
+    double acc[CPT];
+#pragma unroll
+    for (int j = 0; j < CPT; ++j) acc[j] = 0.0;
     for (int r0 = r_begin; r0 < r_end; r0 += kGT) {
         for (int idx = t; idx < kGT * kGT; idx += 256) {
             const int i = idx % kGT, cc = idx / kGT;
             const int gi = r0 + i;
-            const bool rin = gi < r_end;
-            Qs[i][cc] = (rin && a0 + cc < m) ? Q[gi + (size_t)(a0 + cc) * ldq] : 0.0;
-            Ps[i][cc] = (rin && b0 + cc < w) ? P[gi + (size_t)(b0 + cc) * ldp] : 0.0;
+            Qs[i][cc] = (gi < r_end && a0 + cc < m) ? Q[gi + (size_t)(a0 + cc) * ldq] : 0.0;
+        }
+        for (int idx = t; idx < kGT * TW; idx += 256) {
+            const int i = idx % kGT, cc = idx / kGT;
+            const int gi = r0 + i;
+            Ps[i][cc] = (gi < r_end && b0 + cc < w) ? P[gi + (size_t)(b0 + cc) * ldp] : 0.0;
         }
         __syncthreads();
 #pragma unroll 8
         for (int i = 0; i < kGT; ++i) {
             const double q = Qs[i][a];
 #pragma unroll
-            for (int j = 0; j < 4; ++j) acc[j] = fma(q, Ps[i][g * 4 + j], acc[j]);
+            for (int j = 0; j < CPT; ++j) acc[j] = fma(q, Ps[i][g * CPT + j], acc[j]);
         }
         __syncthreads();
     }
     const size_t base = (size_t)chunk * m * w;
 #pragma unroll
-    for (int j = 0; j < 4; ++j) {
-        const int ga = a0 + a, gb = b0 + g * 4 + j;
+    for (int j = 0; j < CPT; ++j) {
+        const int ga = a0 + a, gb = b0 + g * CPT + j;
         if (ga < m && gb < w) part[base + ga + (size_t)gb * m] = acc[j];
     }
+}
+
+template <int TW>
+__global__ void __launch_bounds__(256)
+k_gram_w(int n, int m, int w, const double *__restrict__ Q, int ldq, const double *__restrict__ P,
+         int ldp, double *__restrict__ part, int rows_per_chunk) {
+    gram_tile<TW>(n, m, w, Q, ldq, P, ldp, part, rows_per_chunk);
+}
+
+// 32 x 32 tile instance with a fixed name (used by GCGE_GramNoAlloc)
+__global__ void __launch_bounds__(256)
+k_gram(int n, int m, int w, const double *__restrict__ Q, int ldq, const double *__restrict__ P,
+       int ldp, double *__restrict__ part, int rows_per_chunk) {
+    gram_tile<32>(n, m, w, Q, ldq, P, ldp, part, rows_per_chunk);
 }
 
 __global__ void k_reduce_chunks(const double *__restrict__ part, int chunks, int m, int w,
@@ -217,7 +250,8 @@ __global__ void k_reduce_chunks(const double *__restrict__ part, int chunks, int
 }
 
 static int gram_chunks(int n, int m, int w) {
-    const int tiles = ((m + kGT - 1) / kGT) * ((w + kGT - 1) / kGT);
+    const int tw = w >= 32 ? 32 : std::max(8, ((w + 7) / 8) * 8);
+    const int tiles = ((m + kGT - 1) / kGT) * ((w + tw - 1) / tw);
     const int want = std::max(1, (3 * num_sms() + tiles - 1) / tiles);
     const int maxc = std::max(1, (n + 127) / 128);
     return std::min(want, maxc);
@@ -239,8 +273,14 @@ void gram(int n, int m, int w, const double *Q, int ldq, const double *P, int ld
     int rpc = (n + chunks - 1) / chunks;
     rpc = (rpc + kGT - 1) / kGT * kGT;
     const int nchunks = (n + rpc - 1) / rpc;
-    dim3 grid(nchunks, (m + kGT - 1) / kGT, (w + kGT - 1) / kGT);
-    k_gram<<<grid, 256, 0, st>>>(n, m, w, Q, ldq, P, ldp, scratch, rpc);
+    const int tw = w >= 32 ? 32 : std::max(8, ((w + 7) / 8) * 8);
+    dim3 grid(nchunks, (m + kGT - 1) / kGT, (w + tw - 1) / tw);
+    switch (tw) {
+        case 8: k_gram_w<8><<<grid, 256, 0, st>>>(n, m, w, Q, ldq, P, ldp, scratch, rpc); break;
+        case 16: k_gram_w<16><<<grid, 256, 0, st>>>(n, m, w, Q, ldq, P, ldp, scratch, rpc); break;
+        case 24: k_gram_w<24><<<grid, 256, 0, st>>>(n, m, w, Q, ldq, P, ldp, scratch, rpc); break;
+        default: k_gram_w<32><<<grid, 256, 0, st>>>(n, m, w, Q, ldq, P, ldp, scratch, rpc); break;
+    }
     GCGE_CHECK_LAUNCH();
     const int tot = m * w;
     k_reduce_chunks<<<std::max(1, std::min((tot + 255) / 256, 4 * num_sms())), 256, 0, st>>>(

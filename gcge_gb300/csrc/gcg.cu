@@ -102,7 +102,7 @@ void SolverCtx::reserve(int n_, int nev_max, int nev_init, int bs, int spmm_nblo
         one.alloc(1);
         fill_value(1, one.p, 1.0, lib_stream());
     }
-    pcg.reserve(n_, std::max(bs, 1), spmm_nblocks);
+    pcg.reserve(n_, std::max(bs, 1));
 }
 
 // ---------------------------------------------------------------- phase timer
@@ -458,15 +458,15 @@ struct GcgRun {
                      st);
         timer.mark(PH_LINSOL);
         const bool rel = std::strcmp(g.compW_cg_tol_type, "rel") == 0;
-        int it;
         if (!mixed) {
             const int kp = rows_width(bsz, 8);
             col_to_rows<double, double>(n, bsz, kp, colp(V, startW), ld, c.xr64.p, st);
             col_to_rows<double, double>(n, bsz, kp, c.bbuf.p, ld, c.br64.p, st);
-            it = block_pcg_rows<double>(c.pcg, c.upat, c.us64.p, c.br64.p, c.xr64.p, c.rr64.p,
-                                        c.pr64.p, c.wr64.p, kp, bsz, g.compW_cg_max_iter,
-                                        g.compW_cg_rate, g.compW_cg_tol, rel, st);
+            block_pcg_rows<double>(c.pcg, c.upat, c.us64.p, c.br64.p, c.xr64.p, c.rr64.p,
+                                   c.pr64.p, c.wr64.p, kp, bsz, g.compW_cg_max_iter,
+                                   g.compW_cg_rate, g.compW_cg_tol, rel, false, st);
             rows_to_col<double, double>(n, bsz, kp, c.xr64.p, colp(V, startW), ld, false, st);
+            spmm_calls++;  // the residual b - S x0 inside the solve
         } else {
             // CG from x0 on S x = b is CG from 0 on S d = b - S x0: the residual
             // is formed in FP64 (it is a difference of nearly equal vectors once
@@ -476,15 +476,12 @@ struct GcgRun {
             spmm<double>(c.upat, c.us64.p, colp(V, startW), ld, c.r64.p, ld, bsz, st);
             axpby(n, bsz, 1.0, c.bbuf.p, ld, -1.0, c.r64.p, ld, st);
             col_to_rows<double, float>(n, bsz, kp, c.r64.p, ld, c.br32.p, st);
-            GCGE_CUDA(cudaMemsetAsync(c.xr32.p, 0, sizeof(float) * (size_t)n * kp, st));
-            it = block_pcg_rows<float>(c.pcg, c.upat, c.us32.p, c.br32.p, c.xr32.p, c.rr32.p,
-                                       c.pr32.p, c.wr32.p, kp, bsz, g.compW_cg_max_iter,
-                                       g.compW_cg_rate, g.compW_cg_tol, rel, st);
+            block_pcg_rows<float>(c.pcg, c.upat, c.us32.p, c.br32.p, c.xr32.p, c.rr32.p,
+                                  c.pr32.p, c.wr32.p, kp, bsz, g.compW_cg_max_iter,
+                                  g.compW_cg_rate, g.compW_cg_tol, rel, true, st);
             rows_to_col<float, double>(n, bsz, kp, c.xr32.p, colp(V, startW), ld, true, st);
             spmm_calls++;
         }
-        pcg_iters += it;
-        spmm_calls += it + 1;
         timer.mark(PH_W);
         endW = orth(colp(V, 0), ld, n, startW, endW, B != nullptr, g.compW_orth_zero_tol,
                     g.compW_orth_max_reorth);
@@ -734,11 +731,17 @@ void gcg_eigensolver(void *Ah, void *Bh, double *eval, void **evec, int nevGiven
         c->pub.nevGiven = nevGiven;
         GCGE_REQUIRE(V->ld == R->ld, GCGE_ERR_ARG, "EigenSolver: leading dimensions differ");
         GcgRun run(*c, A, B, V, R);
-        c->pcg.timing_reset();
+        c->pcg.timing_reset(st);
         const int status = run.run(eval, nevGiven, nevConv);
-        c->info.pcg_spmm_ms = c->pcg.timing_collect_ms();
-        c->info.pcg_spmm_launches = c->pcg.spmm_launches;
+        c->pcg.collect(st);
+        c->info.pcg_spmm_ms = c->pcg.spmm_ms;
+        c->info.pcg_spmm_launches = (int)c->pcg.total_iters;
         c->info.pcg_spmm_bytes = c->pcg.spmm_bytes;
+        c->info.pcg_kernel_launches = c->pcg.launches;
+        c->info.pcg_kernel_ms = c->pcg.kernel_ms;
+        c->info.pcg_kernel_bytes = c->pcg.kernel_bytes;
+        run.pcg_iters = (int)c->pcg.total_iters;
+        run.spmm_calls += (int)c->pcg.total_iters;
         c->info.nconv = *nevConv;
         c->info.niter = c->pub.numIter;
         c->info.status = status;

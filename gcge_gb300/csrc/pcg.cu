@@ -1,20 +1,32 @@
 // Block conjugate gradient on (A + sigma B) x = b for all columns of a block
 // at once (reference BlockPCG, src/ops_lin_sol.c:140-437).
 //
-// The reference keeps a compacted list of unconverged columns and runs one
-// SpMM per contiguous run of them; here every kernel covers the whole block
-// and a per-column `active` flag plays the role of the list: inactive columns
-// keep their x and r (alpha = 0) and drop out of the reductions.  The
-// per-column scalars (rho, p^T w, alpha, beta, residual norms) stay on the
-// device; reductions are two-stage with a fixed summation order, so results
-// are deterministic.  The shifted operator is one SELL matrix S = A + sigma B
-// on the union pattern of A and B (the reference's in-place MatAxpby branch,
-// src/ops_eig_sol_gcg.c:600-608), so each iteration streams one matrix.
+// The whole solve is ONE cooperative (persistent) kernel launch.  Each block
+// owns a contiguous range of SELL slices (balanced by stored entries) and the
+// rows they cover; the iteration runs in three phases separated by grid-wide
+// barriers:
+//   1. p = r + beta p                      (own rows; p = r on the first step)
+//   2. w = S p, partial sums of p^T w      (warp per slice, gathers p rows)
+//      -> the last block to arrive sums the partials: alpha = rho / p^T w
+//   3. x += alpha p, r -= alpha w, partial sums of r^T r
+//      -> the last block: residual norms, convergence test, beta, count
+// so nothing returns to the host between iterations.  The reference keeps a
+// compacted list of unconverged columns and runs one SpMM per contiguous run
+// of them; here a per-column `active` flag plays that role: inactive columns
+// keep x and r (alpha = 0), drop out of the sums, and a 16-byte group of
+// columns that is wholly inactive is neither gathered nor updated.
 //
-// Vectors are row-interleaved n x kp blocks (row i's kp values contiguous,
-// kp = k padded to 16 bytes), which turns the SpMM's gathers into contiguous
-// 16-byte loads.  T = double (FP64 GCG) or float (mixed precision: FP32
-// values, FP32 SpMM accumulation; cross-block sums in double).
+// Cross-block sums are taken by one block in a fixed order, so results are
+// deterministic for a given grid.  The shifted operator is one SELL matrix
+// S = A + sigma B on the union pattern of A and B (the reference's in-place
+// MatAxpby branch, src/ops_eig_sol_gcg.c:600-608), so each iteration streams
+// one matrix.  Vectors are row-interleaved n x kp blocks (row i's kp values
+// contiguous, kp = k padded to 16 bytes): a gathered row is kp/4 float4 (kp/2
+// double2) loads.  T = double (FP64 GCG) or float (mixed precision: FP32
+// values and FP32 accumulation within a block; cross-block sums in double).
+//
+// Every barrier wait is bounded (time and poll count); a wait that runs out
+// sets an error flag that makes all blocks return, and the host reports it.
 #include <algorithm>
 
 #include "common.cuh"
@@ -22,178 +34,612 @@
 
 namespace gcge {
 
-// Deterministic column sums of partials: warp c sums column c.
-__device__ inline double sum_partials(const double *part, int nblocks, int kmax, int c, int lane) {
+namespace {
+
+constexpr unsigned long long kBarrierTimeoutNs = 4000000000ull;  // 4 s
+constexpr long long kBarrierMaxPolls = 1LL << 27;
+
+// 16-byte packs of a row-interleaved block
+template <typename T>
+struct Pk;
+template <>
+struct Pk<float> {
+    static constexpr int L = 4;
+    float v[4];
+    __device__ __forceinline__ static Pk ld(const float *p) {
+        const float4 t = *reinterpret_cast<const float4 *>(p);
+        return Pk{{t.x, t.y, t.z, t.w}};
+    }
+    __device__ __forceinline__ void st(float *p) const {
+        *reinterpret_cast<float4 *>(p) = make_float4(v[0], v[1], v[2], v[3]);
+    }
+};
+template <>
+struct Pk<double> {
+    static constexpr int L = 2;
+    double v[2];
+    __device__ __forceinline__ static Pk ld(const double *p) {
+        const double2 t = *reinterpret_cast<const double2 *>(p);
+        return Pk{{t.x, t.y}};
+    }
+    __device__ __forceinline__ void st(double *p) const {
+        *reinterpret_cast<double2 *>(p) = make_double2(v[0], v[1]);
+    }
+};
+
+__device__ __forceinline__ unsigned long long ld_acquire(const unsigned long long *p) {
+    unsigned long long v;
+    asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ void st_release(unsigned long long *p, unsigned long long v) {
+    asm volatile("st.release.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+__device__ __forceinline__ unsigned long long global_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+// Grid-wide barrier number `epoch` (1, 2, ...).  The last block to arrive runs
+// `last` with all its threads before it releases the others, so the
+// cross-block reductions are done once.  Returns false when the wait ran out
+// (or another block's did); the caller then returns.
+template <typename F>
+__device__ __forceinline__ bool grid_sync(PcgSync *gs, int *error, unsigned long long epoch,
+                                          F &&last) {
+    __shared__ int s_last, s_ok;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        const unsigned long long old = atomicAdd(&gs->arrive, 1ull);
+        const int lst = old + 1ull == epoch * gridDim.x;
+        if (lst) __threadfence();
+        s_last = lst;
+        s_ok = 1;
+    }
+    __syncthreads();
+    if (s_last) {
+        last();
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            __threadfence();
+            st_release(&gs->release, epoch);
+        }
+    } else if (threadIdx.x == 0) {
+        const unsigned long long t0 = global_ns();
+        for (long long poll = 0; ld_acquire(&gs->release) < epoch; ++poll) {
+            if ((poll & 31) == 31 &&
+                (*(volatile int *)error != 0 || poll > kBarrierMaxPolls ||
+                 global_ns() - t0 > kBarrierTimeoutNs)) {
+                atomicExch(error, 1);
+                s_ok = 0;
+                break;
+            }
+            __nanosleep(32);
+        }
+    }
+    __syncthreads();
+    return s_ok != 0;
+}
+
+template <typename T>
+struct PcgArgs {
+    const long long *sp;
+    const int *col;
+    const T *val;
+    int n, nslices;
+    const T *B;
+    T *X, *R, *P, *W;
+    int k, max_iter, rel_tol, x_zero;
+    double rate, tol;
+    double matrix_bytes;  // nnz (v + 4) + 4 (n + 1) of S
+    PcgScalars *sc;
+    PcgSync *sync;
+    PcgStats *stats;
+    double *part;  // 2 x gridDim.x x KP
+};
+
+// Compiler-only ordering point between the 16-byte groups of a row in the
+// streaming phases: keeps one group's loads in flight per thread instead of
+// all of them, which bounds the registers (warps supply the parallelism).
+__device__ __forceinline__ void group_fence() { asm volatile("" ::: "memory"); }
+
+__host__ __device__ constexpr int pow2ceil(int x) {
+    int p = 1;
+    while (p < x) p <<= 1;
+    return p;
+}
+
+// Warp sums of N per-lane column values (N a power of two <= 32): returns, in
+// lane l, the sum over the 32 lanes of column l % N.  The first steps add
+// whole vectors across lanes that differ in high bits; the last log2(N) steps
+// exchange halves (a transposing butterfly), so N = 32 columns take 31
+// shuffles instead of 160.
+template <typename T, int N>
+__device__ __forceinline__ T warp_cols_reduce(T (&v)[N], int lane) {
+#pragma unroll
+    for (int o = 16; o >= N; o >>= 1) {
+#pragma unroll
+        for (int i = 0; i < N; ++i) v[i] += __shfl_xor_sync(0xffffffffu, v[i], o);
+    }
+#pragma unroll
+    for (int h = N / 2; h >= 1; h >>= 1) {
+        const bool up = (lane & h) != 0;
+#pragma unroll
+        for (int i = 0; i < h; ++i) {
+            const T send = up ? v[i] : v[i + h];
+            const T keep = up ? v[i + h] : v[i];
+            v[i] = keep + __shfl_xor_sync(0xffffffffu, send, h);
+        }
+    }
+    return v[0];
+}
+
+// Adds the warp's column sums of acc[0..KP) to wrow[0..KP) (this warp's row of
+// shared accumulators; lane c owns column c).
+template <typename T, int KP>
+__device__ __forceinline__ void warp_cols_add(const T (&acc)[KP], double *wrow, int lane) {
+    constexpr int K1 = KP < 32 ? KP : 32;
+    constexpr int N1 = pow2ceil(K1);
+    T v[N1];
+#pragma unroll
+    for (int i = 0; i < N1; ++i) v[i] = i < K1 ? acc[i] : T(0);
+    const T s = warp_cols_reduce<T, N1>(v, lane);
+    if (lane < K1) wrow[lane] += (double)s;
+    if constexpr (KP > 32) {
+        constexpr int K2 = KP - 32;
+        constexpr int N2 = pow2ceil(K2);
+        T u[N2];
+#pragma unroll
+        for (int i = 0; i < N2; ++i) u[i] = i < K2 ? acc[32 + i] : T(0);
+        const T s2 = warp_cols_reduce<T, N2>(u, lane);
+        if (lane < K2) wrow[32 + lane] += (double)s2;
+    }
+}
+
+// Column sums of the gridDim.x block partials part[b * KP + c] into
+// out[0..KP) (shared memory), fixed order: thread t adds blocks t / KP,
+// t / KP + S, ... of column t % KP (S = threads / KP stripes), then the
+// stripes are added pairwise in a fixed tree.
+template <int KP, int NT>
+__device__ __forceinline__ void grid_cols_sum(const double *part, double *out, double *stripe) {
+    constexpr int S = NT / KP;
+    const int t = threadIdx.x;
     double s = 0.0;
-    for (int b = lane; b < nblocks; b += 32) s += part[(size_t)b * kmax + c];
-    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-    return s;
+    if (t < S * KP) {
+        const int c = t % KP;
+        const int nb = gridDim.x;
+        int b = t / KP;
+        double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0;
+        for (; b + 3 * S < nb; b += 4 * S) {
+            s0 += part[(size_t)b * KP + c];
+            s1 += part[(size_t)(b + S) * KP + c];
+            s2 += part[(size_t)(b + 2 * S) * KP + c];
+            s3 += part[(size_t)(b + 3 * S) * KP + c];
+        }
+        for (; b < nb; b += S) s0 += part[(size_t)b * KP + c];
+        s = (s0 + s1) + (s2 + s3);
+    }
+    stripe[t] = s;
+    __syncthreads();
+    for (int width = S; width > 1;) {
+        const int half = (width + 1) / 2;
+        if (t < (width - half) * KP) stripe[t] += stripe[t + half * KP];
+        __syncthreads();
+        width = half;
+    }
+    if (t < KP) out[t] = stripe[t];
+    __syncthreads();
 }
 
-// Per-column sums of squares of a row block (thread per row, grid-stride).
+// Block shape by row width: 512 threads (two resident blocks, <= 64
+// registers) for rows up to 80 bytes, 512 threads (<= 128 registers) up to
+// 160 bytes, and 256 threads (<= 255 registers) for wider FP64 rows.
 template <typename T, int KP>
-__global__ void __launch_bounds__(256)
-k_rows_colsq(int n, int k, const T *__restrict__ R, double *__restrict__ part, int kmax) {
-    __shared__ double red[8][KP];
-    T acc[KP];
-#pragma unroll
-    for (int c = 0; c < KP; ++c) acc[c] = T(0);
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-#pragma unroll
-        for (int c = 0; c < KP; ++c) {
-            const T v = R[(size_t)i * KP + c];
-            acc[c] = fma(v, v, acc[c]);
-        }
-    }
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-#pragma unroll
-    for (int c = 0; c < KP; ++c) {
-        T v = acc[c];
-        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-        if (lane == 0) red[warp][c] = (double)v;
-    }
-    __syncthreads();
-    for (int c = threadIdx.x; c < KP && c < k; c += blockDim.x) {
-        double s = 0.0;
-        for (int w = 0; w < 8; ++w) s += red[w][c];
-        part[(size_t)blockIdx.x * kmax + c] = s;
-    }
+__host__ __device__ constexpr int pcg_threads() {
+    return sizeof(T) * KP <= 160 ? 512 : 256;
 }
-
-__global__ void k_pcg_normb(int k, const double *__restrict__ part, int nblocks, int kmax,
-                            PcgScalars *sc) {
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    for (int c = warp; c < k; c += blockDim.x / 32) {
-        const double bb = sum_partials(part, nblocks, kmax, c, lane);
-        if (lane == 0) sc->norm_b[c] = sqrt(bb);
-    }
-}
-
-// initial residual norms -> init_res, rho2, active, count
-__global__ void k_pcg_init(int k, const double *__restrict__ part, int nblocks, int kmax,
-                           PcgScalars *sc, double tol) {
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    for (int c = warp; c < k; c += blockDim.x / 32) {
-        const double rr = sum_partials(part, nblocks, kmax, c, lane);
-        if (lane == 0) {
-            sc->rho2[c] = rr;
-            sc->init_res[c] = sqrt(rr);
-            sc->last_res[c] = sqrt(rr);
-            sc->active[c] = sqrt(rr) > tol * sc->norm_b[c] ? 1 : 0;
-            sc->beta[c] = 0.0;
-            sc->alpha[c] = 0.0;
-        }
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        int cnt = 0;
-        for (int c = 0; c < k; ++c) cnt += sc->active[c];
-        for (int c = k; c < kPcgMaxCols; ++c) sc->active[c] = 0;
-        sc->nactive = cnt;
-        sc->niter = 0;
-    }
-}
-
-// p = r + beta p on the active columns (p = r on the first iteration)
 template <typename T, int KP>
-__global__ void k_rows_p(int n, const T *__restrict__ R, T *__restrict__ P,
-                         const PcgScalars *__restrict__ sc) {
-    __shared__ T sbeta[KP];
-    __shared__ int sact[KP];
-    const bool first = sc->niter == 0;
-    for (int c = threadIdx.x; c < KP; c += blockDim.x) {
-        sbeta[c] = (T)sc->beta[c];
-        sact[c] = sc->active[c];
-    }
-    __syncthreads();
-    const size_t total = (size_t)n * KP;
-    for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < total;
-         t += (size_t)gridDim.x * blockDim.x) {
-        const int c = (int)(t % KP);
-        if (!sact[c]) continue;
-        P[t] = first ? R[t] : fma(sbeta[c], P[t], R[t]);
-    }
+__host__ __device__ constexpr int pcg_min_blocks() {
+    return sizeof(T) * KP <= 80 ? 2 : 1;
 }
 
-__global__ void k_pcg_alpha(int k, const double *__restrict__ part, int nblocks, int kmax,
-                            PcgScalars *sc) {
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    for (int c = warp; c < k; c += blockDim.x / 32) {
-        const double ptw = sum_partials(part, nblocks, kmax, c, lane);
-        if (lane == 0) {
-            sc->ptw[c] = ptw;
-            sc->rho1[c] = sc->rho2[c];
-            sc->alpha[c] = sc->active[c] ? sc->rho2[c] / ptw : 0.0;
-        }
-    }
-}
-
-// x += alpha p, r -= alpha w on the active columns, per-column sums of r^2
 template <typename T, int KP>
-__global__ void __launch_bounds__(256)
-k_rows_xr(int n, int k, T *__restrict__ X, T *__restrict__ R, const T *__restrict__ P,
-          const T *__restrict__ W, const PcgScalars *__restrict__ sc, double *__restrict__ part,
-          int kmax) {
-    __shared__ double red[8][KP];
-    __shared__ T salpha[KP];
-    __shared__ int sact[KP];
-    for (int c = threadIdx.x; c < KP; c += blockDim.x) {
-        salpha[c] = (T)sc->alpha[c];
-        sact[c] = sc->active[c];
+__global__ void __launch_bounds__(pcg_threads<T, KP>(), pcg_min_blocks<T, KP>())
+k_block_pcg(PcgArgs<T> a) {
+    constexpr int kPcgThreads = pcg_threads<T, KP>();
+    constexpr int L = Pk<T>::L;
+    constexpr int G = KP / L;  // 16-byte groups per row
+    constexpr int nwarps = kPcgThreads / 32;
+    __shared__ double wred[nwarps][KP];  // per-warp column sums of one phase
+    __shared__ double stripe[kPcgThreads];
+    __shared__ double sum1[KP], sum2[KP];
+    __shared__ T s_coef[KP];
+    __shared__ int s_act[KP];
+    __shared__ int s_gact[G];
+    __shared__ int s_nactive;
+    __shared__ long long s_range[2];
+
+    PcgScalars *sc = a.sc;
+    PcgSync *gs = a.sync;
+    int *error = &a.sync->error;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int k = a.k, n = a.n;
+    const double vb = (double)sizeof(T);
+
+    // per-warp accumulators: clear, and flush (fixed-order sum over warps)
+    auto wred_zero = [&]() {
+        for (int i = tid; i < nwarps * KP; i += kPcgThreads) (&wred[0][0])[i] = 0.0;
+        __syncthreads();
+    };
+    auto wred_flush = [&](double *out) {
+        __syncthreads();
+        if (tid < KP) {
+            double s = 0.0;
+#pragma unroll
+            for (int w = 0; w < nwarps; ++w) s += wred[w][tid];
+            out[tid] = s;
+        }
+        __syncthreads();
+    };
+
+    // slice range of this block, balanced by stored entries
+    if (tid < 2) {
+        const long long total = a.sp[a.nslices];
+        const long long target = total * (long long)(blockIdx.x + tid) / gridDim.x;
+        int lo = 0, hi = a.nslices;  // first slice s with sp[s] >= target
+        while (lo < hi) {
+            const int mid = (lo + hi) >> 1;
+            if (a.sp[mid] < target) lo = mid + 1;
+            else hi = mid;
+        }
+        s_range[tid] = (blockIdx.x + tid == gridDim.x) ? a.nslices : lo;
     }
     __syncthreads();
-    T acc[KP];
+    const int s0 = (int)s_range[0], s1 = (int)s_range[1];
+    const int r0 = min(n, 32 * s0), r1 = min(n, 32 * s1);
+    double *part1 = a.part + (size_t)blockIdx.x * KP;
+    double *part2 = a.part + (size_t)(gridDim.x + blockIdx.x) * KP;
+    unsigned long long epoch = 0;
+
+    auto finish = [&](bool ok) {
+        if (blockIdx.x == 0 && tid == 0) {
+            if (!ok || *(volatile int *)error) a.stats->error = 1;
+            a.stats->launches += 1;
+            a.stats->iters += (unsigned long long)sc->niter;
+        }
+    };
+
+    // ---------------- r = b - S x (or r = b for x = 0), p = 0, norms
+    wred_zero();
+    if (a.x_zero) {
+        T racc[KP];
 #pragma unroll
-    for (int c = 0; c < KP; ++c) acc[c] = T(0);
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        for (int c = 0; c < KP; ++c) racc[c] = T(0);
+        for (int row = r0 + tid; row < r1; row += kPcgThreads) {
+            const size_t o = (size_t)row * KP;
 #pragma unroll
-        for (int c = 0; c < KP; ++c) {
-            if (!sact[c]) continue;
-            const size_t o = (size_t)i * KP + c;
-            const T a = salpha[c];
-            X[o] = fma(a, P[o], X[o]);
-            const T rn = fma(-a, W[o], R[o]);
-            R[o] = rn;
-            acc[c] = fma(rn, rn, acc[c]);
+            for (int u = 0; u < G; ++u) {
+                const Pk<T> b = Pk<T>::ld(a.B + o + u * L);
+                Pk<T> z;
+#pragma unroll
+                for (int q = 0; q < L; ++q) {
+                    z.v[q] = T(0);
+                    racc[u * L + q] = fma(b.v[q], b.v[q], racc[u * L + q]);
+                }
+                b.st(a.R + o + u * L);
+                z.st(a.X + o + u * L);
+                z.st(a.P + o + u * L);
+                group_fence();
+            }
+        }
+        warp_cols_add<T, KP>(racc, wred[warp], lane);
+    } else {
+        for (int s = s0 + warp; s < s1; s += nwarps) {
+            T acc[KP];
+#pragma unroll
+            for (int c = 0; c < KP; ++c) acc[c] = T(0);
+            const long long beg = a.sp[s], end = a.sp[s + 1];
+#pragma unroll 1
+            for (long long e = beg + lane; e < end; e += 32) {
+                const int j = __ldg(a.col + e);
+                const T v = __ldg(a.val + e);
+                const T *xj = a.X + (size_t)j * KP;
+#pragma unroll
+                for (int u = 0; u < G; ++u) {
+                    const Pk<T> x = Pk<T>::ld(xj + u * L);
+#pragma unroll
+                    for (int q = 0; q < L; ++q) acc[u * L + q] = fma(v, x.v[q], acc[u * L + q]);
+                }
+            }
+            const int row = s * 32 + lane;
+            if (row < n) {
+                const size_t o = (size_t)row * KP;
+#pragma unroll
+                for (int u = 0; u < G; ++u) {
+                    const Pk<T> b = Pk<T>::ld(a.B + o + u * L);
+                    Pk<T> r, z;
+#pragma unroll
+                    for (int q = 0; q < L; ++q) {
+                        r.v[q] = b.v[q] - acc[u * L + q];
+                        z.v[q] = T(0);
+                        acc[u * L + q] = r.v[q] * r.v[q];
+                    }
+                    r.st(a.R + o + u * L);
+                    z.st(a.P + o + u * L);
+                }
+            } else {
+#pragma unroll
+                for (int c = 0; c < KP; ++c) acc[c] = T(0);
+            }
+            warp_cols_add<T, KP>(acc, wred[warp], lane);
         }
     }
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    wred_flush(part1);
+    if (a.rel_tol) {
+        wred_zero();
+        T bacc[KP];
 #pragma unroll
-    for (int c = 0; c < KP; ++c) {
-        T v = acc[c];
-        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-        if (lane == 0) red[warp][c] = (double)v;
+        for (int c = 0; c < KP; ++c) bacc[c] = T(0);
+        for (int row = r0 + tid; row < r1; row += kPcgThreads) {
+            const size_t o = (size_t)row * KP;
+#pragma unroll
+            for (int u = 0; u < G; ++u) {
+                const Pk<T> b = Pk<T>::ld(a.B + o + u * L);
+#pragma unroll
+                for (int q = 0; q < L; ++q) bacc[u * L + q] = fma(b.v[q], b.v[q], bacc[u * L + q]);
+                group_fence();
+            }
+        }
+        warp_cols_add<T, KP>(bacc, wred[warp], lane);
+        wred_flush(part2);
     }
-    __syncthreads();
-    for (int c = threadIdx.x; c < KP && c < k; c += blockDim.x) {
-        double s = 0.0;
-        for (int w = 0; w < 8; ++w) s += red[w][c];
-        part[(size_t)blockIdx.x * kmax + c] = s;
+    // initial residual norms (src/ops_lin_sol.c:171-233)
+    if (!grid_sync(gs, error, ++epoch, [&]() {
+            grid_cols_sum<KP, kPcgThreads>(a.part, sum1, stripe);
+            if (a.rel_tol) grid_cols_sum<KP, kPcgThreads>(a.part + (size_t)gridDim.x * KP, sum2, stripe);
+            if (tid < kPcgMaxCols) {
+                const int c = tid;
+                if (c < k) {
+                    const double nb = a.rel_tol ? sqrt(sum2[c]) : 1.0;
+                    const double rr = sum1[c];
+                    sc->norm_b[c] = nb;
+                    sc->rho2[c] = rr;
+                    sc->init_res[c] = sqrt(rr);
+                    sc->last_res[c] = sqrt(rr);
+                    sc->active[c] = sqrt(rr) > a.tol * nb ? 1 : 0;
+                    sc->beta[c] = 0.0;
+                    sc->alpha[c] = 0.0;
+                } else {
+                    sc->active[c] = 0;
+                }
+            }
+            __syncthreads();
+            if (tid == 0) {
+                int cnt = 0;
+                for (int c = 0; c < k; ++c) cnt += sc->active[c];
+                sc->nactive = cnt;
+                sc->niter = 0;
+                a.stats->kernel_bytes +=
+                    a.x_zero ? 4.0 * n * KP * vb : a.matrix_bytes + 4.0 * n * KP * vb;
+            }
+        })) {
+        finish(false);
+        return;
     }
+
+    for (int it = 0; it < a.max_iter; ++it) {
+        // ---------------- phase 1: p = r + beta p
+        if (tid < KP) {
+            s_act[tid] = sc->active[tid];
+            s_coef[tid] = (T)sc->beta[tid];
+        }
+        if (tid == 0) s_nactive = sc->nactive;
+        __syncthreads();
+        if (s_nactive == 0) break;
+        if (tid < G) {
+            int any = 0;
+            for (int q = 0; q < L; ++q) any |= s_act[tid * L + q];
+            s_gact[tid] = any;
+        }
+        __syncthreads();
+        const bool first = it == 0;
+        for (int row = r0 + tid; row < r1; row += kPcgThreads) {
+            const size_t o = (size_t)row * KP;
+#pragma unroll
+            for (int u = 0; u < G; ++u) {
+                if (!s_gact[u]) continue;
+                const Pk<T> r = Pk<T>::ld(a.R + o + u * L);
+                Pk<T> p = Pk<T>::ld(a.P + o + u * L);
+#pragma unroll
+                for (int q = 0; q < L; ++q)
+                    if (s_act[u * L + q])
+                        p.v[q] = first ? r.v[q] : fma(s_coef[u * L + q], p.v[q], r.v[q]);
+                p.st(a.P + o + u * L);
+                group_fence();
+            }
+        }
+        wred_zero();
+        if (!grid_sync(gs, error, ++epoch, [&]() {
+                if (tid == 0) a.sync->t_spmm = global_ns();
+            })) {
+            finish(false);
+            return;
+        }
+
+        // ---------------- phase 2: w = S p, p^T w
+        {
+            bool ga[G];
+#pragma unroll
+            for (int u = 0; u < G; ++u) ga[u] = s_gact[u] != 0;
+            for (int s = s0 + warp; s < s1; s += nwarps) {
+                T acc[KP];
+#pragma unroll
+                for (int c = 0; c < KP; ++c) acc[c] = T(0);
+                const long long beg = a.sp[s], end = a.sp[s + 1];
+#pragma unroll 1
+    #pragma unroll 1
+            for (long long e = beg + lane; e < end; e += 32) {
+                    const int j = __ldg(a.col + e);
+                    const T v = __ldg(a.val + e);
+                    const T *pj = a.P + (size_t)j * KP;
+#pragma unroll
+                    for (int u = 0; u < G; ++u) {
+                        if (!ga[u]) continue;
+                        const Pk<T> x = Pk<T>::ld(pj + u * L);
+#pragma unroll
+                        for (int q = 0; q < L; ++q) acc[u * L + q] = fma(v, x.v[q], acc[u * L + q]);
+                    }
+                }
+                const int row = s * 32 + lane;
+                if (row < n) {
+                    const size_t o = (size_t)row * KP;
+#pragma unroll
+                    for (int u = 0; u < G; ++u) {
+                        if (!ga[u]) continue;
+                        Pk<T> w;
+#pragma unroll
+                        for (int q = 0; q < L; ++q) w.v[q] = acc[u * L + q];
+                        w.st(a.W + o + u * L);
+                        const Pk<T> p = Pk<T>::ld(a.P + o + u * L);
+#pragma unroll
+                        for (int q = 0; q < L; ++q)
+                            acc[u * L + q] = s_act[u * L + q] ? p.v[q] * w.v[q] : T(0);
+                    }
+                } else {
+#pragma unroll
+                    for (int c = 0; c < KP; ++c) acc[c] = T(0);
+                }
+#pragma unroll
+                for (int u = 0; u < G; ++u)
+                    if (!ga[u]) {
+#pragma unroll
+                        for (int q = 0; q < L; ++q) acc[u * L + q] = T(0);
+                    }
+                warp_cols_add<T, KP>(acc, wred[warp], lane);
+            }
+            wred_flush(part1);
+        }
+        // alpha = rho / p^T w (src/ops_lin_sol.c:300-330)
+        if (!grid_sync(gs, error, ++epoch, [&]() {
+                grid_cols_sum<KP, kPcgThreads>(a.part, sum1, stripe);
+                if (tid < k) {
+                    const int c = tid;
+                    const double ptw = sum1[c];
+                    sc->ptw[c] = ptw;
+                    sc->rho1[c] = sc->rho2[c];
+                    sc->alpha[c] = sc->active[c] ? sc->rho2[c] / ptw : 0.0;
+                }
+                if (tid == 0) {
+                    int gact = 0;
+                    for (int u = 0; u < G; ++u) gact += s_gact[u];
+                    const double vec = (double)n * gact * L * vb;
+                    a.stats->spmm_ns += global_ns() - a.sync->t_spmm;
+                    // SpMM: the matrix once, p read once, w written once
+                    a.stats->spmm_bytes += a.matrix_bytes + 2.0 * vec;
+                    // iteration: phase 1 (r, p read; p written), phase 2 (p
+                    // gathered and re-read, w written), phase 3 (x, p, r, w
+                    // read; x, r written)
+                    a.stats->kernel_bytes += a.matrix_bytes + 12.0 * vec;
+                }
+            })) {
+            finish(false);
+            return;
+        }
+
+        // ---------------- phase 3: x += alpha p, r -= alpha w, r^T r
+        if (tid < KP) s_coef[tid] = (T)sc->alpha[tid];
+        wred_zero();
+        {
+            T racc[KP];
+#pragma unroll
+            for (int c = 0; c < KP; ++c) racc[c] = T(0);
+            for (int row = r0 + tid; row < r1; row += kPcgThreads) {
+                const size_t o = (size_t)row * KP;
+#pragma unroll
+                for (int u = 0; u < G; ++u) {
+                    if (!s_gact[u]) continue;
+                    Pk<T> x = Pk<T>::ld(a.X + o + u * L);
+                    Pk<T> r = Pk<T>::ld(a.R + o + u * L);
+                    const Pk<T> p = Pk<T>::ld(a.P + o + u * L);
+                    const Pk<T> w = Pk<T>::ld(a.W + o + u * L);
+#pragma unroll
+                    for (int q = 0; q < L; ++q) {
+                        const int c = u * L + q;
+                        if (s_act[c]) {
+                            const T al = s_coef[c];
+                            x.v[q] = fma(al, p.v[q], x.v[q]);
+                            r.v[q] = fma(-al, w.v[q], r.v[q]);
+                            racc[c] = fma(r.v[q], r.v[q], racc[c]);
+                        }
+                    }
+                    x.st(a.X + o + u * L);
+                    r.st(a.R + o + u * L);
+                    group_fence();
+                }
+            }
+            warp_cols_add<T, KP>(racc, wred[warp], lane);
+            wred_flush(part1);
+        }
+        // convergence test of src/ops_lin_sol.c:383-394 and beta for the next step
+        if (!grid_sync(gs, error, ++epoch, [&]() {
+                grid_cols_sum<KP, kPcgThreads>(a.part, sum1, stripe);
+                if (tid < k && sc->active[tid]) {
+                    const int c = tid;
+                    const double rr = sum1[c];
+                    sc->rho2[c] = rr;
+                    const double res = sqrt(rr);
+                    sc->last_res[c] = res;
+                    sc->beta[c] = rr / sc->rho1[c];
+                    if (!(res > a.rate * sc->init_res[c] && res > a.tol * sc->norm_b[c]))
+                        sc->active[c] = 0;
+                }
+                __syncthreads();
+                if (tid == 0) {
+                    int cnt = 0;
+                    for (int c = 0; c < k; ++c) cnt += sc->active[c];
+                    sc->nactive = cnt;
+                    sc->niter += 1;
+                }
+            })) {
+            finish(false);
+            return;
+        }
+    }
+    finish(true);
 }
 
-// convergence test of src/ops_lin_sol.c:383-394 and beta for the next step
-__global__ void k_pcg_conv(int k, const double *__restrict__ part, int nblocks, int kmax,
-                           PcgScalars *sc, double rate, double tol) {
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    for (int c = warp; c < k; c += blockDim.x / 32) {
-        const double rr = sum_partials(part, nblocks, kmax, c, lane);
-        if (lane == 0 && sc->active[c]) {
-            sc->rho2[c] = rr;
-            const double res = sqrt(rr);
-            sc->last_res[c] = res;
-            sc->beta[c] = rr / sc->rho1[c];
-            if (!(res > rate * sc->init_res[c] && res > tol * sc->norm_b[c])) sc->active[c] = 0;
-        }
+int num_sms_pcg() {
+    static int sms = 0;
+    if (!sms) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if (sms <= 0) sms = 148;
     }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        int cnt = 0;
-        for (int c = 0; c < k; ++c) cnt += sc->active[c];
-        sc->nactive = cnt;
-        sc->niter += 1;
-    }
+    return sms;
 }
+
+constexpr int kMaxBlocksPerSm = 4;
+
+template <typename T, int KP>
+void launch_block_pcg(PcgArgs<T> a, cudaStream_t st) {
+    static int bpsm = 0;
+    if (bpsm == 0) {
+        GCGE_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bpsm, k_block_pcg<T, KP>,
+                                                                pcg_threads<T, KP>(), 0));
+        GCGE_REQUIRE(bpsm >= 1, GCGE_ERR_CUDA, "block PCG: kernel does not fit on an SM");
+        bpsm = std::min(bpsm, kMaxBlocksPerSm);
+    }
+    const int nb = std::max(1, std::min(bpsm * num_sms_pcg(), a.nslices));
+    void *args[] = {&a};
+    GCGE_CUDA(cudaLaunchCooperativeKernel((const void *)k_block_pcg<T, KP>, dim3(nb),
+                                          dim3(pcg_threads<T, KP>()), args, 0, st));
+    count_launch();
+}
+
+}  // namespace
 
 // column-major (S, ld) <-> row-interleaved (T, kp); padding columns are zero
 template <typename S, typename T>
@@ -219,18 +665,6 @@ __global__ void k_rows_to_col(int n, int k, int kp, const T *__restrict__ X, D *
     }
 }
 
-static int num_sms_pcg() {
-    static int sms = 0;
-    if (!sms) {
-        int dev = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        if (sms <= 0) sms = 148;
-    }
-    return sms;
-}
-static int row_blocks(int n) { return std::max(1, std::min((n + 255) / 256, 2 * num_sms_pcg())); }
-
 template <typename S, typename T>
 void col_to_rows(int n, int k, int kp, const S *X, int ldx, T *Y, cudaStream_t st) {
     const size_t total = (size_t)n * kp;
@@ -254,113 +688,129 @@ template void rows_to_col<double, double>(int, int, int, const double *, double 
 template void rows_to_col<float, double>(int, int, int, const float *, double *, int, bool,
                                          cudaStream_t);
 
-void PcgWork::timing_reset() {
+void PcgWork::timing_reset(cudaStream_t st) {
     ev_used = 0;
-    spmm_bytes = 0.0;
-    spmm_launches = 0;
+    launches = 0;
+    kernel_ms = spmm_ms = kernel_bytes = spmm_bytes = 0.0;
+    total_iters = 0;
+    GCGE_CUDA(cudaMemsetAsync(stats.p, 0, sizeof(PcgStats), st));
 }
-double PcgWork::timing_collect_ms() {
+void PcgWork::collect(cudaStream_t st) {
+    GCGE_CUDA(cudaMemcpyAsync(h_stats.p, stats.p, sizeof(PcgStats), cudaMemcpyDeviceToHost, st));
+    GCGE_CUDA(cudaStreamSynchronize(st));
     double ms = 0.0;
     for (size_t i = 0; i + 1 < ev_used; i += 2) {
         float t = 0.f;
-        if (cudaEventSynchronize(ev[i + 1]) == cudaSuccess &&
-            cudaEventElapsedTime(&t, ev[i], ev[i + 1]) == cudaSuccess)
-            ms += t;
+        if (cudaEventElapsedTime(&t, ev[i], ev[i + 1]) == cudaSuccess) ms += t;
     }
-    return ms;
+    kernel_ms = ms;
+    spmm_ms = (double)h_stats.p->spmm_ns * 1e-6;
+    kernel_bytes = h_stats.p->kernel_bytes;
+    spmm_bytes = h_stats.p->spmm_bytes;
+    total_iters = (long long)h_stats.p->iters;
+    GCGE_REQUIRE(h_stats.p->error == 0, GCGE_ERR_CUDA,
+                 "block PCG: a grid barrier wait timed out");
 }
 PcgWork::~PcgWork() {
     for (auto e : ev) cudaEventDestroy(e);
 }
 
-void PcgWork::reserve(int n, int kmax_, int spmm_nblocks) {
+void PcgWork::reserve(int n, int kmax_) {
+    (void)n;
     kmax = std::max(kmax_, 40);
-    const size_t need = (size_t)std::max(spmm_nblocks, 2 * num_sms_pcg()) * kmax;
-    part.alloc(std::max<size_t>(need, 1));
-    sc.alloc(1);
-    h_sc.alloc(1);
+    part.alloc((size_t)2 * kMaxBlocksPerSm * num_sms_pcg() * kPcgMaxCols);
+    if (!sc.p) {
+        sc.alloc(1);
+        sync.alloc(1);
+        stats.alloc(1);
+        h_sc.alloc(1);
+        h_stats.alloc(1);
+        GCGE_CUDA(cudaMemsetAsync(stats.p, 0, sizeof(PcgStats), lib_stream()));
+    }
+}
+
+int pcg_last_iters(PcgWork &wk, cudaStream_t st) {
+    GCGE_CUDA(cudaMemcpyAsync(wk.h_sc.p, wk.sc.p, sizeof(PcgScalars), cudaMemcpyDeviceToHost, st));
+    GCGE_CUDA(cudaMemcpyAsync(wk.h_stats.p, wk.stats.p, sizeof(PcgStats), cudaMemcpyDeviceToHost,
+                              st));
+    GCGE_CUDA(cudaStreamSynchronize(st));
+    GCGE_REQUIRE(wk.h_stats.p->error == 0, GCGE_ERR_CUDA,
+                 "block PCG: a grid barrier wait timed out");
+    return wk.h_sc.p->niter;
 }
 
 template <typename T>
-int block_pcg_rows(PcgWork &wk, const SellPattern &pat, const T *sval, const T *Bv, T *X, T *R,
-                   T *P, T *W, int kp, int k, int max_iter, double rate, double tol, bool rel_tol,
-                   cudaStream_t st) {
-    GCGE_REQUIRE(k >= 1 && k <= kp && kp <= 40 && k <= kPcgMaxCols, GCGE_ERR_ARG,
+void block_pcg_rows(PcgWork &wk, const SellPattern &pat, const T *sval, const T *Bv, T *X, T *R,
+                    T *P, T *W, int kp, int k, int max_iter, double rate, double tol, bool rel_tol,
+                    bool x_zero, cudaStream_t st) {
+    constexpr int L = 16 / (int)sizeof(T);
+    GCGE_REQUIRE(k >= 1 && k <= kp && kp <= 40 && kp % L == 0 && k <= kPcgMaxCols, GCGE_ERR_ARG,
                  "block_pcg: block width");
-    const int n = pat.n;
-    const int rb = row_blocks(n);
-    // norm_b (abs: 1; rel: ||b||), src/ops_lin_sol.c:171-197
-    {
-        PcgScalars &hs = *wk.h_sc.p;
-        std::fill(hs.norm_b, hs.norm_b + kPcgMaxCols, 1.0);
-        GCGE_CUDA(cudaMemcpyAsync(&wk.sc.p->norm_b[0], hs.norm_b, sizeof(double) * kPcgMaxCols,
-                                  cudaMemcpyHostToDevice, st));
-    }
-    if (rel_tol) {
-        GCGE_KP_DISPATCH(T, kp, (k_rows_colsq<T, KP><<<rb, 256, 0, st>>>(n, k, Bv, wk.part.p, wk.kmax)));
-        GCGE_CHECK_LAUNCH();
-        k_pcg_normb<<<1, 1024, 0, st>>>(k, wk.part.p, rb, wk.kmax, wk.sc.p);
-        GCGE_CHECK_LAUNCH();
-        count_launch(2);
-    }
-    // r = b - S x  (src/ops_lin_sol.c:202-221)
-    spmm_rows<T>(pat, sval, X, R, kp, k, nullptr, nullptr, 0, false, st);
-    if constexpr (sizeof(T) == 8)
-        axpby(n * kp, 1, 1.0, (const double *)Bv, n * kp, -1.0, (double *)R, n * kp, st);
-    else
-        axpby_f32(n * kp, 1, 1.0f, (const float *)Bv, n * kp, -1.0f, (float *)R, n * kp, st);
-    GCGE_KP_DISPATCH(T, kp, (k_rows_colsq<T, KP><<<rb, 256, 0, st>>>(n, k, R, wk.part.p, wk.kmax)));
-    GCGE_CHECK_LAUNCH();
-    k_pcg_init<<<1, 1024, 0, st>>>(k, wk.part.p, rb, wk.kmax, wk.sc.p, tol);
-    GCGE_CHECK_LAUNCH();
-    count_launch(2);
-    int it = 0;
-    const int pgrid = std::max(1, std::min((int)(((size_t)n * kp + 255) / 256), 16 * num_sms_pcg()));
-    for (it = 0; it < max_iter; ++it) {
-        GCGE_CUDA(cudaMemcpyAsync(&wk.h_sc.p->nactive, &wk.sc.p->nactive, sizeof(int),
-                                  cudaMemcpyDeviceToHost, st));
-        GCGE_CUDA(cudaStreamSynchronize(st));
-        const int nactive = wk.h_sc.p->nactive;
-        if (nactive == 0) break;
-        GCGE_KP_DISPATCH(T, kp, (k_rows_p<T, KP><<<pgrid, 256, 0, st>>>(n, R, P, wk.sc.p)));
-        GCGE_CHECK_LAUNCH();
-        const bool timed = wk.ev_used + 2 <= 65536;
-        if (timed) {
-            while (wk.ev.size() < wk.ev_used + 2) {
-                cudaEvent_t e;
-                GCGE_CUDA(cudaEventCreate(&e));
-                wk.ev.push_back(e);
-            }
-            GCGE_CUDA(cudaEventRecord(wk.ev[wk.ev_used], st));
+    if (pat.n == 0) return;
+    PcgArgs<T> a;
+    a.sp = pat.slice_ptr.p;
+    a.col = pat.col.p;
+    a.val = sval;
+    a.n = pat.n;
+    a.nslices = pat.nslices;
+    a.B = Bv;
+    a.X = X;
+    a.R = R;
+    a.P = P;
+    a.W = W;
+    a.k = k;
+    a.max_iter = std::max(0, max_iter);
+    a.rel_tol = rel_tol ? 1 : 0;
+    a.x_zero = x_zero ? 1 : 0;
+    a.rate = rate;
+    a.tol = tol;
+    a.matrix_bytes = (double)pat.nnz * (sizeof(T) + 4) + 4.0 * (pat.n + 1);
+    a.sc = wk.sc.p;
+    a.sync = wk.sync.p;
+    a.stats = wk.stats.p;
+    a.part = wk.part.p;
+    GCGE_CUDA(cudaMemsetAsync(wk.sync.p, 0, sizeof(PcgSync), st));
+    const bool timed = wk.ev_used + 2 <= 65536;
+    if (timed) {
+        while (wk.ev.size() < wk.ev_used + 2) {
+            cudaEvent_t e;
+            GCGE_CUDA(cudaEventCreate(&e));
+            wk.ev.push_back(e);
         }
-        const int nb = spmm_rows<T>(pat, sval, P, W, kp, k, &wk.sc.p->active[0], wk.part.p,
-                                    wk.kmax, true, st);
-        if (timed) {
-            GCGE_CUDA(cudaEventRecord(wk.ev[wk.ev_used + 1], st));
-            wk.ev_used += 2;
-        }
-        // algorithmic bytes: the matrix once, the kp-wide rows of p read once
-        // and of w written once (inactive columns ride along in the rows)
-        wk.spmm_bytes += (double)pat.nnz * (sizeof(T) + 4) + 4.0 * (n + 1) +
-                         2.0 * n * kp * sizeof(T);
-        wk.spmm_launches++;
-        k_pcg_alpha<<<1, 1024, 0, st>>>(k, wk.part.p, nb, wk.kmax, wk.sc.p);
-        GCGE_CHECK_LAUNCH();
-        GCGE_KP_DISPATCH(T, kp, (k_rows_xr<T, KP><<<rb, 256, 0, st>>>(n, k, X, R, P, W, wk.sc.p,
-                                                                      wk.part.p, wk.kmax)));
-        GCGE_CHECK_LAUNCH();
-        k_pcg_conv<<<1, 1024, 0, st>>>(k, wk.part.p, rb, wk.kmax, wk.sc.p, rate, tol);
-        GCGE_CHECK_LAUNCH();
-        count_launch(4);
+        GCGE_CUDA(cudaEventRecord(wk.ev[wk.ev_used], st));
     }
-    return it;
+    if constexpr (sizeof(T) == 4) {
+        switch (kp) {
+#define GCGE_PCG_CASE(W_)                                     \
+    case W_:                                                  \
+        launch_block_pcg<T, W_>(a, st);                       \
+        break;
+            GCGE_PCG_CASE(4) GCGE_PCG_CASE(8) GCGE_PCG_CASE(12) GCGE_PCG_CASE(16)
+            GCGE_PCG_CASE(20) GCGE_PCG_CASE(24) GCGE_PCG_CASE(28) GCGE_PCG_CASE(32)
+            GCGE_PCG_CASE(36) GCGE_PCG_CASE(40)
+            default: throw CudaError{GCGE_ERR_ARG, "block_pcg: unsupported width"};
+        }
+    } else {
+        switch (kp) {
+            GCGE_PCG_CASE(2) GCGE_PCG_CASE(4) GCGE_PCG_CASE(6) GCGE_PCG_CASE(8)
+            GCGE_PCG_CASE(12) GCGE_PCG_CASE(16) GCGE_PCG_CASE(20) GCGE_PCG_CASE(24)
+            GCGE_PCG_CASE(28) GCGE_PCG_CASE(32) GCGE_PCG_CASE(36) GCGE_PCG_CASE(40)
+#undef GCGE_PCG_CASE
+            default: throw CudaError{GCGE_ERR_ARG, "block_pcg: unsupported width"};
+        }
+    }
+    if (timed) {
+        GCGE_CUDA(cudaEventRecord(wk.ev[wk.ev_used + 1], st));
+        wk.ev_used += 2;
+    }
+    wk.launches++;
 }
 
-template int block_pcg_rows<double>(PcgWork &, const SellPattern &, const double *, const double *,
-                                    double *, double *, double *, double *, int, int, int, double,
-                                    double, bool, cudaStream_t);
-template int block_pcg_rows<float>(PcgWork &, const SellPattern &, const float *, const float *,
-                                   float *, float *, float *, float *, int, int, int, double,
-                                   double, bool, cudaStream_t);
+template void block_pcg_rows<double>(PcgWork &, const SellPattern &, const double *, const double *,
+                                     double *, double *, double *, double *, int, int, int, double,
+                                     double, bool, bool, cudaStream_t);
+template void block_pcg_rows<float>(PcgWork &, const SellPattern &, const float *, const float *,
+                                    float *, float *, float *, float *, int, int, int, double,
+                                    double, bool, bool, cudaStream_t);
 
 }  // namespace gcge

@@ -16,29 +16,58 @@ struct PcgScalars {
     int niter;
 };
 
+// Grid barrier state of the persistent solve kernel (zeroed before each
+// launch) and counters that accumulate over launches.
+struct PcgSync {
+    unsigned long long arrive;   // block arrivals at barriers, over the launch
+    unsigned long long release;  // number of the last barrier released
+    unsigned long long t_spmm;   // globaltimer at the start of the SpMM phase
+    int error;                   // a barrier wait ran out of time
+    int pad;
+};
+struct PcgStats {
+    double kernel_bytes;         // algorithmic bytes of the whole solves
+    double spmm_bytes;           // algorithmic bytes of their SpMM phases
+    unsigned long long spmm_ns;  // summed SpMM phase time (device clock)
+    unsigned long long iters;    // summed iterations
+    unsigned long long launches;
+    int error;                   // sticky: some launch's barrier timed out
+    int pad;
+};
+
 struct PcgWork {
     int kmax = 0;
     DevBuf<double> part;
     DevBuf<PcgScalars> sc;
+    DevBuf<PcgSync> sync;
+    DevBuf<PcgStats> stats;
     PinnedBuf<PcgScalars> h_sc;
-    // per-launch timing of the SpMM inside the iterations (event pairs)
+    PinnedBuf<PcgStats> h_stats;
+    // whole-kernel timing (event pairs) and algorithmic bytes of the solves
     std::vector<cudaEvent_t> ev;
     size_t ev_used = 0;
-    double spmm_bytes = 0.0;
-    int spmm_launches = 0;
-    void reserve(int n, int kmax, int spmm_nblocks);
-    void timing_reset();
-    double timing_collect_ms();  // synchronises, sums the recorded intervals
+    int launches = 0;
+    void reserve(int n, int kmax);
+    void timing_reset(cudaStream_t st);
+    // synchronises; fills the totals below and throws if a barrier timed out
+    void collect(cudaStream_t st);
+    double kernel_ms = 0.0, spmm_ms = 0.0, kernel_bytes = 0.0, spmm_bytes = 0.0;
+    long long total_iters = 0;
     ~PcgWork();
 };
 
 // Solve S x = b column-wise (S on the SELL pattern `pat` with values sval)
-// starting from x.  B, X, R, P, W are row-interleaved n x kp blocks (row i at
-// i*kp, padding columns zero).  Returns the number of iterations run.
+// starting from x (or from 0 when x_zero, in which case x need not be
+// initialised).  B, X, R, P, W are row-interleaved n x kp blocks (row i at
+// i*kp, padding columns of B and X zero).  One cooperative launch runs the
+// whole iteration; the iteration count and any error stay on the device
+// (PcgWork::collect, or pcg_last_iters after a synchronisation).
 template <typename T>
-int block_pcg_rows(PcgWork &wk, const SellPattern &pat, const T *sval, const T *B, T *X, T *R,
-                   T *P, T *W, int kp, int k, int max_iter, double rate, double tol, bool rel_tol,
-                   cudaStream_t st);
+void block_pcg_rows(PcgWork &wk, const SellPattern &pat, const T *sval, const T *B, T *X, T *R,
+                    T *P, T *W, int kp, int k, int max_iter, double rate, double tol, bool rel_tol,
+                    bool x_zero, cudaStream_t st);
+// Iterations of the last solve (synchronises the stream).
+int pcg_last_iters(PcgWork &wk, cudaStream_t st);
 
 // Column-major (ld) <-> row-interleaved (kp) block conversions.
 template <typename S, typename T>

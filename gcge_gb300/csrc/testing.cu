@@ -54,8 +54,10 @@ int GCGE_BlockPCG(void *A, void *B, double sigma, void **b, void **x, int k, int
             const int kp = rows_width(k, 8);
             col_to_rows<double, double>(n, k, kp, xv->data, xv->ld, c.xr64.p, st);
             col_to_rows<double, double>(n, k, kp, bv->data, bv->ld, c.br64.p, st);
-            it = block_pcg_rows<double>(c.pcg, c.upat, c.us64.p, c.br64.p, c.xr64.p, c.rr64.p,
-                                        c.pr64.p, c.wr64.p, kp, k, max_iter, rate, tol, false, st);
+            block_pcg_rows<double>(c.pcg, c.upat, c.us64.p, c.br64.p, c.xr64.p, c.rr64.p,
+                                   c.pr64.p, c.wr64.p, kp, k, max_iter, rate, tol, false, false,
+                                   st);
+            it = pcg_last_iters(c.pcg, st);
             rows_to_col<double, double>(n, k, kp, c.xr64.p, xv->data, xv->ld, false, st);
         } else {
             const int kp = rows_width(k, 4);
@@ -63,8 +65,9 @@ int GCGE_BlockPCG(void *A, void *B, double sigma, void **b, void **x, int k, int
             for (auto *bb : {&x32, &b32, &r32, &p32, &w32}) bb->alloc((size_t)n * kp);
             col_to_rows<double, float>(n, k, kp, xv->data, xv->ld, x32.p, st);
             col_to_rows<double, float>(n, k, kp, bv->data, bv->ld, b32.p, st);
-            it = block_pcg_rows<float>(c.pcg, c.upat, c.us32.p, b32.p, x32.p, r32.p, p32.p, w32.p,
-                                       kp, k, max_iter, rate, tol, false, st);
+            block_pcg_rows<float>(c.pcg, c.upat, c.us32.p, b32.p, x32.p, r32.p, p32.p, w32.p,
+                                  kp, k, max_iter, rate, tol, false, false, st);
+            it = pcg_last_iters(c.pcg, st);
             rows_to_col<float, double>(n, k, kp, x32.p, xv->data, xv->ld, false, st);
         }
         GCGE_CUDA(cudaStreamSynchronize(st));

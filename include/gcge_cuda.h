@@ -90,10 +90,16 @@ typedef struct gcge_solve_info {
     double seconds;     /* wall time of the solve on the host clock */
     double phase_ms[10];/* checkconv, compP, compRR, rr_matW, eig, compRV, compW, linsol,
                            compX, initX (CUDA events on the solver stream) */
-    int pcg_spmm_launches;   /* SpMM launches inside the block-PCG iterations */
-    double pcg_spmm_ms;      /* their summed device time (CUDA events around each launch) */
+    int pcg_spmm_launches;   /* SpMM phases inside the block-PCG iterations (one per iteration) */
+    double pcg_spmm_ms;      /* their summed device time (device clock at the grid barriers
+                                that open and close each SpMM phase) */
     double pcg_spmm_bytes;   /* their summed algorithmic bytes: nnz (v + 4) + 4 (n + 1)
-                                + 2 n k_active v, v = value size (8 FP64, 4 mixed) */
+                                + 2 n k_active v, v = value size (8 FP64, 4 mixed),
+                                k_active = columns in 16-byte groups with an active column */
+    int pcg_kernel_launches; /* block-PCG solves (one persistent kernel launch each) */
+    double pcg_kernel_ms;    /* their summed device time (CUDA events around each launch) */
+    double pcg_kernel_bytes; /* their summed algorithmic bytes: per iteration the matrix once
+                                + 12 n k_active v (p update, SpMM, x/r update), plus the setup */
 } gcge_solve_info;
 
 /* One-call solve of A x = lambda B x for the nev smallest pairs from host
