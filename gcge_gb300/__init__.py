@@ -38,7 +38,8 @@ EXPORTED_SYMBOLS = [
     "CUDA_MatNnz", "CUDA_MultiVecSetFromHost", "CUDA_MultiVecGetToHost", "CUDA_MultiVecSize",
     "GCGE_SetPrecision", "GCGE_Solve", "GCGE_GetSolveInfo", "GCGE_Prepare", "GCGE_PreparedSolve",
     "GCGE_PreparedDestroy", "GCGE_BenchSpMM", "GCGE_DenseEig", "GCGE_BlockPCG", "GCGE_BOrth",
-    "GCGE_TimerStart", "GCGE_TimerStop", "GCGE_GramNoAlloc",
+    "GCGE_TimerStart", "GCGE_TimerStop", "GCGE_GramNoAlloc", "GCGE_DenseGram",
+    "GCGE_DenseLinComb",
 ]
 
 _lib = None
@@ -104,7 +105,7 @@ def load(build_if_missing: bool = False) -> ctypes.CDLL:
                  "GCGE_Solve", "GCGE_Prepare", "GCGE_PreparedSolve", "GCGE_SetPrecision",
                  "GCGE_GetSolveInfo", "GCGE_BenchSpMM", "ops_cuda_last_error", "CUDA_MultiVecSize",
                  "CUDA_MatNnz", "GCGE_DenseEig", "GCGE_BlockPCG", "GCGE_BOrth",
-                 "GCGE_TimerStart", "GCGE_GramNoAlloc"):
+                 "GCGE_TimerStart", "GCGE_GramNoAlloc", "GCGE_DenseGram", "GCGE_DenseLinComb"):
         getattr(lib, name).restype = ctypes.c_int
     lib.GCGE_TimerStop.restype = ctypes.c_double
     _lib = lib
@@ -406,6 +407,44 @@ def block_pcg(A, B, sigma, b, x0, max_iter=30, rate=1e-2, tol=1e-14, fp32=False)
         return ops.download(hx, 0, k), it.value
     finally:
         ops.close()
+
+
+def dense_gram(Q, P, emulated=False):
+    """Q^T P through GCGE_DenseGram (FP64 kernel, or the tensor-core digit
+    kernel when emulated)."""
+    lib = load()
+    Q = np.asfortranarray(Q, dtype=np.float64)
+    P = np.asfortranarray(P, dtype=np.float64)
+    n, m = Q.shape
+    w = P.shape[1]
+    C = np.zeros((m, w), dtype=np.float64, order="F")
+    st = lib.GCGE_DenseGram(ctypes.c_int(n), ctypes.c_int(m), ctypes.c_int(w),
+                            Q.ctypes.data_as(ctypes.c_void_p), ctypes.c_int(max(n, 1)),
+                            P.ctypes.data_as(ctypes.c_void_p), ctypes.c_int(max(n, 1)),
+                            C.ctypes.data_as(ctypes.c_void_p), ctypes.c_int(1 if emulated else 0))
+    if st != GCGE_OK:
+        raise GCGEError(st, "GCGE_DenseGram")
+    return C
+
+
+def dense_lincomb(X, C, Y, beta=None, alpha=1.0, emulated=False):
+    """alpha X C + Y diag(beta) (beta None: overwrite) through GCGE_DenseLinComb."""
+    lib = load()
+    X = np.asfortranarray(X, dtype=np.float64)
+    C = np.asfortranarray(C, dtype=np.float64)
+    Y = np.array(Y, dtype=np.float64, order="F", copy=True)
+    n, k = X.shape
+    m = C.shape[1]
+    b = None if beta is None else np.ascontiguousarray(beta, dtype=np.float64)
+    st = lib.GCGE_DenseLinComb(ctypes.c_int(n), ctypes.c_int(k), ctypes.c_int(m),
+                               X.ctypes.data_as(ctypes.c_void_p), ctypes.c_int(n),
+                               C.ctypes.data_as(ctypes.c_void_p), ctypes.c_int(max(k, 1)),
+                               Y.ctypes.data_as(ctypes.c_void_p), ctypes.c_int(n),
+                               None if b is None else b.ctypes.data_as(ctypes.c_void_p),
+                               ctypes.c_double(alpha), ctypes.c_int(1 if emulated else 0))
+    if st != GCGE_OK:
+        raise GCGEError(st, "GCGE_DenseLinComb")
+    return Y
 
 
 def b_orth(B, X, start, n=None, zero_tol=2 * np.finfo(float).eps, max_reorth=2, A_for_size=None):

@@ -195,6 +195,13 @@ void lincomb(int n, int k, int m, const double *X, int ldx, const double *C, int
 void gram(int n, int m, int w, const double *Q, int ldq, const double *P, int ldp, double *C,
           int ldc, double *scratch, size_t scratch_elems, cudaStream_t st);
 size_t gram_scratch_elems(int n, int m, int w);
+// FP64-accurate products on the bf16 tensor cores (ozaki.cu): same arguments
+// and results as gram / lincomb, to FP64 accuracy.
+void oz_gram(int n, int m, int w, const double *Q, int ldq, const double *P, int ldp, double *C,
+             int ldc, double *scratch, size_t scratch_elems, cudaStream_t st);
+void oz_lincomb(int n, int k, int m, const double *X, int ldx, const double *C, int ldc,
+                double *Y, int ldy, const double *beta_dev, int incb, cudaStream_t st,
+                double alpha = 1.0);
 // per-column dots out[c] = X(:,c) . Y(:,c)
 void coldot(int n, int k, const double *X, int ldx, const double *Y, int ldy, double *out,
             double *scratch, size_t scratch_elems, cudaStream_t st);

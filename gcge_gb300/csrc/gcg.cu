@@ -136,6 +136,26 @@ struct PhaseTimer {
 };
 enum { PH_CHECK = 0, PH_P, PH_RR, PH_RRW, PH_EIG, PH_RV, PH_W, PH_LINSOL, PH_X, PH_INITX, PH_NONE = -1 };
 
+// Products over the long (vector-length) dimension: FP64 FMA kernels in the
+// FP64 solve, FP64-accurate digit products on the tensor cores in the mixed
+// solve (same results to FP64 accuracy).
+static void dgram(const SolverCtx &c, int n, int m, int w, const double *Q, int ldq,
+                  const double *P, int ldp, double *C, int ldc, double *scratch, size_t elems,
+                  cudaStream_t st) {
+    if (c.precision == GCGE_PREC_MIXED)
+        oz_gram(n, m, w, Q, ldq, P, ldp, C, ldc, scratch, elems, st);
+    else
+        gram(n, m, w, Q, ldq, P, ldp, C, ldc, scratch, elems, st);
+}
+static void dlincomb(const SolverCtx &c, int n, int k, int m, const double *X, int ldx,
+                     const double *C, int ldc, double *Y, int ldy, const double *beta, int incb,
+                     cudaStream_t st, double alpha = 1.0) {
+    if (c.precision == GCGE_PREC_MIXED)
+        oz_lincomb(n, k, m, X, ldx, C, ldc, Y, ldy, beta, incb, st, alpha);
+    else
+        lincomb(n, k, m, X, ldx, C, ldc, Y, ldy, beta, incb, st, alpha);
+}
+
 // B-orthonormalise columns [start, end) of x (nrows x ldx) against the
 // B-orthonormal prefix [0, start) and among themselves; returns the new end
 // (columns whose remaining B-norm is below the zero tolerance are dropped).
@@ -169,9 +189,9 @@ int borth(SolverCtx &c, SparseMat *B, double *x, int ldx, int nrows, int start, 
                 applyB(X1, ldx, c.T2.p, ld, k);
                 BX1 = c.T2.p;
             }
-            gram(nrows, start, k, x, ldx, BX1, useB ? ld : ldx, c.dC.p, start, c.gscr.p,
-                 c.gscr.n, st);
-            lincomb(nrows, start, k, x, ldx, c.dC.p, start, X1, ldx, c.one.p, 0, st, -1.0);
+            dgram(c, nrows, start, k, x, ldx, BX1, useB ? ld : ldx, c.dC.p, start, c.gscr.p,
+                  c.gscr.n, st);
+            dlincomb(c, nrows, start, k, x, ldx, c.dC.p, start, X1, ldx, c.one.p, 0, st, -1.0);
             if (pass >= 1 || max_reorth == 0) {
                 if (device_absmax(start, k, c.dC.p, start) < reorth_tol) break;
             }
@@ -184,7 +204,7 @@ int borth(SolverCtx &c, SparseMat *B, double *x, int ldx, int nrows, int start, 
             applyB(X1, ldx, c.T2.p, ld, k);
             BX1 = c.T2.p;
         }
-        gram(nrows, k, k, X1, ldx, BX1, useB ? ld : ldx, c.dC.p, k, c.gscr.p, c.gscr.n, st);
+        dgram(c, nrows, k, k, X1, ldx, BX1, useB ? ld : ldx, c.dC.p, k, c.gscr.p, c.gscr.n, st);
         GCGE_CUDA(cudaMemcpyAsync(c.hbuf.p, c.dC.p, sizeof(double) * k * k,
                                   cudaMemcpyDeviceToHost, st));
         GCGE_CUDA(cudaStreamSynchronize(st));
@@ -234,7 +254,7 @@ int borth(SolverCtx &c, SparseMat *B, double *x, int ldx, int nrows, int start, 
         if (kk > 0) {
             GCGE_CUDA(cudaMemcpyAsync(c.dC.p, Cf, sizeof(double) * k * kk,
                                       cudaMemcpyHostToDevice, st));
-            lincomb(nrows, k, kk, X1, ldx, c.dC.p, k, c.T1.p, ld, nullptr, 0, st);
+            dlincomb(c, nrows, k, kk, X1, ldx, c.dC.p, k, c.T1.p, ld, nullptr, 0, st);
             copy_cols(nrows, kk, c.T1.p, ld, X1, ldx, st);
         }
         k = kk;
@@ -310,8 +330,8 @@ struct GcgRun {
     void compute_ritz_vec() {
         timer.mark(PH_RV);
         const int s = sizeV - sizeC;
-        lincomb(n, s, endX - startN, colp(V, startN), ld, c.evec.p, s, colp(ritz, startN), ritz->ld,
-                nullptr, 0, st);
+        dlincomb(c, n, s, endX - startN, colp(V, startN), ld, c.evec.p, s, colp(ritz, startN),
+                 ritz->ld, nullptr, 0, st);
     }
 
     // ---------------- CheckConvergence (:196-321)
@@ -421,7 +441,7 @@ struct GcgRun {
         sizeP = endP - startP;
         copy_cols(s, sizeP, wk + (size_t)base * s, s, c.coefP.p, s, st);
         // P = V(:, startN:endW) coefP, staged through T1 (it overlaps V's range)
-        lincomb(n, s, sizeP, colp(V, startN), ld, c.coefP.p, s, c.T1.p, ld, nullptr, 0, st);
+        dlincomb(c, n, s, sizeP, colp(V, startN), ld, c.coefP.p, s, c.T1.p, ld, nullptr, 0, st);
         copy_cols(n, sizeP, c.T1.p, ld, colp(V, startP), ld, st);
     }
 
@@ -513,8 +533,8 @@ struct GcgRun {
             // [X P W]^T A W (:976-993)
             spmm<double>(A->pat, A->val.p, colp(V, startW), ld, c.T1.p, ld, sizeW, st);
             spmm_calls++;
-            gram(n, endW - startN, sizeW, colp(V, startN), ld, c.T1.p, ld, M + (size_t)xp * s, s,
-                 c.gscr.p, c.gscr.n, st);
+            dgram(c, n, endW - startN, sizeW, colp(V, startN), ld, c.T1.p, ld, M + (size_t)xp * s,
+                  s, c.gscr.p, c.gscr.n, st);
             transpose_copy(xp, sizeW, M + (size_t)xp * s, s, M + xp, s, st);
         }
         if (sizeX == sizeV) {
@@ -524,8 +544,8 @@ struct GcgRun {
                 const int kc = std::min(bsz, sizeX - c0);
                 spmm<double>(A->pat, A->val.p, colp(V, c0), ld, c.T1.p, ld, kc, st);
                 spmm_calls++;
-                gram(n, sizeX - sizeC, kc, colp(V, sizeC), ld, c.T1.p, ld, M + (size_t)(c0 - sizeC) * s,
-                     s, c.gscr.p, c.gscr.n, st);
+                dgram(c, n, sizeX - sizeC, kc, colp(V, sizeC), ld, c.T1.p, ld,
+                      M + (size_t)(c0 - sizeC) * s, s, c.gscr.p, c.gscr.n, st);
             }
         } else {
             // X block = diag(Ritz values), XP block = 0, P block = PtAP (:1018-1039)
@@ -598,8 +618,9 @@ struct GcgRun {
                 nev = std::min(nev + sizeP + sizeW, nev0);
                 const int newX = std::min(sizeX + sizeP + sizeW, nevMax);
                 const int s = sizeV - sizeC;
-                lincomb(n, s, newX - endX, colp(V, startN), ld, c.evec.p + (size_t)(endX - sizeC) * s,
-                        s, colp(ritz, endX), ritz->ld, nullptr, 0, st);
+                dlincomb(c, n, s, newX - endX, colp(V, startN), ld,
+                         c.evec.p + (size_t)(endX - sizeC) * s, s, colp(ritz, endX), ritz->ld,
+                         nullptr, 0, st);
                 sizeX = newX;
                 sizeP = 0;
                 sizeW = 0;

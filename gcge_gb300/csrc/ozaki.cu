@@ -1,0 +1,404 @@
+// FP64-accurate dense products on the bf16 tensor cores, for the
+// mixed-precision GCG: the tall-skinny Gram products Q^T P (B-orthogonalisation,
+// Rayleigh-Ritz) and the linear combinations Y = X C (orth updates, Ritz
+// vectors, P), the calls the reference makes through DenseMatQtAP and
+// MultiVecLinearComb (app/app_lapack.c:64-183, :463-534).  GB300's FP64 units
+// run at about 1.2 TFLOP/s; these products dominate the FP64 solve.
+//
+// Method (error-free digit splitting, the Ozaki scheme): within each chunk of
+// kBK = 64 consecutive k, every row of the left operand and every column of
+// the right operand gets an exponent e with |x| < 2^e over the chunk, and each
+// x is written as 2^e * sum_i d_i 2^(-7(i+1)), i = 0..7, with signed 7-bit
+// digits d_i (56-bit fixed point, truncated).  Digits are exact in bf16.  A
+// chunk's product sum_k x_k y_k is 2^(ea+eb) * sum_l L_l 2^(-7(l+2)) with level
+// sums L_l = sum_{i+j=l} sum_k d_i(x_k) d_j(y_k), l = 0..7 (the 36 digit pairs
+// with i + j <= 7).  |L_l| <= (l+1) * 64 * 127^2 < 2^24, so the level sums of
+// bf16 products accumulated in FP32 by mma.sync are exact integers.  After the
+// chunk they are folded into two exact int64 words, converted exactly to FP64
+// and added, with the chunk scale, into FP64 accumulators.  The truncation
+// error is below 2^-56 of the chunk's largest |x| |y| per product, the same
+// order as FP64 rounding; non-finite inputs give NaN outputs.
+//
+// Tiles: a CTA computes a 64 x BN block of the result for a range of k; the
+// operands' digit planes for one chunk sit in shared memory (8 planes each,
+// rows padded to 72 bf16 so ldmatrix is conflict-free) and each warp owns a
+// 16 x 8 tile: per 16-wide k step it loads 8 A and 8 B digit fragments and
+// issues 36 MMAs into 8 level accumulators.  Gram products split k over CTAs
+// (partials summed in a fixed order); linear combinations tile the long row
+// dimension and keep k whole.
+#include <cstdint>
+
+#include "common.cuh"
+
+namespace gcge {
+namespace {
+
+constexpr int kDigits = 8;
+constexpr int kDigitBits = 7;
+constexpr int kBK = 64;
+constexpr int kBKP = kBK + 8;
+constexpr int kBM = 64;
+
+template <int BN>
+struct __align__(16) OzSmem {
+    uint16_t a[kDigits][kBM][kBKP];
+    uint16_t b[kDigits][BN][kBKP];
+    int ea[kBM], eb[BN];  // chunk exponent fields (biased, >= 1)
+};
+
+template <int BN>
+__host__ __device__ constexpr int oz_threads() {
+    return (kBM / 16) * (BN / 8) * 32;
+}
+
+// biased exponent field, zero and subnormals counted as 1
+__device__ __forceinline__ int exp_field(double x) {
+    return max((int)((__double_as_longlong(x) >> 52) & 0x7FF), 1);
+}
+
+// The 8 signed 7-bit digits of x relative to 2^(emax - 1022) as bf16 bit
+// patterns (emax >= exp_field(x)).
+__device__ __forceinline__ void split_digits(double x, int emax, uint16_t (&d)[kDigits]) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    const int ef = (int)((b >> 52) & 0x7FF);
+    unsigned long long mant = b & 0x000FFFFFFFFFFFFFull;
+    if (ef != 0) mant |= 0x0010000000000000ull;
+    const int sh = max(ef, 1) - emax + 3;  // <= 3: the value < 2^56 in fixed point
+    const unsigned long long X = sh >= 0 ? (mant << sh) : (sh > -64 ? (mant >> (-sh)) : 0ull);
+    const uint16_t sgn = (uint16_t)((b >> 48) & 0x8000u);
+#pragma unroll
+    for (int i = 0; i < kDigits; ++i) {
+        const unsigned v = (unsigned)(X >> (49 - kDigitBits * i)) & 127u;
+        // exact small-integer float: (2^23 + v) - 2^23; bf16 = its top 16 bits
+        const float f = __uint_as_float(0x4B000000u | v) - 8388608.0f;
+        d[i] = (uint16_t)(__float_as_uint(f) >> 16) | (v ? sgn : (uint16_t)0);
+    }
+}
+
+// exact int64 -> double for |t| < 2^51
+__device__ __forceinline__ double i64_to_f64(long long t) {
+    return __longlong_as_double(t + 0x4338000000000000LL) - 6755399441055744.0;
+}
+
+__device__ __forceinline__ void ldsm_x4(uint32_t (&r)[4], const void *p) {
+    const unsigned a = (unsigned)__cvta_generic_to_shared(p);
+    asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0,%1,%2,%3}, [%4];"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
+                 : "r"(a));
+}
+__device__ __forceinline__ void ldsm_x2(uint32_t (&r)[2], const void *p) {
+    const unsigned a = (unsigned)__cvta_generic_to_shared(p);
+    asm volatile("ldmatrix.sync.aligned.m8n8.x2.shared.b16 {%0,%1}, [%2];"
+                 : "=r"(r[0]), "=r"(r[1])
+                 : "r"(a));
+}
+__device__ __forceinline__ void mma_bf16(float (&d)[4], const uint32_t (&a)[4],
+                                         const uint32_t (&b)[2]) {
+    asm volatile(
+        "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, "
+        "{%8,%9}, {%0,%1,%2,%3};"
+        : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
+}
+
+// Digit planes of R rows of a k-contiguous operand (element (r, k) at
+// p[k + r * ld]) for the chunk [k0, k0 + kBK) clipped to kend; rows at or past
+// nrows are zero.  One warp per row, lane l takes k = k0 + 2l, k0 + 2l + 1.
+template <int R>
+__device__ __forceinline__ void planes_kcontig(const double *__restrict__ p, size_t ld, int r0,
+                                               int nrows, int k0, int kend,
+                                               uint16_t (*planes)[R][kBKP], int *e, int warp,
+                                               int nwarps, int lane) {
+    for (int r = warp; r < R; r += nwarps) {
+        const int gr = r0 + r;
+        const int k = k0 + 2 * lane;
+        double v0 = 0.0, v1 = 0.0;
+        if (gr < nrows) {
+            const double *q = p + (size_t)gr * ld;
+            if (k < kend) v0 = q[k];
+            if (k + 1 < kend) v1 = q[k + 1];
+        }
+        const int em =
+            (int)__reduce_max_sync(0xffffffffu, (unsigned)max(exp_field(v0), exp_field(v1)));
+        uint16_t d0[kDigits], d1[kDigits];
+        split_digits(v0, em, d0);
+        split_digits(v1, em, d1);
+#pragma unroll
+        for (int i = 0; i < kDigits; ++i)
+            *reinterpret_cast<uint32_t *>(&planes[i][r][2 * lane]) =
+                (uint32_t)d0[i] | ((uint32_t)d1[i] << 16);
+        if (lane == 0) e[r] = em;
+    }
+}
+
+// Digit planes of kBM rows of an m-contiguous operand (element (m, k) at
+// p[m + k * ld]); a work item is one row and 8 consecutive k.  Two passes: the
+// chunk exponent of each row (shared-memory max), then the digits.
+template <int NT>
+__device__ __forceinline__ void planes_mcontig(const double *__restrict__ p, size_t ld, int m0,
+                                               int nrows, int k0, int kend,
+                                               uint16_t (*planes)[kBM][kBKP], int *e, int tid) {
+    for (int r = tid; r < kBM; r += NT) e[r] = 1;
+    __syncthreads();
+    constexpr int items = kBM * (kBK / 8);
+    for (int it = tid; it < items; it += NT) {
+        const int r = it % kBM, k8 = it / kBM;
+        const int gr = m0 + r;
+        int em = 1;
+        if (gr < nrows) {
+#pragma unroll
+            for (int q = 0; q < 8; ++q) {
+                const int k = k0 + k8 * 8 + q;
+                if (k < kend) em = max(em, exp_field(p[gr + (size_t)k * ld]));
+            }
+        }
+        atomicMax(&e[r], em);
+    }
+    __syncthreads();
+    for (int it = tid; it < items; it += NT) {
+        const int r = it % kBM, k8 = it / kBM;
+        const int gr = m0 + r;
+        const int em = e[r];
+        uint32_t w[kDigits][4];
+#pragma unroll
+        for (int q = 0; q < 8; q += 2) {
+            const int k = k0 + k8 * 8 + q;
+            double v0 = 0.0, v1 = 0.0;
+            if (gr < nrows) {
+                if (k < kend) v0 = p[gr + (size_t)k * ld];
+                if (k + 1 < kend) v1 = p[gr + (size_t)(k + 1) * ld];
+            }
+            uint16_t d0[kDigits], d1[kDigits];
+            split_digits(v0, em, d0);
+            split_digits(v1, em, d1);
+#pragma unroll
+            for (int i = 0; i < kDigits; ++i)
+                w[i][q / 2] = (uint32_t)d0[i] | ((uint32_t)d1[i] << 16);
+        }
+#pragma unroll
+        for (int i = 0; i < kDigits; ++i)
+            *reinterpret_cast<uint4 *>(&planes[i][r][k8 * 8]) =
+                make_uint4(w[i][0], w[i][1], w[i][2], w[i][3]);
+    }
+}
+
+struct OzArgs {
+    int M, N;
+    const double *A;  // gram: Q (n x M, k-contiguous rows of Q^T); lincomb: X (M x K)
+    size_t lda;
+    const double *B;  // gram: P (n x N); lincomb: C (K x N); both k-contiguous
+    size_t ldb;
+    int kbeg_stride;  // k per CTA along blockIdx.z
+    int K;
+    // gram output: partials part[z][M x N]; lincomb output: Y
+    double *out;
+    size_t ldo;
+    const double *beta;
+    int incb;
+    double alpha;
+};
+
+template <int BN, bool GRAM>
+__global__ void __launch_bounds__(oz_threads<BN>(), 2) k_oz_gemm(OzArgs a) {
+    constexpr int NT = oz_threads<BN>();
+    constexpr int nwarps = NT / 32;
+    extern __shared__ __align__(16) unsigned char oz_raw[];
+    OzSmem<BN> &sm = *reinterpret_cast<OzSmem<BN> *>(oz_raw);
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int mt0 = blockIdx.x * kBM, nt0 = blockIdx.y * BN;
+    const int kb = blockIdx.z * a.kbeg_stride;
+    const int ke = min(a.K, kb + a.kbeg_stride);
+    const int wm = warp % (kBM / 16), wn = warp / (kBM / 16);
+    const int m0 = wm * 16, n0 = wn * 8;
+    const int g = lane >> 2, t4 = lane & 3;
+
+    double acc[4] = {0.0, 0.0, 0.0, 0.0};
+    bool bad[4] = {false, false, false, false};
+
+    for (int k0 = kb; k0 < ke; k0 += kBK) {
+        if constexpr (GRAM)
+            planes_kcontig<kBM>(a.A, a.lda, mt0, a.M, k0, ke, sm.a, sm.ea, warp, nwarps, lane);
+        else
+            planes_mcontig<NT>(a.A, a.lda, mt0, a.M, k0, ke, sm.a, sm.ea, tid);
+        planes_kcontig<BN>(a.B, a.ldb, nt0, a.N, k0, ke, sm.b, sm.eb, warp, nwarps, lane);
+        __syncthreads();
+
+        float lv[kDigits][4];
+#pragma unroll
+        for (int l = 0; l < kDigits; ++l) lv[l][0] = lv[l][1] = lv[l][2] = lv[l][3] = 0.f;
+#pragma unroll
+        for (int ks = 0; ks < kBK / 16; ++ks) {
+            uint32_t bf[kDigits][2];
+#pragma unroll
+            for (int j = 0; j < kDigits; ++j)
+                ldsm_x2(bf[j], &sm.b[j][n0 + (lane & 7)][ks * 16 + ((lane >> 3) & 1) * 8]);
+#pragma unroll
+            for (int i = 0; i < kDigits; ++i) {
+                uint32_t af[4];
+                ldsm_x4(af, &sm.a[i][m0 + (lane & 15)][ks * 16 + (lane >> 4) * 8]);
+#pragma unroll
+                for (int j = 0; j < kDigits - i; ++j) mma_bf16(lv[i + j], af, bf[j]);
+            }
+        }
+        // fold the exact level sums into the FP64 accumulators
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const int rl = m0 + g + ((q >> 1) << 3);
+            const int cl = n0 + 2 * t4 + (q & 1);
+            int L[kDigits];
+#pragma unroll
+            for (int l = 0; l < kDigits; ++l) L[l] = __float2int_rn(lv[l][q]);
+            const long long thi = ((long long)L[0] << 21) + ((long long)L[1] << 14) +
+                                  ((long long)L[2] << 7) + (long long)L[3];
+            const long long tlo = ((long long)L[4] << 21) + ((long long)L[5] << 14) +
+                                  ((long long)L[6] << 7) + (long long)L[7];
+            const int ea = sm.ea[rl], eb = sm.eb[cl];
+            if (ea == 0x7FF || eb == 0x7FF) {
+                bad[q] = true;
+            } else {
+                // scale 2^(ea - 1022 + eb - 1022 - 63): exponent field ea + eb - 1084
+                const int fld = ea + eb - 1084;
+                if (fld > 0) {
+                    const double s = fld >= 2047 ? __longlong_as_double(0x7FF0000000000000LL)
+                                                 : __longlong_as_double((long long)fld << 52);
+                    const double v = fma(i64_to_f64(thi), 268435456.0, i64_to_f64(tlo));
+                    acc[q] = fma(v, s, acc[q]);
+                }
+            }
+        }
+        __syncthreads();
+    }
+
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        const int row = mt0 + m0 + g + ((q >> 1) << 3);
+        const int col = nt0 + n0 + 2 * t4 + (q & 1);
+        if (row >= a.M || col >= a.N) continue;
+        const double v = bad[q] ? __longlong_as_double(0x7FF8000000000000LL) : acc[q];
+        if constexpr (GRAM) {
+            a.out[(size_t)blockIdx.z * a.M * a.N + row + (size_t)col * a.M] = v;
+        } else {
+            double y = a.alpha * v;
+            if (a.beta != nullptr) {
+                const double b = a.beta[a.incb == 0 ? 0 : (size_t)col * a.incb];
+                if (b != 0.0) y = fma(b, a.out[row + (size_t)col * a.ldo], y);
+            }
+            a.out[row + (size_t)col * a.ldo] = y;
+        }
+    }
+}
+
+__global__ void k_oz_reduce(const double *__restrict__ part, int chunks, int m, int w,
+                            double *__restrict__ C, int ldc) {
+    const int total = m * w;
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < total; e += gridDim.x * blockDim.x) {
+        double s = 0.0;
+        for (int c = 0; c < chunks; ++c) s += part[(size_t)c * total + e];
+        C[e % m + (size_t)(e / m) * ldc] = s;
+    }
+}
+
+int oz_num_sms() {
+    static int sms = 0;
+    if (!sms) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if (sms <= 0) sms = 148;
+    }
+    return sms;
+}
+
+template <int BN, bool GRAM>
+void launch_oz(const OzArgs &a, dim3 grid, cudaStream_t st) {
+    static bool attr = false;
+    const int smem = (int)sizeof(OzSmem<BN>);
+    if (!attr) {
+        GCGE_CUDA(cudaFuncSetAttribute(k_oz_gemm<BN, GRAM>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+        attr = true;
+    }
+    k_oz_gemm<BN, GRAM><<<grid, oz_threads<BN>(), smem, st>>>(a);
+    GCGE_CHECK_LAUNCH();
+    count_launch();
+}
+
+int oz_tile_n(int n) { return n <= 8 ? 8 : (n <= 16 ? 16 : 24); }
+
+template <bool GRAM>
+void launch_oz_bn(const OzArgs &a, int bn, dim3 grid, cudaStream_t st) {
+    switch (bn) {
+        case 8: launch_oz<8, GRAM>(a, grid, st); break;
+        case 16: launch_oz<16, GRAM>(a, grid, st); break;
+        default: launch_oz<24, GRAM>(a, grid, st); break;
+    }
+}
+
+}  // namespace
+
+// C (m x w, ldc) = Q^T P for Q n x m (ldq), P n x w (ldp); scratch holds the
+// split-k partials (scratch_elems doubles).
+void oz_gram(int n, int m, int w, const double *Q, int ldq, const double *P, int ldp, double *C,
+             int ldc, double *scratch, size_t scratch_elems, cudaStream_t st) {
+    if (m <= 0 || w <= 0) return;
+    if (n <= 0) {
+        GCGE_CUDA(cudaMemset2DAsync(C, sizeof(double) * ldc, 0, sizeof(double) * m, w, st));
+        return;
+    }
+    const int bn = oz_tile_n(w);
+    const int mt = (m + kBM - 1) / kBM, nt = (w + bn - 1) / bn;
+    const int chunks = (n + kBK - 1) / kBK;
+    // about four CTAs per SM over the whole grid, at least two chunks each
+    long long z = std::max(1, (4 * oz_num_sms() + mt * nt - 1) / (mt * nt));
+    z = std::min<long long>(z, std::max(1, chunks / 2));
+    z = std::min<long long>(z, (long long)(scratch_elems / ((size_t)m * w)));
+    GCGE_REQUIRE(z >= 1, GCGE_ERR_ARG, "oz_gram: scratch too small");
+    const int per = (int)((chunks + z - 1) / z) * kBK;
+    const int zz = (n + per - 1) / per;
+    OzArgs a{};
+    a.M = m;
+    a.N = w;
+    a.A = Q;
+    a.lda = (size_t)ldq;
+    a.B = P;
+    a.ldb = (size_t)ldp;
+    a.kbeg_stride = per;
+    a.K = n;
+    a.out = scratch;
+    launch_oz_bn<true>(a, bn, dim3(mt, nt, zz), st);
+    const int tot = m * w;
+    k_oz_reduce<<<std::max(1, std::min((tot + 255) / 256, 4 * oz_num_sms())), 256, 0, st>>>(
+        scratch, zz, m, w, C, ldc);
+    GCGE_CHECK_LAUNCH();
+    count_launch();
+}
+
+// Y (n x m, ldy) = alpha X C + Y diag(beta) for X n x k (ldx), C k x m (ldc);
+// beta == nullptr overwrites Y; incb == 0 broadcasts beta[0].
+void oz_lincomb(int n, int k, int m, const double *X, int ldx, const double *C, int ldc,
+                double *Y, int ldy, const double *beta_dev, int incb, cudaStream_t st,
+                double alpha) {
+    if (n <= 0 || m <= 0) return;
+    if (k <= 0) {
+        lincomb(n, k, m, X, ldx, C, ldc, Y, ldy, beta_dev, incb, st, alpha);
+        return;
+    }
+    const int bn = oz_tile_n(m);
+    OzArgs a{};
+    a.M = n;
+    a.N = m;
+    a.A = X;
+    a.lda = (size_t)ldx;
+    a.B = C;
+    a.ldb = (size_t)ldc;
+    a.kbeg_stride = k;
+    a.K = k;
+    a.out = Y;
+    a.ldo = (size_t)ldy;
+    a.beta = beta_dev;
+    a.incb = incb;
+    a.alpha = alpha;
+    launch_oz_bn<false>(a, bn, dim3((n + kBM - 1) / kBM, (m + bn - 1) / bn, 1), st);
+}
+
+}  // namespace gcge

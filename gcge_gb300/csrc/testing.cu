@@ -1,6 +1,7 @@
-// Component entry points: the dense eigensolver, the block-PCG inner solve
-// and the B-orthonormalisation, each callable on its own through the C ABI so
-// they can be checked against the CPU oracle in isolation.
+// Component entry points: the dense eigensolver, the block-PCG inner solve,
+// the B-orthonormalisation and the long-dimension dense products, each
+// callable on its own through the C ABI so they can be checked against the
+// CPU oracle (or FP64 host arithmetic) in isolation.
 #include <cstring>
 
 #include "gcg.cuh"
@@ -92,6 +93,79 @@ int GCGE_BOrth(void *B, void **x, int start, int *end, double zero_tol, int max_
         *end = borth(c, Bm, xv->data, xv->ld, xv->nrows, start, *end, Bm != nullptr, zero_tol,
                      max_reorth, nullptr);
         GCGE_CUDA(cudaStreamSynchronize(lib_stream()));
+        return GCGE_OK;
+    } catch (const CudaError &e) {
+        set_error(e.status, e.where.c_str());
+        take_error();
+        return e.status;
+    }
+}
+
+
+int GCGE_DenseGram(int n, int m, int w, const double *Q, int ldq, const double *P, int ldp,
+                   double *C, int emulated) {
+    try {
+        GCGE_REQUIRE(n >= 0 && m >= 1 && w >= 1 && C && (n == 0 || (Q && P && ldq >= n && ldp >= n)),
+                     GCGE_ERR_ARG, "GCGE_DenseGram: arguments");
+        cudaStream_t st = lib_stream();
+        DevBuf<double> dQ, dP, dC, scr;
+        dQ.alloc(std::max<size_t>((size_t)n * m, 1));
+        dP.alloc(std::max<size_t>((size_t)n * w, 1));
+        dC.alloc((size_t)m * w);
+        const size_t elems = std::max<size_t>(gram_scratch_elems(n, m, w), (size_t)1 << 20);
+        scr.alloc(elems);
+        if (n > 0) {
+            GCGE_CUDA(cudaMemcpy2DAsync(dQ.p, sizeof(double) * n, Q, sizeof(double) * ldq,
+                                        sizeof(double) * n, m, cudaMemcpyHostToDevice, st));
+            GCGE_CUDA(cudaMemcpy2DAsync(dP.p, sizeof(double) * n, P, sizeof(double) * ldp,
+                                        sizeof(double) * n, w, cudaMemcpyHostToDevice, st));
+        }
+        if (emulated)
+            oz_gram(n, m, w, dQ.p, std::max(n, 1), dP.p, std::max(n, 1), dC.p, m, scr.p, elems, st);
+        else
+            gram(n, m, w, dQ.p, std::max(n, 1), dP.p, std::max(n, 1), dC.p, m, scr.p, elems, st);
+        GCGE_CUDA(cudaMemcpyAsync(C, dC.p, sizeof(double) * m * w, cudaMemcpyDeviceToHost, st));
+        GCGE_CUDA(cudaStreamSynchronize(st));
+        return GCGE_OK;
+    } catch (const CudaError &e) {
+        set_error(e.status, e.where.c_str());
+        take_error();
+        return e.status;
+    }
+}
+
+int GCGE_DenseLinComb(int n, int k, int m, const double *X, int ldx, const double *Cf, int ldc,
+                      double *Y, int ldy, const double *beta, double alpha, int emulated) {
+    try {
+        GCGE_REQUIRE(n >= 1 && k >= 0 && m >= 1 && Y && ldy >= n &&
+                         (k == 0 || (X && Cf && ldx >= n && ldc >= k)),
+                     GCGE_ERR_ARG, "GCGE_DenseLinComb: arguments");
+        cudaStream_t st = lib_stream();
+        DevBuf<double> dX, dC, dY, dB;
+        dX.alloc(std::max<size_t>((size_t)n * k, 1));
+        dC.alloc(std::max<size_t>((size_t)k * m, 1));
+        dY.alloc((size_t)n * m);
+        if (k > 0) {
+            GCGE_CUDA(cudaMemcpy2DAsync(dX.p, sizeof(double) * n, X, sizeof(double) * ldx,
+                                        sizeof(double) * n, k, cudaMemcpyHostToDevice, st));
+            GCGE_CUDA(cudaMemcpy2DAsync(dC.p, sizeof(double) * k, Cf, sizeof(double) * ldc,
+                                        sizeof(double) * k, m, cudaMemcpyHostToDevice, st));
+        }
+        GCGE_CUDA(cudaMemcpy2DAsync(dY.p, sizeof(double) * n, Y, sizeof(double) * ldy,
+                                    sizeof(double) * n, m, cudaMemcpyHostToDevice, st));
+        const double *bp = nullptr;
+        if (beta) {
+            dB.alloc(m);
+            GCGE_CUDA(cudaMemcpyAsync(dB.p, beta, sizeof(double) * m, cudaMemcpyHostToDevice, st));
+            bp = dB.p;
+        }
+        if (emulated)
+            oz_lincomb(n, k, m, dX.p, n, dC.p, std::max(k, 1), dY.p, n, bp, 1, st, alpha);
+        else
+            lincomb(n, k, m, dX.p, n, dC.p, std::max(k, 1), dY.p, n, bp, 1, st, alpha);
+        GCGE_CUDA(cudaMemcpy2DAsync(Y, sizeof(double) * ldy, dY.p, sizeof(double) * n,
+                                    sizeof(double) * n, m, cudaMemcpyDeviceToHost, st));
+        GCGE_CUDA(cudaStreamSynchronize(st));
         return GCGE_OK;
     } catch (const CudaError &e) {
         set_error(e.status, e.where.c_str());

@@ -161,6 +161,18 @@ int GCGE_BlockPCG(void *A, void *B, double sigma, void **b, void **x, int k, int
  * the number of dependent columns dropped. */
 int GCGE_BOrth(void *B, void **x, int start, int *end, double zero_tol, int max_reorth);
 
+/* Long-dimension dense products from host arrays, through the FP64 kernels
+ * (emulated = 0) or the FP64-accurate tensor-core digit kernels of the mixed
+ * solve (emulated = 1).  GCGE_DenseGram: C (m x w, leading dimension m) =
+ * Q^T P for Q n x m and P n x w, as DenseMatQtAP with matA = NULL
+ * (app/app_lapack.c:64-183).  GCGE_DenseLinComb: Y (n x m) = alpha X C +
+ * Y diag(beta) for X n x k and C k x m (beta NULL: Y overwritten), as
+ * MultiVecLinearComb (app/app_lapack.c:463-534). */
+int GCGE_DenseGram(int n, int m, int w, const double *Q, int ldq, const double *P, int ldp,
+                   double *C, int emulated);
+int GCGE_DenseLinComb(int n, int k, int m, const double *X, int ldx, const double *C, int ldc,
+                      double *Y, int ldy, const double *beta, double alpha, int emulated);
+
 /* ---- allocation-free Gram product ---------------------------------------
  * No counterpart in the reference: an addition for callers that may not
  * allocate device memory (their memory belongs to another allocator or a
