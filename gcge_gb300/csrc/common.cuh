@@ -152,34 +152,8 @@ void spmm(const SellPattern &pat, const T *val, const T *X, int ldx, T *Y, int l
 int residual_norms(const SellPattern &pat, const double *a, const double *b, const double *X,
                    int ldx, const double *lam, int k, double *partial, int kmax, cudaStream_t st);
 int spmm_blocks(const SellPattern &pat);
-// Row-interleaved variant: X, Y are n x kp with row i at X + i*kp (kp = k
-// padded to 16 bytes, see rows_width).  With dot, partial[block*kmax + c] =
-// sum over the block's rows of X(i,c) Y(i,c) for active columns c < k.
-template <typename T>
-int spmm_rows(const SellPattern &pat, const T *val, const T *X, T *Y, int kp, int k,
-              const int *active, double *partial, int kmax, bool dot, cudaStream_t st);
+// Smallest block-PCG row width >= k (whole 16-byte column groups).
 int rows_width(int k, int elem_bytes);
-
-// Dispatch on the instantiated row widths of the row-interleaved kernels.
-#define GCGE_KP_DISPATCH(T, kp, BODY)                                        \
-    do {                                                                     \
-        switch (kp) {                                                        \
-            case 2: { constexpr int KP = 2; BODY; break; }                   \
-            case 4: { constexpr int KP = 4; BODY; break; }                   \
-            case 6: { constexpr int KP = 6; BODY; break; }                   \
-            case 8: { constexpr int KP = 8; BODY; break; }                   \
-            case 12: { constexpr int KP = 12; BODY; break; }                 \
-            case 16: { constexpr int KP = 16; BODY; break; }                 \
-            case 20: { constexpr int KP = 20; BODY; break; }                 \
-            case 24: { constexpr int KP = 24; BODY; break; }                 \
-            case 28: { constexpr int KP = 28; BODY; break; }                 \
-            case 32: { constexpr int KP = 32; BODY; break; }                 \
-            case 36: { constexpr int KP = 36; BODY; break; }                 \
-            case 40: { constexpr int KP = 40; BODY; break; }                 \
-            default:                                                         \
-                throw CudaError{GCGE_ERR_ARG, "row SpMM: unsupported width"}; \
-        }                                                                    \
-    } while (0)
 
 
 // Dense (dense.cu).

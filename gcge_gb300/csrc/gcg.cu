@@ -71,7 +71,7 @@ void SolverCtx::reserve(int n_, int nev_max, int nev_init, int bs, int spmm_nblo
     if (bs > cap_bs || (size_t)ld * bs > bbuf.n) {
         bbuf.alloc((size_t)ld * bs);
         r64.alloc((size_t)ld * bs);
-        const size_t nr = (size_t)n_ * rows_width(std::min(bs, 40), 8);
+        const size_t nr = pcg_block_elems(n_, rows_width(std::min(bs, 40), 8));
         for (auto *b : {&xr64, &br64, &rr64, &pr64, &wr64}) b->alloc(nr);
         cap_bs = bs;
     }
@@ -742,7 +742,7 @@ void gcg_eigensolver(void *Ah, void *Bh, double *eval, void **evec, int nevGiven
         prepare_union(*c, A, B, st);
         c->reserve(A->n, c->pub.nevMax, c->pub.nevInit, c->pub.block_size, spmm_blocks(c->upat));
         if (c->precision == GCGE_PREC_MIXED) {
-            const size_t nb = (size_t)A->n * rows_width(std::min(c->pub.block_size, 40), 4);
+            const size_t nb = pcg_block_elems(A->n, rows_width(std::min(c->pub.block_size, 40), 4));
             for (auto *b : {&c->xr32, &c->br32, &c->rr32, &c->pr32, &c->wr32}) b->alloc(nb);
         }
         c->pub.A = Ah;

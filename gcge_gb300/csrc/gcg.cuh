@@ -23,7 +23,7 @@ struct SolverCtx {
     // work buffers
     int n = 0, ld = 0, cap_cols = 0, cap_s = 0, cap_bs = 0;
     DevBuf<double> T1, T2, bbuf, r64;
-    // row-interleaved block-PCG vectors (n x 40 at most)
+    // slice-blocked block-PCG vectors (n x 40 at most)
     DevBuf<double> xr64, br64, rr64, pr64, wr64;
     DevBuf<float> xr32, br32, rr32, pr32, wr32;
     DevBuf<double> M0, M1, evec, work, coefP, ptap, dC, dtmp, gscr, part, dvec, dmax, one;

@@ -20,9 +20,12 @@
 // deterministic for a given grid.  The shifted operator is one SELL matrix
 // S = A + sigma B on the union pattern of A and B (the reference's in-place
 // MatAxpby branch, src/ops_eig_sol_gcg.c:600-608), so each iteration streams
-// one matrix.  Vectors are row-interleaved n x kp blocks (row i's kp values
-// contiguous, kp = k padded to 16 bytes): a gathered row is kp/4 float4 (kp/2
-// double2) loads.  T = double (FP64 GCG) or float (mixed precision: FP32
+// one matrix.  Vectors are slice-blocked n x kp blocks (kp = k padded to 16
+// bytes, G = kp / (16 / sizeof T) 16-byte column groups; for every 32-row
+// slice, group u of its 32 rows is one contiguous 512-byte run): a lane owns
+// a row and gathers a neighbour row as G 16-byte loads, and for a stencil the
+// 32 lanes of a warp read one or two contiguous runs per load instead of 32
+// scattered rows.  T = double (FP64 GCG) or float (mixed precision: FP32
 // values and FP32 accumulation within a block; cross-block sums in double).
 //
 // Every barrier wait is bounded (time and poll count); a wait that runs out
@@ -39,7 +42,7 @@ namespace {
 constexpr unsigned long long kBarrierTimeoutNs = 4000000000ull;  // 4 s
 constexpr long long kBarrierMaxPolls = 1LL << 27;
 
-// 16-byte packs of a row-interleaved block
+// 16-byte packs of a slice-blocked block
 template <typename T>
 struct Pk;
 template <>
@@ -66,6 +69,54 @@ struct Pk<double> {
         *reinterpret_cast<double2 *>(p) = make_double2(v[0], v[1]);
     }
 };
+
+// Element offset of row i, 16-byte group u in a slice-blocked block of width KP.
+template <typename T, int KP>
+__device__ __forceinline__ size_t boff(int i, int u) {
+    constexpr int L = Pk<T>::L, G = KP / L;
+    return ((size_t)(i >> 5) * G + u) * (32 * L) + (size_t)(i & 31) * L;
+}
+
+// acc += sum over the lane's row of a slice of val[e] * X(col[e], :), e =
+// e0 + 32 i, i < width: the column indices and values of the next kPrefetch
+// entries are in flight while the current entry's 16-byte groups are gathered,
+// so the gathers do not wait on the matrix stream.  Groups with ga[u] false
+// are skipped.
+constexpr int kPrefetch = 2;
+template <typename T, int KP>
+__device__ __forceinline__ void gather_row(const int *__restrict__ col, const T *__restrict__ val,
+                                           long long e0, int width, const T *X,
+                                           const bool (&ga)[KP / Pk<T>::L], T (&acc)[KP]) {
+    constexpr int L = Pk<T>::L, G = KP / L;
+    int jq[kPrefetch];
+    T vq[kPrefetch];
+#pragma unroll
+    for (int d = 0; d < kPrefetch; ++d) {
+        const bool in = d < width;
+        jq[d] = in ? __ldg(col + e0 + 32LL * d) : 0;
+        vq[d] = in ? __ldg(val + e0 + 32LL * d) : T(0);
+    }
+#pragma unroll 1
+    for (int e = 0; e < width; ++e) {
+        const int j = jq[0];
+        const T v = vq[0];
+#pragma unroll
+        for (int d = 0; d + 1 < kPrefetch; ++d) {
+            jq[d] = jq[d + 1];
+            vq[d] = vq[d + 1];
+        }
+        const int en = e + kPrefetch;
+        jq[kPrefetch - 1] = en < width ? __ldg(col + e0 + 32LL * en) : 0;
+        vq[kPrefetch - 1] = en < width ? __ldg(val + e0 + 32LL * en) : T(0);
+#pragma unroll
+        for (int u = 0; u < G; ++u) {
+            if (!ga[u]) continue;
+            const Pk<T> x = Pk<T>::ld(X + boff<T, KP>(j, u));
+#pragma unroll
+            for (int q = 0; q < L; ++q) acc[u * L + q] = fma(v, x.v[q], acc[u * L + q]);
+        }
+    }
+}
 
 __device__ __forceinline__ unsigned long long ld_acquire(const unsigned long long *p) {
     unsigned long long v;
@@ -318,19 +369,18 @@ k_block_pcg(PcgArgs<T> a) {
 #pragma unroll
         for (int c = 0; c < KP; ++c) racc[c] = T(0);
         for (int row = r0 + tid; row < r1; row += kPcgThreads) {
-            const size_t o = (size_t)row * KP;
 #pragma unroll
             for (int u = 0; u < G; ++u) {
-                const Pk<T> b = Pk<T>::ld(a.B + o + u * L);
+                const Pk<T> b = Pk<T>::ld(a.B + boff<T, KP>(row, u));
                 Pk<T> z;
 #pragma unroll
                 for (int q = 0; q < L; ++q) {
                     z.v[q] = T(0);
                     racc[u * L + q] = fma(b.v[q], b.v[q], racc[u * L + q]);
                 }
-                b.st(a.R + o + u * L);
-                z.st(a.X + o + u * L);
-                z.st(a.P + o + u * L);
+                b.st(a.R + boff<T, KP>(row, u));
+                z.st(a.X + boff<T, KP>(row, u));
+                z.st(a.P + boff<T, KP>(row, u));
                 group_fence();
             }
         }
@@ -341,24 +391,15 @@ k_block_pcg(PcgArgs<T> a) {
 #pragma unroll
             for (int c = 0; c < KP; ++c) acc[c] = T(0);
             const long long beg = a.sp[s], end = a.sp[s + 1];
-#pragma unroll 1
-            for (long long e = beg + lane; e < end; e += 32) {
-                const int j = __ldg(a.col + e);
-                const T v = __ldg(a.val + e);
-                const T *xj = a.X + (size_t)j * KP;
+            bool all[G];
 #pragma unroll
-                for (int u = 0; u < G; ++u) {
-                    const Pk<T> x = Pk<T>::ld(xj + u * L);
-#pragma unroll
-                    for (int q = 0; q < L; ++q) acc[u * L + q] = fma(v, x.v[q], acc[u * L + q]);
-                }
-            }
+            for (int u = 0; u < G; ++u) all[u] = true;
+            gather_row<T, KP>(a.col, a.val, beg + lane, (int)((end - beg) >> 5), a.X, all, acc);
             const int row = s * 32 + lane;
             if (row < n) {
-                const size_t o = (size_t)row * KP;
 #pragma unroll
                 for (int u = 0; u < G; ++u) {
-                    const Pk<T> b = Pk<T>::ld(a.B + o + u * L);
+                    const Pk<T> b = Pk<T>::ld(a.B + boff<T, KP>(row, u));
                     Pk<T> r, z;
 #pragma unroll
                     for (int q = 0; q < L; ++q) {
@@ -366,8 +407,8 @@ k_block_pcg(PcgArgs<T> a) {
                         z.v[q] = T(0);
                         acc[u * L + q] = r.v[q] * r.v[q];
                     }
-                    r.st(a.R + o + u * L);
-                    z.st(a.P + o + u * L);
+                    r.st(a.R + boff<T, KP>(row, u));
+                    z.st(a.P + boff<T, KP>(row, u));
                 }
             } else {
 #pragma unroll
@@ -383,10 +424,9 @@ k_block_pcg(PcgArgs<T> a) {
 #pragma unroll
         for (int c = 0; c < KP; ++c) bacc[c] = T(0);
         for (int row = r0 + tid; row < r1; row += kPcgThreads) {
-            const size_t o = (size_t)row * KP;
 #pragma unroll
             for (int u = 0; u < G; ++u) {
-                const Pk<T> b = Pk<T>::ld(a.B + o + u * L);
+                const Pk<T> b = Pk<T>::ld(a.B + boff<T, KP>(row, u));
 #pragma unroll
                 for (int q = 0; q < L; ++q) bacc[u * L + q] = fma(b.v[q], b.v[q], bacc[u * L + q]);
                 group_fence();
@@ -446,17 +486,16 @@ k_block_pcg(PcgArgs<T> a) {
         __syncthreads();
         const bool first = it == 0;
         for (int row = r0 + tid; row < r1; row += kPcgThreads) {
-            const size_t o = (size_t)row * KP;
 #pragma unroll
             for (int u = 0; u < G; ++u) {
                 if (!s_gact[u]) continue;
-                const Pk<T> r = Pk<T>::ld(a.R + o + u * L);
-                Pk<T> p = Pk<T>::ld(a.P + o + u * L);
+                const Pk<T> r = Pk<T>::ld(a.R + boff<T, KP>(row, u));
+                Pk<T> p = Pk<T>::ld(a.P + boff<T, KP>(row, u));
 #pragma unroll
                 for (int q = 0; q < L; ++q)
                     if (s_act[u * L + q])
                         p.v[q] = first ? r.v[q] : fma(s_coef[u * L + q], p.v[q], r.v[q]);
-                p.st(a.P + o + u * L);
+                p.st(a.P + boff<T, KP>(row, u));
                 group_fence();
             }
         }
@@ -478,31 +517,18 @@ k_block_pcg(PcgArgs<T> a) {
 #pragma unroll
                 for (int c = 0; c < KP; ++c) acc[c] = T(0);
                 const long long beg = a.sp[s], end = a.sp[s + 1];
-#pragma unroll 1
-    #pragma unroll 1
-            for (long long e = beg + lane; e < end; e += 32) {
-                    const int j = __ldg(a.col + e);
-                    const T v = __ldg(a.val + e);
-                    const T *pj = a.P + (size_t)j * KP;
-#pragma unroll
-                    for (int u = 0; u < G; ++u) {
-                        if (!ga[u]) continue;
-                        const Pk<T> x = Pk<T>::ld(pj + u * L);
-#pragma unroll
-                        for (int q = 0; q < L; ++q) acc[u * L + q] = fma(v, x.v[q], acc[u * L + q]);
-                    }
-                }
+                gather_row<T, KP>(a.col, a.val, beg + lane, (int)((end - beg) >> 5), a.P, ga,
+                                  acc);
                 const int row = s * 32 + lane;
                 if (row < n) {
-                    const size_t o = (size_t)row * KP;
 #pragma unroll
                     for (int u = 0; u < G; ++u) {
                         if (!ga[u]) continue;
                         Pk<T> w;
 #pragma unroll
                         for (int q = 0; q < L; ++q) w.v[q] = acc[u * L + q];
-                        w.st(a.W + o + u * L);
-                        const Pk<T> p = Pk<T>::ld(a.P + o + u * L);
+                        w.st(a.W + boff<T, KP>(row, u));
+                        const Pk<T> p = Pk<T>::ld(a.P + boff<T, KP>(row, u));
 #pragma unroll
                         for (int q = 0; q < L; ++q)
                             acc[u * L + q] = s_act[u * L + q] ? p.v[q] * w.v[q] : T(0);
@@ -556,14 +582,13 @@ k_block_pcg(PcgArgs<T> a) {
 #pragma unroll
             for (int c = 0; c < KP; ++c) racc[c] = T(0);
             for (int row = r0 + tid; row < r1; row += kPcgThreads) {
-                const size_t o = (size_t)row * KP;
 #pragma unroll
                 for (int u = 0; u < G; ++u) {
                     if (!s_gact[u]) continue;
-                    Pk<T> x = Pk<T>::ld(a.X + o + u * L);
-                    Pk<T> r = Pk<T>::ld(a.R + o + u * L);
-                    const Pk<T> p = Pk<T>::ld(a.P + o + u * L);
-                    const Pk<T> w = Pk<T>::ld(a.W + o + u * L);
+                    Pk<T> x = Pk<T>::ld(a.X + boff<T, KP>(row, u));
+                    Pk<T> r = Pk<T>::ld(a.R + boff<T, KP>(row, u));
+                    const Pk<T> p = Pk<T>::ld(a.P + boff<T, KP>(row, u));
+                    const Pk<T> w = Pk<T>::ld(a.W + boff<T, KP>(row, u));
 #pragma unroll
                     for (int q = 0; q < L; ++q) {
                         const int c = u * L + q;
@@ -574,8 +599,8 @@ k_block_pcg(PcgArgs<T> a) {
                             racc[c] = fma(r.v[q], r.v[q], racc[c]);
                         }
                     }
-                    x.st(a.X + o + u * L);
-                    r.st(a.R + o + u * L);
+                    x.st(a.X + boff<T, KP>(row, u));
+                    r.st(a.R + boff<T, KP>(row, u));
                     group_fence();
                 }
             }
@@ -641,15 +666,32 @@ void launch_block_pcg(PcgArgs<T> a, cudaStream_t st) {
 
 }  // namespace
 
-// column-major (S, ld) <-> row-interleaved (T, kp); padding columns are zero
+// column-major (S, ld) <-> slice-blocked (T, kp): element (i, c) of the
+// blocked block sits at ((i / 32) G + c / L) 32 L + (i % 32) L + c % L with
+// L = 16 / sizeof(T), G = kp / L; rows up to the next multiple of 32 and
+// columns k..kp-1 are zero.
+template <typename T>
+__host__ __device__ __forceinline__ size_t blk_index(int i, int c, int kp) {
+    constexpr int L = 16 / (int)sizeof(T);
+    const int G = kp / L;
+    return ((size_t)(i >> 5) * G + c / L) * (32 * L) + (size_t)(i & 31) * L + c % L;
+}
 template <typename S, typename T>
 __global__ void k_col_to_rows(int n, int k, int kp, const S *__restrict__ X, int ldx,
                               T *__restrict__ Y) {
-    const size_t total = (size_t)n * kp;
+    constexpr int L = 16 / (int)sizeof(T);
+    const int G = kp / L;
+    const size_t total = (size_t)((n + 31) / 32) * 32 * kp;
     for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < total;
          t += (size_t)gridDim.x * blockDim.x) {
-        const int i = (int)(t / kp), c = (int)(t % kp);
-        Y[t] = c < k ? (T)X[i + (size_t)c * ldx] : T(0);
+        // t = ((s G + u) 32 + l) L + e
+        const int e = (int)(t % L);
+        const size_t q = t / L;
+        const int l = (int)(q % 32);
+        const size_t su = q / 32;
+        const int u = (int)(su % G);
+        const int i = (int)(su / G) * 32 + l, c = u * L + e;
+        Y[t] = (i < n && c < k) ? (T)X[i + (size_t)c * ldx] : T(0);
     }
 }
 template <typename T, typename D>
@@ -659,7 +701,7 @@ __global__ void k_rows_to_col(int n, int k, int kp, const T *__restrict__ X, D *
     for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < total;
          t += (size_t)gridDim.x * blockDim.x) {
         const int c = (int)(t / n), i = (int)(t % n);
-        const D v = (D)X[(size_t)i * kp + c];
+        const D v = (D)X[blk_index<T>(i, c, kp)];
         D &y = Y[i + (size_t)c * ldy];
         y = add ? y + v : v;
     }
@@ -667,7 +709,7 @@ __global__ void k_rows_to_col(int n, int k, int kp, const T *__restrict__ X, D *
 
 template <typename S, typename T>
 void col_to_rows(int n, int k, int kp, const S *X, int ldx, T *Y, cudaStream_t st) {
-    const size_t total = (size_t)n * kp;
+    const size_t total = (size_t)((n + 31) / 32) * 32 * kp;
     const int g = (int)std::max<size_t>(1, std::min<size_t>((total + 255) / 256, 16 * num_sms_pcg()));
     k_col_to_rows<S, T><<<g, 256, 0, st>>>(n, k, kp, X, ldx, Y);
     GCGE_CHECK_LAUNCH();

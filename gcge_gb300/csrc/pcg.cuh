@@ -58,8 +58,8 @@ struct PcgWork {
 
 // Solve S x = b column-wise (S on the SELL pattern `pat` with values sval)
 // starting from x (or from 0 when x_zero, in which case x need not be
-// initialised).  B, X, R, P, W are row-interleaved n x kp blocks (row i at
-// i*kp, padding columns of B and X zero).  One cooperative launch runs the
+// initialised).  B, X, R, P, W are slice-blocked n x kp blocks
+// (pcg_block_elems; padding rows and columns of B and X zero).  One cooperative launch runs the
 // whole iteration; the iteration count and any error stay on the device
 // (PcgWork::collect, or pcg_last_iters after a synchronisation).
 template <typename T>
@@ -69,7 +69,10 @@ void block_pcg_rows(PcgWork &wk, const SellPattern &pat, const T *sval, const T 
 // Iterations of the last solve (synchronises the stream).
 int pcg_last_iters(PcgWork &wk, cudaStream_t st);
 
-// Column-major (ld) <-> row-interleaved (kp) block conversions.
+// Elements of a slice-blocked n x kp block (rows padded to a multiple of 32).
+inline size_t pcg_block_elems(int n, int kp) { return (size_t)((n + 31) / 32) * 32 * kp; }
+
+// Column-major (ld) <-> slice-blocked (kp) block conversions (pcg.cu).
 template <typename S, typename T>
 void col_to_rows(int n, int k, int kp, const S *X, int ldx, T *Y, cudaStream_t st);
 template <typename T, typename D>

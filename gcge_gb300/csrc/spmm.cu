@@ -1,6 +1,6 @@
-// Sparse kernels on SELL-32 matrices: SpMM over a block of columns, the fused
-// residual norm ||(A - lambda_c B) x_c||^2 of CheckConvergence, and SpMM on
-// row-interleaved blocks with a fused per-column dot product (block-PCG).
+// Sparse kernels on SELL-32 matrices: SpMM over a block of columns and the
+// fused residual norm ||(A - lambda_c B) x_c||^2 of CheckConvergence (the
+// block-PCG SpMM lives inside the persistent kernel of pcg.cu).
 //
 // Layout: one warp owns one 32-row slice; lane l owns row 32*slice + l and
 // walks the slice's entries e = 0..width-1 at slice_ptr + e*32 + l, so each
@@ -194,117 +194,11 @@ template void spmm<float>(const SellPattern &, const float *, const float *, int
                           int, cudaStream_t);
 }  // namespace gcge
 
-// ==================================================================== rows
-// SpMM on row-interleaved blocks: X and Y are n x kp with row i's kp values
-// contiguous (kp = k padded to 16 bytes).  Per nonzero a lane issues kp/4
-// float4 (kp/2 double2) loads of one contiguous row of X, and the 32 lanes of
-// a warp read 32 neighbouring rows of a stencil offset: one contiguous span.
-// The fused variant adds the per-column partial sums of X(i,:) .* Y(i,:)
-// (block-PCG p^T w).
+// ==================================================================== widths
 namespace gcge {
 
-template <typename T>
-struct Vec16;
-template <>
-struct Vec16<float> {
-    using type = float4;
-    static constexpr int n = 4;
-};
-template <>
-struct Vec16<double> {
-    using type = double2;
-    static constexpr int n = 2;
-};
-
-template <typename T, int KP>
-__device__ __forceinline__ void load_row(const T *__restrict__ p, T (&v)[KP]) {
-    using V = typename Vec16<T>::type;
-    constexpr int L = Vec16<T>::n;
-    const V *q = reinterpret_cast<const V *>(p);
-#pragma unroll
-    for (int u = 0; u < KP / L; ++u) {
-        const V t = __ldg(q + u);
-        if constexpr (L == 4) {
-            v[4 * u] = t.x;
-            v[4 * u + 1] = t.y;
-            v[4 * u + 2] = t.z;
-            v[4 * u + 3] = t.w;
-        } else {
-            v[2 * u] = t.x;
-            v[2 * u + 1] = t.y;
-        }
-    }
-}
-template <typename T, int KP>
-__device__ __forceinline__ void store_row(T *__restrict__ p, const T (&v)[KP]) {
-    using V = typename Vec16<T>::type;
-    constexpr int L = Vec16<T>::n;
-    V *q = reinterpret_cast<V *>(p);
-#pragma unroll
-    for (int u = 0; u < KP / L; ++u) {
-        V t;
-        if constexpr (L == 4) {
-            t.x = v[4 * u];
-            t.y = v[4 * u + 1];
-            t.z = v[4 * u + 2];
-            t.w = v[4 * u + 3];
-        } else {
-            t.x = v[2 * u];
-            t.y = v[2 * u + 1];
-        }
-        q[u] = t;
-    }
-}
-
-template <typename T, int KP, bool DOT>
-__global__ void __launch_bounds__(kSpmmThreads)
-k_spmm_rows(const long long *__restrict__ sp, const int *__restrict__ col, const T *__restrict__ val,
-            int n, int nslices, const T *__restrict__ X, T *__restrict__ Y,
-            const int *__restrict__ active, int k, double *__restrict__ partial, int kmax) {
-    const int slice = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    T acc[KP];
-#pragma unroll
-    for (int c = 0; c < KP; ++c) acc[c] = T(0);
-    const int row = slice * 32 + lane;
-    if (slice < nslices) {
-        const long long beg = sp[slice], end = sp[slice + 1];
-        for (long long e = beg + lane; e < end; e += 32) {
-            const int j = __ldg(col + e);
-            const T a = __ldg(val + e);
-            T xv[KP];
-            load_row<T, KP>(X + (size_t)j * KP, xv);
-#pragma unroll
-            for (int c = 0; c < KP; ++c) acc[c] = fma(a, xv[c], acc[c]);
-        }
-        if (row < n) store_row<T, KP>(Y + (size_t)row * KP, acc);
-    }
-    if constexpr (DOT) {
-        __shared__ double red[kSpmmThreads / 32][KP];
-        T xr[KP];
-        if (slice < nslices && row < n) {
-            load_row<T, KP>(X + (size_t)row * KP, xr);
-        } else {
-#pragma unroll
-            for (int c = 0; c < KP; ++c) xr[c] = T(0);
-        }
-#pragma unroll
-        for (int c = 0; c < KP; ++c) {
-            T v = (c < k && (active == nullptr || active[c])) ? xr[c] * acc[c] : T(0);
-            for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-            if (lane == 0) red[warp][c] = (double)v;
-        }
-        __syncthreads();
-        for (int c = threadIdx.x; c < KP; c += blockDim.x) {
-            double s = 0.0;
-#pragma unroll
-            for (int w = 0; w < kSpmmThreads / 32; ++w) s += red[w][c];
-            if (c < kmax) partial[(size_t)blockIdx.x * kmax + c] = s;
-        }
-    }
-}
-
-// Smallest instantiated row width >= k whose rows are 16-byte aligned.
+// Smallest block-PCG row width >= k whose 16-byte column groups are whole
+// (instantiated widths of the block-PCG kernel).
 int rows_width(int k, int elem_bytes) {
     static const int w32[] = {4, 8, 12, 16, 20, 24, 28, 32, 36, 40};
     static const int w64[] = {2, 4, 6, 8, 12, 16, 20, 24, 28, 32, 36, 40};
@@ -315,34 +209,7 @@ int rows_width(int k, int elem_bytes) {
         for (int w : w64)
             if (w >= k) return w;
     }
-    throw CudaError{GCGE_ERR_ARG, "row SpMM: block wider than 40 columns"};
+    throw CudaError{GCGE_ERR_ARG, "block PCG: block wider than 40 columns"};
 }
-
-template <typename T>
-int spmm_rows(const SellPattern &pat, const T *val, const T *X, T *Y, int kp, int k,
-              const int *active, double *partial, int kmax, bool dot, cudaStream_t st) {
-    const int blocks = spmm_blocks(pat);
-    if (pat.n == 0) return 0;
-    GCGE_REQUIRE(kp % (16 / (int)sizeof(T)) == 0 && kp <= 40, GCGE_ERR_ARG,
-                 "spmm_rows: row width");
-    if (dot) {
-        GCGE_REQUIRE(k <= kmax, GCGE_ERR_ARG, "spmm_rows: partial width");
-        GCGE_KP_DISPATCH(T, kp, (k_spmm_rows<T, KP, true><<<blocks, kSpmmThreads, 0, st>>>(
-                                     pat.slice_ptr.p, pat.col.p, val, pat.n, pat.nslices, X, Y,
-                                     active, k, partial, kmax)));
-    } else {
-        GCGE_KP_DISPATCH(T, kp, (k_spmm_rows<T, KP, false><<<blocks, kSpmmThreads, 0, st>>>(
-                                     pat.slice_ptr.p, pat.col.p, val, pat.n, pat.nslices, X, Y,
-                                     nullptr, k, nullptr, 0)));
-    }
-    GCGE_CHECK_LAUNCH();
-    count_launch();
-    return blocks;
-}
-
-template int spmm_rows<float>(const SellPattern &, const float *, const float *, float *, int, int,
-                              const int *, double *, int, bool, cudaStream_t);
-template int spmm_rows<double>(const SellPattern &, const double *, const double *, double *, int,
-                               int, const int *, double *, int, bool, cudaStream_t);
 
 }  // namespace gcge

@@ -63,7 +63,7 @@ int GCGE_BlockPCG(void *A, void *B, double sigma, void **b, void **x, int k, int
         } else {
             const int kp = rows_width(k, 4);
             DevBuf<float> x32, b32, r32, p32, w32;
-            for (auto *bb : {&x32, &b32, &r32, &p32, &w32}) bb->alloc((size_t)n * kp);
+            for (auto *bb : {&x32, &b32, &r32, &p32, &w32}) bb->alloc(pcg_block_elems(n, kp));
             col_to_rows<double, float>(n, k, kp, xv->data, xv->ld, x32.p, st);
             col_to_rows<double, float>(n, k, kp, bv->data, bv->ld, b32.p, st);
             block_pcg_rows<float>(c.pcg, c.upat, c.us32.p, b32.p, x32.p, r32.p, p32.p, w32.p,
