@@ -24,6 +24,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libgcge_cuda.so")
 
 GCGE_OK = 0
+GCGE_ERR_CUDA = 1
+GCGE_ERR_ARG = 2
 GCGE_ERR_NOT_CONVERGED = 6
 PREC_FP64 = 0
 PREC_MIXED = 1

@@ -158,11 +158,21 @@ static void CUDA_MatView(void *mat, OPS *ops) {
     GCGE_TRY({
         SparseMat *A = as_mat(mat);
         GCGE_REQUIRE(A != nullptr, GCGE_ERR_HANDLE, "MatView");
+        std::vector<int> ptr(A->n + 1), ind(std::max<long long>(A->nnz, 1));
+        std::vector<double> val(std::max<long long>(A->nnz, 1));
+        GCGE_CUDA(cudaMemcpy(ptr.data(), A->csr.ptr.p, sizeof(int) * (A->n + 1),
+                             cudaMemcpyDeviceToHost));
+        if (A->nnz > 0) {
+            GCGE_CUDA(cudaMemcpy(ind.data(), A->csr.ind.p, sizeof(int) * A->nnz,
+                                 cudaMemcpyDeviceToHost));
+            GCGE_CUDA(cudaMemcpy(val.data(), A->csr.val.p, sizeof(double) * A->nnz,
+                                 cudaMemcpyDeviceToHost));
+        }
         for (int i = 0; i < A->n; ++i) {
             for (int j = 0; j < A->n; ++j) {
                 double v = 0.0;
-                for (int e = A->h_ptr[i]; e < A->h_ptr[i + 1]; ++e)
-                    if (A->h_ind[e] == j) v += A->h_val[e];
+                for (int e = ptr[i]; e < ptr[i + 1]; ++e)
+                    if (ind[e] == j) v += val[e];
                 ops->Printf("%6.4e\t", v);
             }
             ops->Printf("\n");
@@ -577,42 +587,24 @@ int CUDA_MatCreateFromCCS(void **mat, int nrows, int ncols, const int *j_col, co
         const long long nnz = j_col[n];
         GCGE_REQUIRE(nnz >= 0 && (nnz == 0 || (i_row && data)), GCGE_ERR_ARG,
                      "CUDA_MatCreateFromCCS: arrays");
+        for (int j = 0; j < n; ++j)
+            GCGE_REQUIRE(j_col[j] <= j_col[j + 1], GCGE_ERR_ARG,
+                         "CUDA_MatCreateFromCCS: column pointers must not decrease");
+        GCGE_REQUIRE(j_col[0] == 0, GCGE_ERR_ARG, "CUDA_MatCreateFromCCS: j_col[0] must be 0");
         SparseMat *A = new SparseMat();
         A->serial = g_serial.fetch_add(1);
         A->n = n;
         A->nnz = nnz;
-        // CCS -> CSR (transpose by counting), so y = A x holds for any A
-        A->h_ptr.assign(n + 1, 0);
-        for (long long e = 0; e < nnz; ++e) {
-            const int r = i_row[e];
-            if (r < 0 || r >= n) {
-                delete A;
-                throw CudaError{GCGE_ERR_ARG, "CUDA_MatCreateFromCCS: row index out of range"};
-            }
-            A->h_ptr[r + 1]++;
-        }
-        for (int i = 0; i < n; ++i) A->h_ptr[i + 1] += A->h_ptr[i];
-        A->h_ind.assign(nnz, 0);
-        A->h_val.assign(nnz, 0.0);
-        std::vector<int> fill(A->h_ptr.begin(), A->h_ptr.end() - 1);
-        for (int j = 0; j < n; ++j)
-            for (int e = j_col[j]; e < j_col[j + 1]; ++e) {
-                const int r = i_row[e];
-                A->h_ind[fill[r]] = j;
-                A->h_val[fill[r]] = data[e];
-                fill[r]++;
-            }
-        std::vector<std::vector<double>> vals;
-        std::vector<int> h_col;
-        std::vector<long long> h_sp;
-        sell_from_csr(n, A->h_ptr.data(), A->h_ind.data(), {A->h_val.data()}, A->pat, vals, h_col, h_sp);
         cudaStream_t st = lib_stream();
-        upload_sell(A->pat, h_col, h_sp, st);
-        A->val.alloc(std::max<size_t>(A->pat.padded, 1));
-        if (A->pat.padded)
-            GCGE_CUDA(cudaMemcpyAsync(A->val.p, vals[0].data(), sizeof(double) * A->pat.padded,
-                                      cudaMemcpyHostToDevice, st));
-        GCGE_CUDA(cudaStreamSynchronize(st));
+        try {
+            // CCS -> CSR on the device (y = A x for any A), then SELL-32
+            csr_from_ccs_device(n, j_col, i_row, data, A->csr, st);
+            sell_from_csr_device(A->csr, nullptr, A->pat, A->val, nullptr, st);
+            GCGE_CUDA(cudaStreamSynchronize(st));
+        } catch (...) {
+            delete A;
+            throw;
+        }
         *mat = A;
     });
 }

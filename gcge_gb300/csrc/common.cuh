@@ -119,14 +119,20 @@ struct SellPattern {
     DevBuf<int> col;
 };
 
+// CSR on the device, rows sorted by column (format.cu).
+struct DevCsr {
+    int n = 0;
+    long long nnz = 0;
+    DevBuf<int> ptr, ind;
+    DevBuf<double> val;
+};
+
 struct SparseMat {
     uint32_t magic = kMatMagic;
     unsigned long long serial = 0;  // unique per created matrix
     int n = 0;
     long long nnz = 0;
-    // host CSR copy (symmetric matrix: CSR == CCS)
-    std::vector<int> h_ptr, h_ind;
-    std::vector<double> h_val;
+    DevCsr csr;              // y = A x orientation, rows sorted
     SellPattern pat;
     DevBuf<double> val;      // FP64 values in SELL order
 };
@@ -134,14 +140,18 @@ struct SparseMat {
 MultiVec *as_mv(void *h);
 SparseMat *as_mat(void *h);
 
-// SELL-32 construction from host CSR arrays (row indices sorted or not).
-// Every input value array is laid out in the padded SELL order; the pattern
-// (slice pointers, column indices) is returned on the host for upload.
-void sell_from_csr(int n, const int *ptr, const int *ind, const std::vector<const double *> &vals,
-                   SellPattern &pat, std::vector<std::vector<double>> &out_vals,
-                   std::vector<int> &h_col, std::vector<long long> &h_sp);
-void upload_sell(SellPattern &pat, const std::vector<int> &h_col, const std::vector<long long> &h_sp,
-                 cudaStream_t st);
+// Device-side formats (format.cu).  csr_from_ccs_device uploads a CCS matrix
+// (column pointers, row indices, values on the host) and transposes it to CSR;
+// union_csr_device merges A's and B's patterns and the diagonal (B null: the
+// identity) with A's values in U.val and B's in ub; sell_from_csr_device lays
+// a CSR (and optionally a second value array in the same order) out as SELL-32.
+void csr_from_ccs_device(int n, const int *h_colptr, const int *h_rowind, const double *h_val,
+                         DevCsr &out, cudaStream_t st);
+void union_csr_device(const DevCsr &A, const DevCsr *B, DevCsr &U, DevBuf<double> &ub,
+                      cudaStream_t st);
+void sell_from_csr_device(const DevCsr &M, const double *second, SellPattern &pat,
+                          DevBuf<double> &v0, DevBuf<double> *v1, cudaStream_t st);
+
 
 // ---------------------------------------------------------------- launchers
 // Sparse (spmm.cu).  X, Y column-major with leading dimensions; k columns.

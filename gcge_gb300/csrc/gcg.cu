@@ -27,9 +27,6 @@
 
 namespace gcge {
 
-void upload_sell(SellPattern &pat, const std::vector<int> &h_col,
-                 const std::vector<long long> &h_sp, cudaStream_t st);
-
 static inline double *colp(MultiVec *X, int c) { return X->data + (size_t)c * X->ld; }
 static inline int round32(int n) { return (n + 31) / 32 * 32; }
 
@@ -666,52 +663,15 @@ struct GcgRun {
 void prepare_union(SolverCtx &c, SparseMat *A, SparseMat *B, cudaStream_t st) {
     const unsigned long long ka = A->serial, kb = B ? B->serial : 0ULL;
     if (c.has_union && c.keyA == ka && c.keyB == kb) return;
-    const int n = A->n;
-    std::vector<int> ptr(n + 1, 0), ind;
-    std::vector<double> av, bv;
-    ind.reserve(A->h_ind.size() + (B ? B->h_ind.size() : 0) + n);
-    av.reserve(ind.capacity());
-    bv.reserve(ind.capacity());
-    std::vector<std::pair<int, std::pair<double, double>>> row;
-    for (int i = 0; i < n; ++i) {
-        row.clear();
-        for (int e = A->h_ptr[i]; e < A->h_ptr[i + 1]; ++e) row.push_back({A->h_ind[e], {A->h_val[e], 0.0}});
-        if (B) {
-            for (int e = B->h_ptr[i]; e < B->h_ptr[i + 1]; ++e) row.push_back({B->h_ind[e], {0.0, B->h_val[e]}});
-        } else {
-            row.push_back({i, {0.0, 1.0}});
-        }
-        row.push_back({i, {0.0, 0.0}});
-        std::sort(row.begin(), row.end(), [](const auto &x, const auto &y) { return x.first < y.first; });
-        int last = -1;
-        for (auto &e : row) {
-            if (e.first == last) {
-                av.back() += e.second.first;
-                bv.back() += e.second.second;
-            } else {
-                ind.push_back(e.first);
-                av.push_back(e.second.first);
-                bv.push_back(e.second.second);
-                last = e.first;
-            }
-        }
-        ptr[i + 1] = (int)ind.size();
-    }
-    std::vector<std::vector<double>> vals;
-    std::vector<int> h_col;
-    std::vector<long long> h_sp;
-    sell_from_csr(n, ptr.data(), ind.data(), {av.data(), bv.data()}, c.upat, vals, h_col, h_sp);
-    upload_sell(c.upat, h_col, h_sp, st);
+    // union pattern of A, B (or the identity) and the diagonal, built on the device
+    DevCsr U;
+    DevBuf<double> ubv;
+    union_csr_device(A->csr, B ? &B->csr : nullptr, U, ubv, st);
+    sell_from_csr_device(U, ubv.p, c.upat, c.ua, &c.ub, st);
     const size_t P = std::max<size_t>(c.upat.padded, 1);
-    c.ua.alloc(P);
-    c.ub.alloc(P);
     c.us64.alloc(P);
     c.us32.alloc(P);
-    GCGE_CUDA(cudaMemcpyAsync(c.ua.p, vals[0].data(), sizeof(double) * c.upat.padded,
-                              cudaMemcpyHostToDevice, st));
-    GCGE_CUDA(cudaMemcpyAsync(c.ub.p, vals[1].data(), sizeof(double) * c.upat.padded,
-                              cudaMemcpyHostToDevice, st));
-    GCGE_CUDA(cudaStreamSynchronize(st));
+    GCGE_CUDA(cudaStreamSynchronize(st));  // U and ubv are freed on return
     c.keyA = ka;
     c.keyB = kb;
     c.has_union = true;

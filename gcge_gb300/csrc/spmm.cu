@@ -22,61 +22,6 @@ int spmm_blocks(const SellPattern &pat) {
     return (pat.nslices + (kSpmmThreads / 32) - 1) / (kSpmmThreads / 32);
 }
 
-// Host-side SELL construction.  Returns the padded value arrays in host memory
-// (one per input value array) so callers can upload them or derive others.
-void sell_from_csr(int n, const int *ptr, const int *ind, const std::vector<const double *> &vals,
-                   SellPattern &pat, std::vector<std::vector<double>> &out_vals,
-                   std::vector<int> &h_col, std::vector<long long> &h_sp) {
-    const int ns = (n + 31) / 32;
-    h_sp.assign(ns + 1, 0);
-    long long nnz = 0;
-    for (int s = 0; s < ns; ++s) {
-        int w = 0;
-        for (int l = 0; l < 32; ++l) {
-            int r = s * 32 + l;
-            if (r < n) w = std::max(w, ptr[r + 1] - ptr[r]);
-        }
-        h_sp[s + 1] = h_sp[s] + (long long)w * 32;
-    }
-    nnz = ptr[n];
-    const long long padded = h_sp[ns];
-    h_col.assign(padded, 0);
-    out_vals.assign(vals.size(), std::vector<double>(padded, 0.0));
-    for (int s = 0; s < ns; ++s) {
-        const long long base = h_sp[s];
-        const int w = (int)((h_sp[s + 1] - base) / 32);
-        for (int l = 0; l < 32; ++l) {
-            const int r = s * 32 + l;
-            const int rr = r < n ? r : n - 1;
-            const int len = r < n ? ptr[r + 1] - ptr[r] : 0;
-            for (int e = 0; e < w; ++e) {
-                const long long pos = base + (long long)e * 32 + l;
-                if (e < len) {
-                    h_col[pos] = ind[ptr[r] + e];
-                    for (size_t v = 0; v < vals.size(); ++v) out_vals[v][pos] = vals[v][ptr[r] + e];
-                } else {
-                    h_col[pos] = rr;  // padding: own row, zero value
-                }
-            }
-        }
-    }
-    pat.n = n;
-    pat.nslices = ns;
-    pat.nnz = nnz;
-    pat.padded = padded;
-}
-
-void upload_sell(SellPattern &pat, const std::vector<int> &h_col, const std::vector<long long> &h_sp,
-                 cudaStream_t st) {
-    pat.slice_ptr.alloc(h_sp.size());
-    pat.col.alloc(std::max<size_t>(h_col.size(), 1));
-    GCGE_CUDA(cudaMemcpyAsync(pat.slice_ptr.p, h_sp.data(), h_sp.size() * sizeof(long long),
-                              cudaMemcpyHostToDevice, st));
-    if (!h_col.empty())
-        GCGE_CUDA(cudaMemcpyAsync(pat.col.p, h_col.data(), h_col.size() * sizeof(int),
-                                  cudaMemcpyHostToDevice, st));
-}
-
 // ---------------------------------------------------------------- kernels
 template <typename T, int K>
 __global__ void __launch_bounds__(kSpmmThreads)

@@ -51,6 +51,61 @@ def test_nonsymmetric_ccs_is_y_equals_a_x(ops, gpu_lib):
     np.testing.assert_allclose(ops.download(y, 0, 3), M @ X, rtol=0, atol=1e-12)
 
 
+def test_ccs_upload_edge_cases(ops, gpu_lib):
+    """The device-side CCS -> CSR -> SELL pipeline: unsorted row indices within
+    columns, duplicate entries (summed, as y = A x sums them), empty rows and
+    columns, rows longer than a slice is wide elsewhere, n not a multiple of 32;
+    and an out-of-range row index is rejected with an error, not a fault."""
+    import ctypes
+    rng = np.random.default_rng(4)
+    n = 77
+    cols = []
+    for j in range(n):
+        if j % 11 == 5:
+            cols.append(([], []))                      # empty column
+            continue
+        k = rng.integers(1, 6)
+        rows = list(rng.choice(n, size=k, replace=False))
+        if j % 7 == 0:
+            rows.append(rows[0])                       # duplicate (r, j)
+        rows = [r for r in rows if r % 13 != 3]        # rows 3, 16, ... stay empty
+        if j == 40:
+            rows += list(range(0, n, 2))               # one long column -> long rows? (columns)
+        rng.shuffle(rows)                              # unsorted within the column
+        cols.append((rows, list(rng.standard_normal(len(rows)))))
+    rows = [r for r in range(n) if r % 13 != 3]
+    cols[9] = (rows, list(rng.standard_normal(len(rows))))  # a dense column -> long rows
+    indptr = np.zeros(n + 1, dtype=np.int32)
+    ind, val = [], []
+    for j, (rr, vv) in enumerate(cols):
+        ind += [int(r) for r in rr]
+        val += [float(v) for v in vv]
+        indptr[j + 1] = len(ind)
+    ind = np.array(ind, dtype=np.int32)
+    val = np.array(val)
+    dense = np.zeros((n, n))
+    for j in range(n):
+        for e in range(indptr[j], indptr[j + 1]):
+            dense[ind[e], j] += val[e]
+    h = ops.mat(P.CSRMatrix(n, indptr, ind, val))
+    X = rng.standard_normal((n, 5))
+    x = ops.multivec(h, 5, X)
+    y = ops.multivec(h, 5)
+    ops.mat_dot(h, x, y, (0, 0), (5, 5))
+    np.testing.assert_allclose(ops.download(y, 0, 5), dense @ X, rtol=0, atol=1e-12)
+    bad = ind.copy()
+    bad[3] = n + 5
+    hb = ctypes.c_void_p()
+    st = gpu_lib.load().CUDA_MatCreateFromCCS(ctypes.byref(hb), ctypes.c_int(n), ctypes.c_int(n),
+                                              indptr.ctypes.data_as(ctypes.c_void_p),
+                                              bad.ctypes.data_as(ctypes.c_void_p),
+                                              val.ctypes.data_as(ctypes.c_void_p))
+    assert st == gpu_lib.GCGE_ERR_ARG
+    # the library still works afterwards
+    ops.mat_dot(h, x, y, (0, 0), (5, 5))
+    np.testing.assert_allclose(ops.download(y, 0, 5), dense @ X, rtol=0, atol=1e-12)
+
+
 @pytest.mark.parametrize("alpha,beta,usex", [(2.0, -1.0, True), (0.5, 0.0, True), (0.0, 3.0, False),
                                              (1.0, 1.0, True)])
 def test_axpby(ops, alpha, beta, usex):
