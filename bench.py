@@ -14,7 +14,8 @@ second (nev / solve time).  `value` is the mixed-precision solver (FP32
 block-PCG inner solve, everything else FP64) with inputs resident in HBM,
 timed with CUDA events on the library stream; `fp64_value` is the plain FP64
 GPU GCG on the same inputs; `e2e` is the same metric through GCGE_Solve from
-host CCS arrays (matrix upload, SELL build, solve, eigenvector download).
+host CCS arrays in pinned memory (matrix upload, device-side format build,
+solve, eigenvalue and eigenvector download into pinned memory).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
@@ -223,6 +224,7 @@ def run_reference(args, d: Dist):
 
 def run_ours(args, d: Dist):
     os.environ.setdefault("CUDA_VISIBLE_DEVICES", str(d.local))
+    import numpy as np
     import gcge_gb300 as G
     G.load(build_if_missing=True)
     c, X0 = build_workload(args.size)
@@ -254,13 +256,24 @@ def run_ours(args, d: Dist):
     value = d.sum(pairs_mixed) / t_mixed_max
     fp64_value = d.sum(pairs_fp64) / d.max(t_fp64)
 
-    # end to end through GCGE_Solve from host arrays
+    # end to end through GCGE_Solve: every step uploads the CCS arrays and the
+    # initial block from pinned host memory, builds the formats, solves, and
+    # reads eigenvalues and eigenvectors back into pinned host memory
+    from gcge_gb300 import problems as PP
+    pA = PP.CSRMatrix(A.n, G.pinned_copy(A.indptr.astype(np.int32)),
+                      G.pinned_copy(A.indices.astype(np.int32)), G.pinned_copy(A.data))
+    pB = PP.CSRMatrix(B.n, G.pinned_copy(B.indptr.astype(np.int32)),
+                      G.pinned_copy(B.indices.astype(np.int32)), G.pinned_copy(B.data))
+    kw_e2e = dict(kw)
+    kw_e2e["X0"] = G.pinned_copy(np.asfortranarray(X0), order="F")
+    ev_out = G.pinned_empty(c["nev_max"])
+    evec_out = G.pinned_empty((A.n, c["nev_max"]), order="F")
     e2e_steps = max(1, args.steps // 2)
     d.barrier()
     t0 = time.perf_counter()
     e2e_pairs = 0
     for _ in range(e2e_steps):
-        r = G.solve(A, B, precision=G.PREC_MIXED, **kw)
+        r = G.solve(pA, pB, precision=G.PREC_MIXED, evec_out=evec_out, eval_out=ev_out, **kw_e2e)
         e2e_pairs += min(r.nconv, nev) if r.status == G.GCGE_OK else 0
     t_e2e = d.max(time.perf_counter() - t0)
     e2e_value = d.sum(e2e_pairs) / t_e2e

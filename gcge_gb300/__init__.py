@@ -41,7 +41,7 @@ EXPORTED_SYMBOLS = [
     "GCGE_SetPrecision", "GCGE_Solve", "GCGE_GetSolveInfo", "GCGE_Prepare", "GCGE_PreparedSolve",
     "GCGE_PreparedDestroy", "GCGE_BenchSpMM", "GCGE_DenseEig", "GCGE_BlockPCG", "GCGE_BOrth",
     "GCGE_TimerStart", "GCGE_TimerStop", "GCGE_GramNoAlloc", "GCGE_DenseGram",
-    "GCGE_DenseLinComb",
+    "GCGE_DenseLinComb", "GCGE_HostAlloc", "GCGE_HostFree",
 ]
 
 _lib = None
@@ -110,6 +110,9 @@ def load(build_if_missing: bool = False) -> ctypes.CDLL:
                  "GCGE_TimerStart", "GCGE_GramNoAlloc", "GCGE_DenseGram", "GCGE_DenseLinComb"):
         getattr(lib, name).restype = ctypes.c_int
     lib.GCGE_TimerStop.restype = ctypes.c_double
+    lib.GCGE_HostAlloc.restype = ctypes.c_void_p
+    lib.GCGE_HostAlloc.argtypes = [ctypes.c_size_t]
+    lib.GCGE_HostFree.argtypes = [ctypes.c_void_p]
     _lib = lib
     return lib
 
@@ -136,18 +139,59 @@ class SolveResult:
     info: dict = field(default_factory=dict)
 
 
+class _HostBlock:
+    """Owner of a GCGE_HostAlloc block; frees it when the last view goes."""
+
+    def __init__(self, nbytes):
+        self.lib = load()
+        self.ptr = self.lib.GCGE_HostAlloc(ctypes.c_size_t(max(int(nbytes), 1)))
+        if not self.ptr:
+            raise GCGEError(3, "GCGE_HostAlloc")
+
+    def __del__(self):
+        if getattr(self, "ptr", None):
+            self.lib.GCGE_HostFree(ctypes.c_void_p(self.ptr))
+            self.ptr = None
+
+
+def pinned_empty(shape, dtype=np.float64, order="C"):
+    """numpy array in page-locked host memory (GCGE_HostAlloc)."""
+    dtype = np.dtype(dtype)
+    shape = (shape,) if np.isscalar(shape) else tuple(shape)
+    count = int(np.prod(shape)) if shape else 1
+    owner = _HostBlock(count * dtype.itemsize)
+    buf = (ctypes.c_char * max(count * dtype.itemsize, 1)).from_address(owner.ptr)
+    buf._gcge_owner = owner  # the array's base is buf: the block lives as long as the array
+    return np.frombuffer(buf, dtype=dtype, count=count).reshape(shape, order=order)
+
+
+def pinned_copy(a, order="C"):
+    """Copy of a numpy array in page-locked host memory."""
+    a = np.asarray(a)
+    out = pinned_empty(a.shape, a.dtype, order=order)
+    out[...] = a
+    return out
+
+
 def solve(A, B, nev, block_size, nev_init, nev_max, X0=None, tol=(1e300, 1e-8), max_iter=500,
-          gap_min=1e-5, auto_shift=1, precision=PREC_FP64, want_evec=True) -> SolveResult:
+          gap_min=1e-5, auto_shift=1, precision=PREC_FP64, want_evec=True, evec_out=None,
+          eval_out=None) -> SolveResult:
     """One GCG solve through GCGE_Solve.  A, B: problems.CSRMatrix (symmetric,
-    so CSR arrays == CCS arrays); B None = identity.  X0 (n x k) seeds the basis."""
+    so CSR arrays == CCS arrays); B None = identity.  X0 (n x k) seeds the basis.
+    evec_out (n x nev_max, column-major) and eval_out (nev_max) may be given to
+    receive the results in caller memory (e.g. pinned_empty buffers)."""
     lib = load()
     n = A.n
     a = _csr_args(A)
     b = _csr_args(B)
     X0 = None if X0 is None else np.asfortranarray(X0, dtype=np.float64)
     ng = 0 if X0 is None else X0.shape[1]
-    ev = np.zeros(nev_max)
-    evec = np.zeros((n, nev_max), order="F") if want_evec else None
+    ev = np.zeros(nev_max) if eval_out is None else eval_out
+    if evec_out is not None:
+        assert evec_out.shape == (n, nev_max) and evec_out.flags.f_contiguous
+        evec = evec_out
+    else:
+        evec = np.zeros((n, nev_max), order="F") if want_evec else None
     info = SolveInfo()
     t = (ctypes.c_double * 2)(*tol)
     st = lib.GCGE_Solve(ctypes.c_int(n), _p(a[0]), _p(a[1]), _p(a[2]), _p(b[0]), _p(b[1]), _p(b[2]),

@@ -909,6 +909,19 @@ int GCGE_Solve(int n, const int *a_colptr, const int *a_rowind, const double *a_
     return st;
 }
 
+void *GCGE_HostAlloc(size_t bytes) {
+    void *p = nullptr;
+    const cudaError_t e = cudaMallocHost(&p, std::max<size_t>(bytes, 1));
+    if (e != cudaSuccess) {
+        set_error(GCGE_ERR_ALLOC, "GCGE_HostAlloc: cudaMallocHost failed");
+        return nullptr;
+    }
+    return p;
+}
+void GCGE_HostFree(void *p) {
+    if (p) cudaFreeHost(p);
+}
+
 static cudaEvent_t g_t0 = nullptr, g_t1 = nullptr;
 int GCGE_TimerStart(void) {
     GCGE_TRY_RET({

@@ -288,13 +288,21 @@ __global__ void __launch_bounds__(oz_threads<BN>(), 2) k_oz_gemm(OzArgs a) {
     }
 }
 
+// Split-k partial sums in a fixed order: eight interleaved running sums per
+// output keep eight loads in flight, then a fixed tree.
 __global__ void k_oz_reduce(const double *__restrict__ part, int chunks, int m, int w,
                             double *__restrict__ C, int ldc) {
     const int total = m * w;
     for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < total; e += gridDim.x * blockDim.x) {
-        double s = 0.0;
-        for (int c = 0; c < chunks; ++c) s += part[(size_t)c * total + e];
-        C[e % m + (size_t)(e / m) * ldc] = s;
+        double s[8] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+        int c = 0;
+        for (; c + 8 <= chunks; c += 8) {
+#pragma unroll
+            for (int q = 0; q < 8; ++q) s[q] += part[(size_t)(c + q) * total + e];
+        }
+        for (int q = 0; c < chunks; ++c, ++q) s[q] += part[(size_t)c * total + e];
+        C[e % m + (size_t)(e / m) * ldc] =
+            ((s[0] + s[1]) + (s[2] + s[3])) + ((s[4] + s[5]) + (s[6] + s[7]));
     }
 }
 
@@ -367,7 +375,7 @@ void oz_gram(int n, int m, int w, const double *Q, int ldq, const double *P, int
     a.out = scratch;
     launch_oz_bn<true>(a, bn, dim3(mt, nt, zz), st);
     const int tot = m * w;
-    k_oz_reduce<<<std::max(1, std::min((tot + 255) / 256, 4 * oz_num_sms())), 256, 0, st>>>(
+    k_oz_reduce<<<std::max(1, std::min((tot + 127) / 128, 8 * oz_num_sms())), 128, 0, st>>>(
         scratch, zz, m, w, C, ldc);
     GCGE_CHECK_LAUNCH();
     count_launch();

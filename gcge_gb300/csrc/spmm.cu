@@ -62,9 +62,12 @@ k_residual(const long long *__restrict__ sp, const int *__restrict__ col,
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     for (int c = threadIdx.x; c < K; c += blockDim.x) slam[c] = c < k ? lam[c] : 0.0;
     __syncthreads();
-    double acc[K];
+    // A x and B x accumulated separately (as the reference's two SpMMs and
+    // axpby, src/ops_eig_sol_gcg.c:220-238), skipping stored zeros of either
+    // value array: on a union pattern most entries belong to one matrix only
+    double acc[K], bcc[K];
 #pragma unroll
-    for (int c = 0; c < K; ++c) acc[c] = 0.0;
+    for (int c = 0; c < K; ++c) acc[c] = bcc[c] = 0.0;
     const int row = slice * 32 + lane;
     if (slice < nslices) {
         const long long beg = sp[slice], end = sp[slice + 1];
@@ -72,14 +75,31 @@ k_residual(const long long *__restrict__ sp, const int *__restrict__ col,
             const int j = __ldg(col + e);
             const double av = __ldg(a + e), bv = __ldg(b + e);
             const double *xj = X + j;
+            if (av != 0.0) {
+                if (bv != 0.0) {
 #pragma unroll
-            for (int c = 0; c < K; ++c)
-                if (c < k) acc[c] = fma(fma(-slam[c], bv, av), __ldg(xj + (size_t)c * ldx), acc[c]);
+                    for (int c = 0; c < K; ++c)
+                        if (c < k) {
+                            const double x = __ldg(xj + (size_t)c * ldx);
+                            acc[c] = fma(av, x, acc[c]);
+                            bcc[c] = fma(bv, x, bcc[c]);
+                        }
+                } else {
+#pragma unroll
+                    for (int c = 0; c < K; ++c)
+                        if (c < k) acc[c] = fma(av, __ldg(xj + (size_t)c * ldx), acc[c]);
+                }
+            } else if (bv != 0.0) {
+#pragma unroll
+                for (int c = 0; c < K; ++c)
+                    if (c < k) bcc[c] = fma(bv, __ldg(xj + (size_t)c * ldx), bcc[c]);
+            }
         }
     }
 #pragma unroll
     for (int c = 0; c < K; ++c) {
-        double v = (row < n && c < k) ? acc[c] * acc[c] : 0.0;
+        const double r = fma(-slam[c], bcc[c], acc[c]);
+        double v = (row < n && c < k) ? r * r : 0.0;
         for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
         if (lane == 0) red[warp][c] = v;
     }

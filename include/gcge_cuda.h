@@ -116,6 +116,12 @@ int GCGE_Solve(int n, const int *a_colptr, const int *a_rowind, const double *a_
                double gap_min, int auto_shift, int precision, const double *X0, int nev_given,
                double *eval, double *evec, gcge_solve_info *info);
 
+/* Page-locked host memory for GCGE_Solve's inputs and outputs (the CCS
+ * arrays, X0, eval, evec): copies from and to it run as DMA at link speed,
+ * while pageable buffers are staged by the driver.  NULL on failure. */
+void *GCGE_HostAlloc(size_t bytes);
+void GCGE_HostFree(void *p);
+
 /* Statistics of the last ops->EigenSolver call on this ops. */
 int GCGE_GetSolveInfo(struct OPS_ *ops, gcge_solve_info *info);
 
