@@ -38,6 +38,7 @@ constexpr int kDigitBits = 7;
 constexpr int kBK = 64;
 constexpr int kBKP = kBK + 8;
 constexpr int kBM = 64;
+constexpr int kSuper = 8;  // chunks per shared exponent (int64 sums stay below 2^51)
 
 template <int BN>
 struct __align__(16) OzSmem {
@@ -101,9 +102,43 @@ __device__ __forceinline__ void mma_bf16(float (&d)[4], const uint32_t (&a)[4],
         : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
 }
 
+// Exponent fields (max over [k0, kend), at least 1) of R rows of a
+// k-contiguous operand: one warp per row.
+template <int R>
+__device__ __forceinline__ void exps_kcontig(const double *__restrict__ p, size_t ld, int r0,
+                                             int nrows, int k0, int kend, int *e, int warp,
+                                             int nwarps, int lane) {
+    for (int r = warp; r < R; r += nwarps) {
+        const int gr = r0 + r;
+        int em = 1;
+        if (gr < nrows) {
+            const double *q = p + (size_t)gr * ld;
+            for (int k = k0 + lane; k < kend; k += 32) em = max(em, exp_field(q[k]));
+        }
+        em = (int)__reduce_max_sync(0xffffffffu, (unsigned)em);
+        if (lane == 0) e[r] = em;
+    }
+}
+
+// The same for the kBM rows of an m-contiguous operand: NT / kBM threads per
+// row (consecutive threads read consecutive rows), shared-memory maximum.
+// e[] must hold 1 for every row beforehand.
+template <int NT>
+__device__ __forceinline__ void exps_mcontig(const double *__restrict__ p, size_t ld, int m0,
+                                             int nrows, int k0, int kend, int *e, int tid) {
+    constexpr int groups = NT / kBM;
+    const int r = tid % kBM, g0 = tid / kBM;
+    const int gr = m0 + r;
+    int em = 1;
+    if (gr < nrows && g0 < groups)
+        for (int k = k0 + g0; k < kend; k += groups) em = max(em, exp_field(p[gr + (size_t)k * ld]));
+    atomicMax(&e[r], em);
+}
+
 // Digit planes of R rows of a k-contiguous operand (element (r, k) at
-// p[k + r * ld]) for the chunk [k0, k0 + kBK) clipped to kend; rows at or past
-// nrows are zero.  One warp per row, lane l takes k = k0 + 2l, k0 + 2l + 1.
+// p[k + r * ld]) for the chunk [k0, k0 + kBK) clipped to kend, relative to the
+// exponent fields e[r]; rows at or past nrows are zero.  One warp per row,
+// lane l takes k = k0 + 2l, k0 + 2l + 1.
 template <int R>
 __device__ __forceinline__ void planes_kcontig(const double *__restrict__ p, size_t ld, int r0,
                                                int nrows, int k0, int kend,
@@ -118,8 +153,7 @@ __device__ __forceinline__ void planes_kcontig(const double *__restrict__ p, siz
             if (k < kend) v0 = q[k];
             if (k + 1 < kend) v1 = q[k + 1];
         }
-        const int em =
-            (int)__reduce_max_sync(0xffffffffu, (unsigned)max(exp_field(v0), exp_field(v1)));
+        const int em = e[r];
         uint16_t d0[kDigits], d1[kDigits];
         split_digits(v0, em, d0);
         split_digits(v1, em, d1);
@@ -127,34 +161,18 @@ __device__ __forceinline__ void planes_kcontig(const double *__restrict__ p, siz
         for (int i = 0; i < kDigits; ++i)
             *reinterpret_cast<uint32_t *>(&planes[i][r][2 * lane]) =
                 (uint32_t)d0[i] | ((uint32_t)d1[i] << 16);
-        if (lane == 0) e[r] = em;
     }
 }
 
 // Digit planes of kBM rows of an m-contiguous operand (element (m, k) at
-// p[m + k * ld]); a work item is one row and 8 consecutive k.  Two passes: the
-// chunk exponent of each row (shared-memory max), then the digits.
+// p[m + k * ld]) relative to the exponent fields e[r]; a work item is one row
+// and 8 consecutive k.
 template <int NT>
 __device__ __forceinline__ void planes_mcontig(const double *__restrict__ p, size_t ld, int m0,
                                                int nrows, int k0, int kend,
-                                               uint16_t (*planes)[kBM][kBKP], int *e, int tid) {
-    for (int r = tid; r < kBM; r += NT) e[r] = 1;
-    __syncthreads();
+                                               uint16_t (*planes)[kBM][kBKP], const int *e,
+                                               int tid) {
     constexpr int items = kBM * (kBK / 8);
-    for (int it = tid; it < items; it += NT) {
-        const int r = it % kBM, k8 = it / kBM;
-        const int gr = m0 + r;
-        int em = 1;
-        if (gr < nrows) {
-#pragma unroll
-            for (int q = 0; q < 8; ++q) {
-                const int k = k0 + k8 * 8 + q;
-                if (k < kend) em = max(em, exp_field(p[gr + (size_t)k * ld]));
-            }
-        }
-        atomicMax(&e[r], em);
-    }
-    __syncthreads();
     for (int it = tid; it < items; it += NT) {
         const int r = it % kBM, k8 = it / kBM;
         const int gr = m0 + r;
@@ -212,56 +230,76 @@ __global__ void __launch_bounds__(oz_threads<BN>(), 2) k_oz_gemm(OzArgs a) {
     const int m0 = wm * 16, n0 = wn * 8;
     const int g = lane >> 2, t4 = lane & 3;
 
-    double acc[4] = {0.0, 0.0, 0.0, 0.0};
-    bool bad[4] = {false, false, false, false};
+    double acc[4] = {0.0, 0.0, 0.0, 0.0};  // NaN once a non-finite input was seen
 
-    for (int k0 = kb; k0 < ke; k0 += kBK) {
-        if constexpr (GRAM)
-            planes_kcontig<kBM>(a.A, a.lda, mt0, a.M, k0, ke, sm.a, sm.ea, warp, nwarps, lane);
-        else
-            planes_mcontig<NT>(a.A, a.lda, mt0, a.M, k0, ke, sm.a, sm.ea, tid);
-        planes_kcontig<BN>(a.B, a.ldb, nt0, a.N, k0, ke, sm.b, sm.eb, warp, nwarps, lane);
-        __syncthreads();
-
-        float lv[kDigits][4];
-#pragma unroll
-        for (int l = 0; l < kDigits; ++l) lv[l][0] = lv[l][1] = lv[l][2] = lv[l][3] = 0.f;
-#pragma unroll
-        for (int ks = 0; ks < kBK / 16; ++ks) {
-            uint32_t bf[kDigits][2];
-#pragma unroll
-            for (int j = 0; j < kDigits; ++j)
-                ldsm_x2(bf[j], &sm.b[j][n0 + (lane & 7)][ks * 16 + ((lane >> 3) & 1) * 8]);
-#pragma unroll
-            for (int i = 0; i < kDigits; ++i) {
-                uint32_t af[4];
-                ldsm_x4(af, &sm.a[i][m0 + (lane & 15)][ks * 16 + (lane >> 4) * 8]);
-#pragma unroll
-                for (int j = 0; j < kDigits - i; ++j) mma_bf16(lv[i + j], af, bf[j]);
-            }
+    // super-chunks of kSuper chunks share one exponent per row and column, so
+    // the exact level sums of their chunks add up in int64 and are folded into
+    // FP64 once per super-chunk
+    for (int sk = kb; sk < ke; sk += kSuper * kBK) {
+        const int ske = min(ke, sk + kSuper * kBK);
+        if constexpr (GRAM) {
+            exps_kcontig<kBM>(a.A, a.lda, mt0, a.M, sk, ske, sm.ea, warp, nwarps, lane);
+        } else {
+            for (int r = tid; r < kBM; r += NT) sm.ea[r] = 1;
+            __syncthreads();
+            exps_mcontig<NT>(a.A, a.lda, mt0, a.M, sk, ske, sm.ea, tid);
         }
-        // fold the exact level sums into the FP64 accumulators
+        exps_kcontig<BN>(a.B, a.ldb, nt0, a.N, sk, ske, sm.eb, warp, nwarps, lane);
+        __syncthreads();
+        long long thi[4] = {0, 0, 0, 0}, tlo[4] = {0, 0, 0, 0};
+        for (int k0 = sk; k0 < ske; k0 += kBK) {
+            if constexpr (GRAM)
+                planes_kcontig<kBM>(a.A, a.lda, mt0, a.M, k0, ske, sm.a, sm.ea, warp, nwarps, lane);
+            else
+                planes_mcontig<NT>(a.A, a.lda, mt0, a.M, k0, ske, sm.a, sm.ea, tid);
+            planes_kcontig<BN>(a.B, a.ldb, nt0, a.N, k0, ske, sm.b, sm.eb, warp, nwarps, lane);
+            __syncthreads();
+
+            float lv[kDigits][4];
+#pragma unroll
+            for (int l = 0; l < kDigits; ++l) lv[l][0] = lv[l][1] = lv[l][2] = lv[l][3] = 0.f;
+#pragma unroll
+            for (int ks = 0; ks < kBK / 16; ++ks) {
+                uint32_t bf[kDigits][2];
+#pragma unroll
+                for (int j = 0; j < kDigits; ++j)
+                    ldsm_x2(bf[j], &sm.b[j][n0 + (lane & 7)][ks * 16 + ((lane >> 3) & 1) * 8]);
+#pragma unroll
+                for (int i = 0; i < kDigits; ++i) {
+                    uint32_t af[4];
+                    ldsm_x4(af, &sm.a[i][m0 + (lane & 15)][ks * 16 + (lane >> 4) * 8]);
+#pragma unroll
+                    for (int j = 0; j < kDigits - i; ++j) mma_bf16(lv[i + j], af, bf[j]);
+                }
+            }
+            // the exact level sums as two int64 words (|hi| < 2^42.1, |lo| < 2^44.3
+            // per chunk)
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                int L[kDigits];
+#pragma unroll
+                for (int l = 0; l < kDigits; ++l) L[l] = __float2int_rn(lv[l][q]);
+                thi[q] += ((long long)L[0] << 21) + ((long long)L[1] << 14) +
+                          ((long long)L[2] << 7) + (long long)L[3];
+                tlo[q] += ((long long)L[4] << 21) + ((long long)L[5] << 14) +
+                          ((long long)L[6] << 7) + (long long)L[7];
+            }
+            __syncthreads();
+        }
+        // fold into the FP64 accumulators: value = 2^(ea-1022 + eb-1022 - 63) (hi 2^28 + lo)
 #pragma unroll
         for (int q = 0; q < 4; ++q) {
             const int rl = m0 + g + ((q >> 1) << 3);
             const int cl = n0 + 2 * t4 + (q & 1);
-            int L[kDigits];
-#pragma unroll
-            for (int l = 0; l < kDigits; ++l) L[l] = __float2int_rn(lv[l][q]);
-            const long long thi = ((long long)L[0] << 21) + ((long long)L[1] << 14) +
-                                  ((long long)L[2] << 7) + (long long)L[3];
-            const long long tlo = ((long long)L[4] << 21) + ((long long)L[5] << 14) +
-                                  ((long long)L[6] << 7) + (long long)L[7];
             const int ea = sm.ea[rl], eb = sm.eb[cl];
             if (ea == 0x7FF || eb == 0x7FF) {
-                bad[q] = true;
+                acc[q] = __longlong_as_double(0x7FF8000000000000LL);
             } else {
-                // scale 2^(ea - 1022 + eb - 1022 - 63): exponent field ea + eb - 1084
-                const int fld = ea + eb - 1084;
+                const int fld = ea + eb - 1084;  // exponent field of the scale
                 if (fld > 0) {
                     const double s = fld >= 2047 ? __longlong_as_double(0x7FF0000000000000LL)
                                                  : __longlong_as_double((long long)fld << 52);
-                    const double v = fma(i64_to_f64(thi), 268435456.0, i64_to_f64(tlo));
+                    const double v = fma(i64_to_f64(thi[q]), 268435456.0, i64_to_f64(tlo[q]));
                     acc[q] = fma(v, s, acc[q]);
                 }
             }
@@ -274,7 +312,7 @@ __global__ void __launch_bounds__(oz_threads<BN>(), 2) k_oz_gemm(OzArgs a) {
         const int row = mt0 + m0 + g + ((q >> 1) << 3);
         const int col = nt0 + n0 + 2 * t4 + (q & 1);
         if (row >= a.M || col >= a.N) continue;
-        const double v = bad[q] ? __longlong_as_double(0x7FF8000000000000LL) : acc[q];
+        const double v = acc[q];
         if constexpr (GRAM) {
             a.out[(size_t)blockIdx.z * a.M * a.N + row + (size_t)col * a.M] = v;
         } else {
@@ -288,21 +326,31 @@ __global__ void __launch_bounds__(oz_threads<BN>(), 2) k_oz_gemm(OzArgs a) {
     }
 }
 
-// Split-k partial sums in a fixed order: eight interleaved running sums per
-// output keep eight loads in flight, then a fixed tree.
-__global__ void k_oz_reduce(const double *__restrict__ part, int chunks, int m, int w,
-                            double *__restrict__ C, int ldc) {
+// Split-k partial sums in a fixed order: block b sums outputs
+// [32 b, 32 b + 32); thread (o, g) adds chunks g, g + 8, ... of output o
+// (consecutive o read consecutive addresses), then the 8 groups are added in
+// a fixed tree.
+__global__ void __launch_bounds__(256) k_oz_reduce(const double *__restrict__ part, int chunks,
+                                                   int m, int w, double *__restrict__ C, int ldc) {
+    __shared__ double red[8][33];
     const int total = m * w;
-    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < total; e += gridDim.x * blockDim.x) {
-        double s[8] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
-        int c = 0;
-        for (; c + 8 <= chunks; c += 8) {
-#pragma unroll
-            for (int q = 0; q < 8; ++q) s[q] += part[(size_t)(c + q) * total + e];
+    const int o = threadIdx.x & 31, grp = threadIdx.x >> 5;
+    const int e = blockIdx.x * 32 + o;
+    double s0 = 0.0, s1 = 0.0;
+    if (e < total) {
+        int c = grp;
+        for (; c + 8 < chunks; c += 16) {
+            s0 += part[(size_t)c * total + e];
+            s1 += part[(size_t)(c + 8) * total + e];
         }
-        for (int q = 0; c < chunks; ++c, ++q) s[q] += part[(size_t)c * total + e];
-        C[e % m + (size_t)(e / m) * ldc] =
-            ((s[0] + s[1]) + (s[2] + s[3])) + ((s[4] + s[5]) + (s[6] + s[7]));
+        if (c < chunks) s0 += part[(size_t)c * total + e];
+    }
+    red[grp][o] = s0 + s1;
+    __syncthreads();
+    if (grp == 0 && e < total) {
+        const double v = ((red[0][o] + red[1][o]) + (red[2][o] + red[3][o])) +
+                         ((red[4][o] + red[5][o]) + (red[6][o] + red[7][o]));
+        C[e % m + (size_t)(e / m) * ldc] = v;
     }
 }
 
@@ -356,8 +404,8 @@ void oz_gram(int n, int m, int w, const double *Q, int ldq, const double *P, int
     const int bn = oz_tile_n(w);
     const int mt = (m + kBM - 1) / kBM, nt = (w + bn - 1) / bn;
     const int chunks = (n + kBK - 1) / kBK;
-    // about four CTAs per SM over the whole grid, at least two chunks each
-    long long z = std::max(1, (4 * oz_num_sms() + mt * nt - 1) / (mt * nt));
+    // one wave of two CTAs per SM over the whole grid, at least two chunks each
+    long long z = std::max(1, (2 * oz_num_sms() + mt * nt - 1) / (mt * nt));
     z = std::min<long long>(z, std::max(1, chunks / 2));
     z = std::min<long long>(z, (long long)(scratch_elems / ((size_t)m * w)));
     GCGE_REQUIRE(z >= 1, GCGE_ERR_ARG, "oz_gram: scratch too small");
@@ -375,8 +423,7 @@ void oz_gram(int n, int m, int w, const double *Q, int ldq, const double *P, int
     a.out = scratch;
     launch_oz_bn<true>(a, bn, dim3(mt, nt, zz), st);
     const int tot = m * w;
-    k_oz_reduce<<<std::max(1, std::min((tot + 127) / 128, 8 * oz_num_sms())), 128, 0, st>>>(
-        scratch, zz, m, w, C, ldc);
+    k_oz_reduce<<<(tot + 31) / 32, 256, 0, st>>>(scratch, zz, m, w, C, ldc);
     GCGE_CHECK_LAUNCH();
     count_launch();
 }
