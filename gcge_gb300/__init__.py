@@ -41,7 +41,8 @@ EXPORTED_SYMBOLS = [
     "GCGE_SetPrecision", "GCGE_Solve", "GCGE_GetSolveInfo", "GCGE_Prepare", "GCGE_PreparedSolve",
     "GCGE_PreparedDestroy", "GCGE_BenchSpMM", "GCGE_DenseEig", "GCGE_BlockPCG", "GCGE_BOrth",
     "GCGE_TimerStart", "GCGE_TimerStop", "GCGE_GramNoAlloc", "GCGE_DenseGram",
-    "GCGE_DenseLinComb", "GCGE_HostAlloc", "GCGE_HostFree",
+    "GCGE_DenseLinComb", "GCGE_HostAlloc", "GCGE_HostFree", "GCGE_ServerCreate",
+    "GCGE_ServerSubmit", "GCGE_ServerWait", "GCGE_ServerDestroy", "GCGE_SolveBatch",
 ]
 
 _lib = None
@@ -113,6 +114,14 @@ def load(build_if_missing: bool = False) -> ctypes.CDLL:
     lib.GCGE_HostAlloc.restype = ctypes.c_void_p
     lib.GCGE_HostAlloc.argtypes = [ctypes.c_size_t]
     lib.GCGE_HostFree.argtypes = [ctypes.c_void_p]
+    lib.GCGE_ServerCreate.restype = ctypes.c_void_p
+    lib.GCGE_ServerCreate.argtypes = [ctypes.c_int, ctypes.c_size_t]
+    lib.GCGE_ServerSubmit.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
+    lib.GCGE_ServerWait.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
+    lib.GCGE_ServerDestroy.argtypes = [ctypes.c_void_p]
+    lib.GCGE_SolveBatch.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_size_t]
+    for name in ("GCGE_ServerSubmit", "GCGE_ServerWait", "GCGE_SolveBatch"):
+        getattr(lib, name).restype = ctypes.c_int
     _lib = lib
     return lib
 
@@ -247,6 +256,102 @@ class Prepared:
             self.close()
         except Exception:
             pass
+
+
+# ---------------------------------------------------------------------------
+# Many solves on one GPU: batched problems and the serving loop (serve.cu)
+# ---------------------------------------------------------------------------
+class Request(ctypes.Structure):
+    _fields_ = [("n", ctypes.c_int), ("a_colptr", ctypes.c_void_p), ("a_rowind", ctypes.c_void_p),
+                ("a_val", ctypes.c_void_p), ("b_colptr", ctypes.c_void_p),
+                ("b_rowind", ctypes.c_void_p), ("b_val", ctypes.c_void_p), ("nev", ctypes.c_int),
+                ("block_size", ctypes.c_int), ("nev_init", ctypes.c_int), ("nev_max", ctypes.c_int),
+                ("max_iter", ctypes.c_int), ("tol", ctypes.c_double * 2), ("gap_min", ctypes.c_double),
+                ("auto_shift", ctypes.c_int), ("precision", ctypes.c_int), ("X0", ctypes.c_void_p),
+                ("nev_given", ctypes.c_int), ("eval", ctypes.c_void_p), ("evec", ctypes.c_void_p),
+                ("info", SolveInfo), ("status", ctypes.c_int), ("done", ctypes.c_int),
+                ("t_submit", ctypes.c_double), ("t_start", ctypes.c_double),
+                ("t_end", ctypes.c_double)]
+
+
+class Job:
+    """One solve for the server: the request and the arrays it points to."""
+
+    def __init__(self, A, B, nev, block_size, nev_init, nev_max, X0=None, tol=(1e300, 1e-8),
+                 max_iter=500, gap_min=1e-5, auto_shift=1, precision=PREC_MIXED, want_evec=False):
+        self.arrays = [_csr_args(A), _csr_args(B)]
+        a, b = self.arrays
+        self.X0 = None if X0 is None else np.asfortranarray(X0, dtype=np.float64)
+        self.eval = np.zeros(nev_max)
+        self.evec = np.zeros((A.n, nev_max), order="F") if want_evec else None
+        r = Request()
+        r.n = A.n
+        r.a_colptr, r.a_rowind, r.a_val = (x.ctypes.data for x in a)
+        if B is not None:
+            r.b_colptr, r.b_rowind, r.b_val = (x.ctypes.data for x in b)
+        r.nev, r.block_size, r.nev_init, r.nev_max, r.max_iter = nev, block_size, nev_init, nev_max, max_iter
+        r.tol[0], r.tol[1] = tol
+        r.gap_min, r.auto_shift, r.precision = gap_min, auto_shift, precision
+        if self.X0 is not None:
+            r.X0, r.nev_given = self.X0.ctypes.data, self.X0.shape[1]
+        r.eval = self.eval.ctypes.data
+        r.evec = None if self.evec is None else self.evec.ctypes.data
+        self.req = r
+
+    @property
+    def result(self) -> SolveResult:
+        r = self.req
+        return SolveResult(self.eval, self.evec, r.info.nconv, r.info.niter, r.status,
+                           r.info.as_dict())
+
+    @property
+    def latency(self) -> float:
+        return self.req.t_end - self.req.t_submit
+
+
+class Server:
+    """Serving loop: requests submitted at any time run on `workers` host
+    threads (one CUDA stream each), admitted by device-memory footprint."""
+
+    def __init__(self, workers=4, budget_bytes=0):
+        self.lib = load()
+        self.h = self.lib.GCGE_ServerCreate(workers, budget_bytes)
+        if not self.h:
+            raise GCGEError(self.lib.ops_cuda_last_error(), "GCGE_ServerCreate")
+
+    def submit(self, job: Job):
+        st = self.lib.GCGE_ServerSubmit(self.h, ctypes.byref(job.req))
+        if st != GCGE_OK:
+            raise GCGEError(st, "GCGE_ServerSubmit")
+        return job
+
+    def wait(self, job: Job) -> SolveResult:
+        self.lib.GCGE_ServerWait(self.h, ctypes.byref(job.req))
+        return job.result
+
+    def close(self):
+        if self.h:
+            hp = ctypes.c_void_p(self.h)
+            self.lib.GCGE_ServerDestroy(ctypes.byref(hp))
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+
+def solve_batch(jobs, workers=4, budget_bytes=0):
+    """Solve a list of Jobs through GCGE_SolveBatch; returns their results."""
+    lib = load()
+    arr = (Request * len(jobs))()
+    for i, j in enumerate(jobs):
+        arr[i] = j.req
+    lib.GCGE_SolveBatch(arr, len(jobs), workers, budget_bytes)
+    for i, j in enumerate(jobs):
+        j.req = arr[i]
+    return [j.result for j in jobs]
 
 
 # ---------------------------------------------------------------------------

@@ -18,7 +18,8 @@
 
 namespace gcge {
 
-unsigned long long g_kernel_launches = 0;
+thread_local unsigned long long t_kernel_launches = 0;
+thread_local int t_pcg_share = 0;
 static thread_local int t_last_error = GCGE_OK;
 static thread_local std::string t_last_where;
 static std::mutex g_detail_mu;
@@ -56,16 +57,51 @@ const char *status_string(int s) {
     }
 }
 
-static std::once_flag g_stream_once;
-static cudaStream_t g_stream = nullptr;
-cudaStream_t lib_stream() {
-    std::call_once(g_stream_once, [] {
+namespace {
+struct ThreadStream {
+    cudaStream_t s = nullptr;
+    ~ThreadStream() {
+        if (s) {
+            cudaStreamSynchronize(s);
+            cudaStreamDestroy(s);
+        }
+    }
+};
+thread_local ThreadStream t_stream;
+std::once_flag g_device_once;
+bool g_have_device = false;
+int g_sms = 0;
+
+void device_init() {
+    std::call_once(g_device_once, [] {
         int ndev = 0;
         if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return;
-        cudaStreamCreateWithFlags(&g_stream, cudaStreamNonBlocking);
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&g_sms, cudaDevAttrMultiProcessorCount, dev);
+        if (g_sms <= 0) g_sms = 148;
+        // keep freed pool blocks cached for reuse instead of returning them
+        cudaMemPool_t pool;
+        if (cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
+            unsigned long long keep = ~0ULL;
+            cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+        }
+        g_have_device = true;
     });
-    if (g_stream == nullptr) throw CudaError{GCGE_ERR_NO_DEVICE, "no CUDA device visible"};
-    return g_stream;
+    if (!g_have_device) throw CudaError{GCGE_ERR_NO_DEVICE, "no CUDA device visible"};
+}
+}  // namespace
+
+cudaStream_t lib_stream() {
+    if (t_stream.s == nullptr) {
+        device_init();
+        GCGE_CUDA(cudaStreamCreateWithFlags(&t_stream.s, cudaStreamNonBlocking));
+    }
+    return t_stream.s;
+}
+int device_sms() {
+    device_init();
+    return g_sms;
 }
 
 MultiVec *as_mv(void *h) {
@@ -84,7 +120,7 @@ static MultiVec *mv_create(int nrows, int ncols) {
     m->ncols = ncols;
     m->ld = std::max(32, (nrows + 31) / 32 * 32);
     const size_t bytes = sizeof(double) * (size_t)m->ld * std::max(ncols, 1);
-    cudaError_t e = cudaMalloc((void **)&m->data, bytes);
+    cudaError_t e = cudaMallocAsync((void **)&m->data, bytes, lib_stream());
     if (e != cudaSuccess) {
         delete m;
         throw CudaError{GCGE_ERR_ALLOC, std::string("multivector: ") + cudaGetErrorString(e)};
@@ -94,7 +130,15 @@ static MultiVec *mv_create(int nrows, int ncols) {
 }
 static void mv_destroy(MultiVec *m) {
     if (!m) return;
-    if (m->owns && m->data) cudaFree(m->data);
+    if (m->owns && m->data) {
+        cudaStream_t st = nullptr;
+        try {
+            st = lib_stream();
+        } catch (...) {
+        }
+        if (st) cudaFreeAsync(m->data, st);
+        else cudaFree(m->data);
+    }
     m->magic = 0;
     delete m;
 }
@@ -922,7 +966,7 @@ void GCGE_HostFree(void *p) {
     if (p) cudaFreeHost(p);
 }
 
-static cudaEvent_t g_t0 = nullptr, g_t1 = nullptr;
+static thread_local cudaEvent_t g_t0 = nullptr, g_t1 = nullptr;
 int GCGE_TimerStart(void) {
     GCGE_TRY_RET({
         if (!g_t0) {

@@ -39,12 +39,26 @@ struct CudaError {
         if (!(cond)) throw ::gcge::CudaError{(status), std::string(msg)};            \
     } while (0)
 
-// Count of kernels launched by the library (per process); the solver reports
-// the difference over a solve.
-extern unsigned long long g_kernel_launches;
-inline void count_launch(int k = 1) { g_kernel_launches += (unsigned long long)k; }
+// Count of kernels launched by the library from the calling thread; the
+// solver reports the difference over a solve (a solve runs on one thread).
+extern thread_local unsigned long long t_kernel_launches;
+inline void count_launch(int k = 1) { t_kernel_launches += (unsigned long long)k; }
+
+// The calling thread's stream (created on first use, destroyed at thread
+// exit): every kernel and copy of a solve runs on it, so solves driven from
+// different host threads overlap on the device.
+cudaStream_t lib_stream();
+// Streaming multiprocessors of the current device (queried once).
+int device_sms();
+// Number of solves sharing the device with the calling thread's solves (0 or
+// 1: the whole device); the persistent block-PCG kernel then takes that share
+// of the co-resident grid, so the cooperative kernels of concurrent solves
+// always fit on the device together.  Set by the batch/serving workers.
+extern thread_local int t_pcg_share;
 
 // ---------------------------------------------------------------- buffers
+// Device buffers come from the stream-ordered pool allocator on the calling
+// thread's stream (no device-wide synchronisation, freed blocks reused).
 template <typename T>
 struct DevBuf {
     T *p = nullptr;
@@ -54,7 +68,15 @@ struct DevBuf {
     DevBuf &operator=(const DevBuf &) = delete;
     ~DevBuf() { release(); }
     void release() {
-        if (p) cudaFree(p);
+        if (p) {
+            cudaStream_t st = nullptr;
+            try {
+                st = lib_stream();
+            } catch (...) {
+            }
+            if (st) cudaFreeAsync(p, st);
+            else cudaFree(p);
+        }
         p = nullptr;
         n = 0;
     }
@@ -62,10 +84,10 @@ struct DevBuf {
         if (count <= n && p) return;
         release();
         if (count == 0) return;
-        cudaError_t e = cudaMalloc((void **)&p, count * sizeof(T));
+        cudaError_t e = cudaMallocAsync((void **)&p, count * sizeof(T), lib_stream());
         if (e != cudaSuccess) {
             p = nullptr;
-            throw CudaError{GCGE_ERR_ALLOC, std::string("cudaMalloc: ") + cudaGetErrorString(e)};
+            throw CudaError{GCGE_ERR_ALLOC, std::string("cudaMallocAsync: ") + cudaGetErrorString(e)};
         }
         n = count;
     }
@@ -214,8 +236,5 @@ void transpose_copy(int m, int k, const double *X, int ldx, double *Y, int ldy, 
 void shift_values(size_t count, const double *a, const double *b, double sigma, double *y64,
                   float *y32, cudaStream_t st);
 void copy_cols(int n, int k, const double *X, int ldx, double *Y, int ldy, cudaStream_t st);
-// Stream shared by every library call (created on first use).
-cudaStream_t lib_stream();
-
 
 }  // namespace gcge

@@ -18,6 +18,7 @@
 //      exactly on the host (tiny FP64 Jacobi) and sorts ascending.
 // The 2x2 rotation is the symmetric Schur decomposition of Golub & Van Loan
 // (Matrix Computations, Alg. 8.4.1).
+#include <mutex>
 #include <algorithm>
 #include <cmath>
 #include <numeric>
@@ -196,15 +197,16 @@ k_jacobi32(int s, const double *__restrict__ M, int ldm, float2 *__restrict__ lo
 // Largest dynamic shared memory the Jacobi kernel may request: the device's
 // opt-in per-block limit minus the kernel's static shared memory.
 static size_t jacobi_dyn_limit() {
+    static std::once_flag once;
     static size_t lim = 0;
-    if (lim == 0) {
+    std::call_once(once, [] {
         int dev = 0, optin = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
         cudaFuncAttributes fa{};
         cudaFuncGetAttributes(&fa, k_jacobi32);
         lim = optin > 0 ? (size_t)optin - fa.sharedSizeBytes : 48 * 1024;
-    }
+    });
     return lim;
 }
 
@@ -323,12 +325,11 @@ int sym_eig(EigWork &wk, int s, const double *M, int ld, double *eval_host, doub
     GCGE_REQUIRE(s <= jacobi_max_dim(), GCGE_ERR_TOO_LARGE,
                  "sym_eig: projected dimension exceeds the shared-memory Jacobi capacity");
     const size_t smem = jacobi_smem_bytes(s);
-    static size_t attr_set = 0;
-    if (smem > 48 * 1024 && smem > attr_set) {
+    static std::once_flag once;  // allow the largest size once, for every caller thread
+    std::call_once(once, [] {
         GCGE_CUDA(cudaFuncSetAttribute(k_jacobi32, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       (int)smem));
-        attr_set = smem;
-    }
+                                       (int)jacobi_dyn_limit()));
+    });
     k_jacobi32<<<1, kJacobiThreads, smem, st>>>(s, M, ld, wk.log.p, wk.max_rounds, wk.info.p);
     GCGE_CHECK_LAUNCH();
     const int rows_blocks = (s + 7) / 8;

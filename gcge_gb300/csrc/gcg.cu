@@ -685,7 +685,7 @@ void gcg_eigensolver(void *Ah, void *Bh, double *eval, void **evec, int nevGiven
         return;
     }
     const auto t0 = std::chrono::steady_clock::now();
-    const unsigned long long l0 = g_kernel_launches;
+    const unsigned long long l0 = t_kernel_launches;
     try {
         SparseMat *A = as_mat(Ah);
         SparseMat *B = Bh ? as_mat(Bh) : nullptr;
@@ -735,7 +735,7 @@ void gcg_eigensolver(void *Ah, void *Bh, double *eval, void **evec, int nevGiven
         c->info.status = e.status;
         c->last_status = e.status;
     }
-    c->info.kernel_launches = (int)(g_kernel_launches - l0);
+    c->info.kernel_launches = (int)(t_kernel_launches - l0);
     c->info.seconds =
         std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
     if (c->pub.printtime) {

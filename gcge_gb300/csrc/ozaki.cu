@@ -27,6 +27,7 @@
 // (partials summed in a fixed order); linear combinations tile the long row
 // dimension and keep k whole.
 #include <cstdint>
+#include <mutex>
 
 #include "common.cuh"
 
@@ -354,26 +355,16 @@ __global__ void __launch_bounds__(256) k_oz_reduce(const double *__restrict__ pa
     }
 }
 
-int oz_num_sms() {
-    static int sms = 0;
-    if (!sms) {
-        int dev = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        if (sms <= 0) sms = 148;
-    }
-    return sms;
-}
+int oz_num_sms() { return device_sms(); }
 
 template <int BN, bool GRAM>
 void launch_oz(const OzArgs &a, dim3 grid, cudaStream_t st) {
-    static bool attr = false;
+    static std::once_flag once;
     const int smem = (int)sizeof(OzSmem<BN>);
-    if (!attr) {
+    std::call_once(once, [smem] {
         GCGE_CUDA(cudaFuncSetAttribute(k_oz_gemm<BN, GRAM>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
-        attr = true;
-    }
+    });
     k_oz_gemm<BN, GRAM><<<grid, oz_threads<BN>(), smem, st>>>(a);
     GCGE_CHECK_LAUNCH();
     count_launch();

@@ -31,6 +31,7 @@
 // Every barrier wait is bounded (time and poll count); a wait that runs out
 // sets an error flag that makes all blocks return, and the host reports it.
 #include <algorithm>
+#include <mutex>
 
 #include "common.cuh"
 #include "pcg.cuh"
@@ -635,29 +636,23 @@ k_block_pcg(PcgArgs<T> a) {
     finish(true);
 }
 
-int num_sms_pcg() {
-    static int sms = 0;
-    if (!sms) {
-        int dev = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        if (sms <= 0) sms = 148;
-    }
-    return sms;
-}
+int num_sms_pcg() { return device_sms(); }
 
 constexpr int kMaxBlocksPerSm = 4;
 
 template <typename T, int KP>
 void launch_block_pcg(PcgArgs<T> a, cudaStream_t st) {
+    static std::once_flag once;
     static int bpsm = 0;
-    if (bpsm == 0) {
-        GCGE_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bpsm, k_block_pcg<T, KP>,
+    std::call_once(once, [] {
+        int b = 0;
+        GCGE_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_block_pcg<T, KP>,
                                                                 pcg_threads<T, KP>(), 0));
-        GCGE_REQUIRE(bpsm >= 1, GCGE_ERR_CUDA, "block PCG: kernel does not fit on an SM");
-        bpsm = std::min(bpsm, kMaxBlocksPerSm);
-    }
-    const int nb = std::max(1, std::min(bpsm * num_sms_pcg(), a.nslices));
+        bpsm = std::min(b, kMaxBlocksPerSm);
+    });
+    GCGE_REQUIRE(bpsm >= 1, GCGE_ERR_CUDA, "block PCG: kernel does not fit on an SM");
+    int nb = std::max(1, std::min(bpsm * num_sms_pcg(), a.nslices));
+    if (t_pcg_share > 1) nb = std::min(nb, std::max(1, bpsm * num_sms_pcg() / t_pcg_share));
     void *args[] = {&a};
     GCGE_CUDA(cudaLaunchCooperativeKernel((const void *)k_block_pcg<T, KP>, dim3(nb),
                                           dim3(pcg_threads<T, KP>()), args, 0, st));

@@ -122,6 +122,42 @@ int GCGE_Solve(int n, const int *a_colptr, const int *a_rowind, const double *a_
 void *GCGE_HostAlloc(size_t bytes);
 void GCGE_HostFree(void *p);
 
+/* ---- many solves on one GPU (batched problems, serving) ----------------
+ * A request is one GCGE_Solve call (same inputs and outputs) plus its state.
+ * A server runs requests on `workers` host threads, each with its own CUDA
+ * stream, so solves overlap on the device; a request starts when its estimated
+ * device footprint fits the memory budget (0: 80% of the free memory at
+ * creation), or when nothing else runs.  Results are the same alone and in a
+ * mix up to the rounding of the block-PCG reductions, whose grid is shared
+ * between the workers.  No counterpart in the reference (one solve per
+ * process, file-static solver state). */
+typedef struct gcge_request {
+    int n;
+    const int *a_colptr, *a_rowind;
+    const double *a_val;
+    const int *b_colptr, *b_rowind; /* B may be NULL = identity */
+    const double *b_val;
+    int nev, block_size, nev_init, nev_max, max_iter;
+    double tol[2];
+    double gap_min;
+    int auto_shift, precision;
+    const double *X0;
+    int nev_given;
+    double *eval;  /* nev_max */
+    double *evec;  /* n x nev_max or NULL */
+    gcge_solve_info info;
+    int status;    /* set when done */
+    int done;      /* 1 when the outputs are final */
+    double t_submit, t_start, t_end; /* host clock, seconds */
+} gcge_request;
+typedef struct gcge_server gcge_server;
+gcge_server *GCGE_ServerCreate(int workers, size_t device_budget_bytes);
+int GCGE_ServerSubmit(gcge_server *s, gcge_request *r);  /* returns at once */
+int GCGE_ServerWait(gcge_server *s, gcge_request *r);    /* waits for r; returns its status */
+void GCGE_ServerDestroy(gcge_server **s);                 /* runs the queue out, joins */
+/* Submit all, wait for all; returns the first error other than NOT_CONVERGED. */
+int GCGE_SolveBatch(gcge_request *reqs, int count, int workers, size_t device_budget_bytes);
+
 /* Statistics of the last ops->EigenSolver call on this ops. */
 int GCGE_GetSolveInfo(struct OPS_ *ops, gcge_solve_info *info);
 

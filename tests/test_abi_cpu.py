@@ -98,3 +98,29 @@ def test_layout_matches_reference_headers(tmp_path):
     ref = _probe(tmp_path, '"ops_eig_sol_gcg.h"',
                  [os.path.join(ROOT, "oracle", "ref"), ref_src, "/root/reference/app"])
     assert ours == ref
+
+
+@pytest.mark.skipif(shutil.which("gcc") is None, reason="gcc not available")
+def test_request_and_info_layout_match_the_python_mirror(tmp_path):
+    """gcge_request / gcge_solve_info as the C header lays them out == the ctypes
+    structures the Python mirror passes across the ABI."""
+    src = tmp_path / "probe_req.c"
+    src.write_text(r'''
+#include <stdio.h>
+#include <stddef.h>
+#include "gcge_cuda.h"
+int main(void) {
+    printf("%zu %zu %zu %zu %zu %zu\n", sizeof(gcge_request), offsetof(gcge_request, info),
+           offsetof(gcge_request, status), offsetof(gcge_request, t_end),
+           sizeof(gcge_solve_info), offsetof(gcge_solve_info, pcg_kernel_bytes));
+    return 0;
+}
+''')
+    exe = tmp_path / "probe_req"
+    subprocess.run(["gcc", "-w", str(src), "-o", str(exe), f"-I{INC}"], check=True,
+                   capture_output=True)
+    c = [int(x) for x in subprocess.run([str(exe)], check=True, capture_output=True,
+                                        text=True).stdout.split()]
+    py = [ctypes.sizeof(G.Request), G.Request.info.offset, G.Request.status.offset,
+          G.Request.t_end.offset, ctypes.sizeof(G.SolveInfo), G.SolveInfo.pcg_kernel_bytes.offset]
+    assert c == py
