@@ -61,6 +61,12 @@ def parse():
     ap.add_argument("--threads", type=int, default=0,
                     help="host threads of the CPU reference arm (0 = all)")
     ap.add_argument("--size", type=int, default=64, help="grid size k (k^3 unknowns)")
+    ap.add_argument("--no-batch", action="store_true", help="skip the batched and serving lines")
+    ap.add_argument("--batch-count", type=int, default=64)
+    ap.add_argument("--workers", type=int, default=8)
+    ap.add_argument("--serve-count", type=int, default=24)
+    ap.add_argument("--serve-rate", type=float, default=8.0)
+    ap.add_argument("--serve-max-n", type=int, default=100_000)
     ap.add_argument("--solve-once", choices=["mixed", "fp64"], default=None,
                     help="prepare the workload and run one solve (for profiler captures)")
     return ap.parse_args()
@@ -290,6 +296,9 @@ def run_ours(args, d: Dist):
            + B.data.nbytes + X0.nbytes)
     d2h = 8 * c["nev_max"] * (1 + A.n)
 
+    # many solves on this GPU (batched problems, serving); rank 0 of a 1-GPU run
+    batch = run_batch_lines(G, args) if (not args.no_batch and d.world == 1) else None
+
     spmm_ms = sum(i["pcg_spmm_ms"] for i in infos)
     spmm_bytes = sum(i["pcg_spmm_bytes"] for i in infos)
     spmm_phases = sum(i["pcg_spmm_launches"] for i in infos)
@@ -329,6 +338,8 @@ def run_ours(args, d: Dist):
                                     "phases": spmm_phases}},
         "clocks": clk,
     }
+    if batch:
+        line.update(batch)
     prep_mixed.close()
     prep_fp64.close()
     if d.rank == 0 and d.world == 1 and not args.no_cpu_baseline:
@@ -346,6 +357,70 @@ def run_ours(args, d: Dist):
                                     "sample": f"failed: {e}"}
     if d.rank == 0:
         print(json.dumps(line), flush=True)
+
+
+def _percentiles(xs):
+    xs = sorted(xs)
+
+    def q(p):
+        k = (len(xs) - 1) * p / 100.0
+        lo, hi = int(k), min(len(xs) - 1, int(k) + 1)
+        return xs[lo] + (xs[hi] - xs[lo]) * (k - lo)
+    return {"p50": 1000.0 * q(50), "p99": 1000.0 * q(99)}
+
+
+def run_batch_lines(G, args):
+    """Many solves on the one GPU through the request server: the batched
+    workload (first `--batch-count` problems of the 512-problem generator) in
+    mixed and FP64 precision, and a Poisson stream of serving requests."""
+    from gcge_gb300 import problems as P
+
+    def job(c, prec):
+        return G.Job(c["A"], c["B"], c["nev"], c["block_size"], c["nev_init"], c["nev_max"],
+                     X0=P.initial_block(c["A"].n, c["nev_init"], seed=1),
+                     tol=c.get("tol", (1e300, 1e-8)), precision=prec)
+
+    def pairs_of(cs, results):
+        return sum(min(r.nconv, c["nev"]) for c, r in zip(cs, results) if r.status == G.GCGE_OK)
+
+    probs = P.batch_problems(count=args.batch_count, seed=4)
+    G.solve_batch([job(c, G.PREC_MIXED) for c in probs[:args.workers]], workers=args.workers)
+    out = {}
+    for name, prec in (("mixed", G.PREC_MIXED), ("fp64", G.PREC_FP64)):
+        jobs = [job(c, prec) for c in probs]
+        t0 = time.perf_counter()
+        res = G.solve_batch(jobs, workers=args.workers)
+        dt = time.perf_counter() - t0
+        out[name] = {"eigenpairs_per_s": pairs_of(probs, res) / dt, "seconds": dt,
+                     "ok": sum(r.status == G.GCGE_OK for r in res)}
+    batch = {"batch": {
+        "workload": f"first {len(probs)} of the 512 anisotropic 2D problems (nx, ny in 40..220, "
+                    "anisotropy 1..100, diagonal B, nev 8..64, tol 1e-8), seeded",
+        "workers": args.workers, "mixed": out["mixed"], "fp64": out["fp64"],
+        "mixed_over_fp64": out["mixed"]["eigenpairs_per_s"] / out["fp64"]["eigenpairs_per_s"]}}
+
+    reqs = P.serving_requests(args.serve_count, seed=5, rate=args.serve_rate, max_n=args.serve_max_n)
+    jobs = [job(c, G.PREC_MIXED) for c in reqs]
+    with G.Server(workers=args.workers) as srv:
+        t0 = time.perf_counter()
+        for c, j in zip(reqs, jobs):
+            delay = t0 + c["arrival"] - time.perf_counter()
+            if delay > 0:
+                time.sleep(delay)
+            srv.submit(j)
+        res = [srv.wait(j) for j in jobs]
+        span = time.perf_counter() - t0
+    batch["serve"] = {
+        "workload": f"{len(reqs)} Poisson-arrival requests at {args.serve_rate}/s: 2D/3D Laplacians, "
+                    f"shifted RGG Laplacians, variable-coefficient 3D diffusion, n <= "
+                    f"{args.serve_max_n}, nev 10..100, tol 1e-6..1e-10, B = I or lumped mass",
+        "workers": args.workers, "eigenpairs_per_s": pairs_of(reqs, res) / span, "seconds": span,
+        "ok": sum(r.status == G.GCGE_OK for r in res),
+        "not_ok": [[c["name"], c["nev"], r.status, r.nconv, r.niter]
+                   for c, r in zip(reqs, res) if r.status != G.GCGE_OK],
+        "latency_ms": _percentiles([j.latency for j in jobs]),
+        "latency_what": "arrival (submit) to results on the host"}
+    return batch
 
 
 def solve_once(args):

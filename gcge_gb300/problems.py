@@ -306,3 +306,48 @@ def batch_problems(count: int = 512, seed: int = 4, nx_range=(40, 220), nev_rang
         out.append(dict(name=f"aniso2d_{nx}x{ny}_eps{eps:.2f}", A=A, B=diag_matrix(bd), nev=nev,
                         block_size=bs, nev_init=ni, nev_max=nm))
     return out
+
+
+def serving_requests(count: int = 64, seed: int = 5, rate: float = 8.0, max_n: int = 300_000):
+    """The serving workload: a Poisson stream of generalized solve requests
+    mixing three kinds -- (a) 2D/3D Dirichlet Laplacians, n from 1k to 300k;
+    (b) shifted random-geometric-graph Laplacians L + 1e-3 I, n from 5k to
+    200k, mean degree 8-12; (c) the variable-coefficient operator at 32^3 to
+    96^3 -- with B = I or a lumped mass, nev from 10 to 100 and a relative
+    tolerance from 1e-6 to 1e-10 per request.  `max_n` caps the sizes (for
+    short runs).  Every request carries its arrival time in seconds
+    (exponential gaps of mean 1/rate)."""
+    u = splitmix_uniform(seed, 8 * count, 0).reshape(count, 8)
+    out, t = [], 0.0
+    for i in range(count):
+        t += -np.log(max(1e-12, 1.0 - u[i, 0])) / rate
+        kind = int(u[i, 1] * 3)
+        nev = 10 + int(u[i, 2] * 91)
+        tol = float(10.0 ** (-6.0 - 4.0 * u[i, 3]))
+        lumped = u[i, 4] < 0.5
+        if kind == 0:
+            n = int(np.exp(np.log(1000) + u[i, 5] * (np.log(min(300_000, max_n)) - np.log(1000))))
+            if u[i, 6] < 0.5:
+                nx = max(32, int(np.sqrt(n)))
+                A, name, h2 = laplace2d(nx, nx), f"lap2d_{nx}^2", 1.0 / (nx + 1) ** 2
+            else:
+                k = max(12, int(round(n ** (1.0 / 3.0))))
+                A, name, h2 = laplace3d(k), f"lap3d_{k}^3", (1.0 / (k + 1)) ** 3
+            B = (diag_matrix(h2 * (1.0 + 0.1 * splitmix_uniform(seed + 100 + i, A.n, 0)))
+                 if lumped else None)
+        elif kind == 1:
+            n = int(np.exp(np.log(5000) + u[i, 5] * (np.log(min(200_000, max_n)) - np.log(5000))))
+            deg = 8.0 + 4.0 * u[i, 6]
+            A, name = rgg_laplacian(n, deg, seed + 200 + i), f"rgg_{n}_deg{deg:.1f}"
+            B = (diag_matrix(1.0 + 0.1 * splitmix_uniform(seed + 300 + i, A.n, 0))
+                 if lumped else None)
+        else:
+            kmax = max(32, min(96, int(max_n ** (1.0 / 3.0))))
+            k = 32 + int(u[i, 5] * (kmax - 32 + 1))
+            A, B = vardiff3d(k, seed + 400 + i)
+            name = f"vardiff3d_{k}^3"
+        nev = min(nev, A.n // 4)
+        bs, ni, nm = gcge_block_rule(nev)
+        out.append(dict(name=name, A=A, B=B, nev=nev, block_size=bs, nev_init=ni, nev_max=nm,
+                        tol=(1e300, tol), arrival=t))
+    return out
