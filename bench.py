@@ -320,6 +320,7 @@ def run_ours(args, d: Dist):
         "niter": [i["niter"] for i in infos], "nconv": [i["nconv"] for i in infos],
         "phase_ms_last_step": infos[-1]["phase_ms"], "phase_ms_fp64": infos64[-1]["phase_ms"],
         "gpu_launches": sum(i["kernel_launches"] for i in infos),
+        "escalated_solves": sum(i.get("precision_escalation_iter", 0) > 0 for i in infos),
         "latency_ms": {"p50": percentile(lat, 50), "p99": percentile(lat, 99), "solves": len(lat),
                        "what": "one mixed solve, inputs resident in HBM"},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d),

@@ -73,7 +73,7 @@ class SolveInfo(ctypes.Structure):
                 ("phase_ms", ctypes.c_double * 10), ("pcg_spmm_launches", ctypes.c_int),
                 ("pcg_spmm_ms", ctypes.c_double), ("pcg_spmm_bytes", ctypes.c_double),
                 ("pcg_kernel_launches", ctypes.c_int), ("pcg_kernel_ms", ctypes.c_double),
-                ("pcg_kernel_bytes", ctypes.c_double)]
+                ("pcg_kernel_bytes", ctypes.c_double), ("precision_escalation_iter", ctypes.c_int)]
 
     PHASES = ("checkconv", "compP", "compRR", "rr_matW", "eig", "compRV", "compW", "linsol",
               "compX", "initX")
@@ -83,7 +83,7 @@ class SolveInfo(ctypes.Structure):
                                            "kernel_launches", "seconds", "pcg_spmm_launches",
                                            "pcg_spmm_ms", "pcg_spmm_bytes",
                                            "pcg_kernel_launches", "pcg_kernel_ms",
-                                           "pcg_kernel_bytes")}
+                                           "pcg_kernel_bytes", "precision_escalation_iter")}
         d["phase_ms"] = {p: self.phase_ms[i] for i, p in enumerate(self.PHASES)}
         return d
 

@@ -139,7 +139,7 @@ enum { PH_CHECK = 0, PH_P, PH_RR, PH_RRW, PH_EIG, PH_RV, PH_W, PH_LINSOL, PH_X, 
 static void dgram(const SolverCtx &c, int n, int m, int w, const double *Q, int ldq,
                   const double *P, int ldp, double *C, int ldc, double *scratch, size_t elems,
                   cudaStream_t st) {
-    if (c.precision == GCGE_PREC_MIXED)
+    if (c.precision == GCGE_PREC_MIXED && !c.escalated)
         oz_gram(n, m, w, Q, ldq, P, ldp, C, ldc, scratch, elems, st);
     else
         gram(n, m, w, Q, ldq, P, ldp, C, ldc, scratch, elems, st);
@@ -147,7 +147,7 @@ static void dgram(const SolverCtx &c, int n, int m, int w, const double *Q, int 
 static void dlincomb(const SolverCtx &c, int n, int k, int m, const double *X, int ldx,
                      const double *C, int ldc, double *Y, int ldy, const double *beta, int incb,
                      cudaStream_t st, double alpha = 1.0) {
-    if (c.precision == GCGE_PREC_MIXED)
+    if (c.precision == GCGE_PREC_MIXED && !c.escalated)
         oz_lincomb(n, k, m, X, ldx, C, ldc, Y, ldy, beta, incb, st, alpha);
     else
         lincomb(n, k, m, X, ldx, C, ldc, Y, ldy, beta, incb, st, alpha);
@@ -364,12 +364,16 @@ struct GcgRun {
                 break;
             }
         }
+        const double first_abs = idx < numCheck ? res[idx] : 0.0;
+        const double first_rel =
+            idx < numCheck ? res[idx] / std::max(std::fabs(ss_eval[startN + idx]), 1e-300) : 0.0;
         for (; idx > 0; --idx) {
             if (std::fabs((ss_eval[startN + idx - 1] - ss_eval[startN + idx]) / ss_eval[startN + idx - 1]) >
                 g.gapMin)
                 break;
         }
         const int nevConv = sizeC + idx;
+        watch_progress(nevConv, first_abs, first_rel);
         offset[0] = 0;
         int state = 1, num_unconv = 0;
         for (idx = 0; idx < numCheck; ++idx) {
@@ -404,6 +408,35 @@ struct GcgRun {
     }
     std::vector<double> last_res;
     int iter_print = 0;
+
+    // Precision escalation of the mixed solve.  The FP32 inner solve sees the
+    // shifted operator with entry errors of about eps32 |S|, which the
+    // near-singular shift (0.01 of a gap from the target eigenvalue) amplifies,
+    // and the digit products are exact only to 2^-56 of each chunk's largest
+    // entries; for tolerances tight against |A| (small eigenvalues, tol ~1e-10)
+    // the residuals then stop falling just above the tolerance.  When the
+    // first unconverged residual is within 100x of the tolerance and shrinks
+    // by less than 2x over 10 outer iterations with no newly converged pair,
+    // the rest of the solve runs in FP64 (inner solve and dense products: the
+    // reference's arithmetic).
+    int escalated_at = 0;
+    std::vector<std::pair<int, double>> progress;
+    void watch_progress(int nevConv, double first_abs, double first_rel) {
+        if (c.precision != GCGE_PREC_MIXED || c.escalated) return;
+        progress.push_back({nevConv, first_rel});
+        constexpr size_t K = 10;
+        if (progress.size() <= K) return;
+        const bool near_tol = first_rel <= 100.0 * g.tol[1] && first_abs <= 100.0 * g.tol[0];
+        const auto &old = progress[progress.size() - 1 - K];
+        const auto &cur = progress.back();
+        if (near_tol && cur.first <= old.first && cur.second > 0.5 * old.second) {
+            c.escalated = true;
+            escalated_at = iter_print + 1;
+            if (g.print)
+                printf("%3d mixed precision: residual %6.5e stalled near the tolerance, FP64 from here\n",
+                       escalated_at, cur.second);
+        }
+    }
 
     // ---------------- ComputeP (:322-463)
     void compute_p(const std::vector<int> &offset) {
@@ -470,7 +503,7 @@ struct GcgRun {
         GCGE_CUDA(cudaMemcpyAsync(c.dvec.p, hscale, sizeof(double) * bsz, cudaMemcpyHostToDevice, st));
         scale_columns(n, bsz, c.bbuf.p, ld, c.dvec.p, st);
         // shifted operator S = A + sigma B on the union pattern
-        const bool mixed = c.precision == GCGE_PREC_MIXED;
+        const bool mixed = c.precision == GCGE_PREC_MIXED && !c.escalated;
         shift_values(c.upat.padded, c.ua.p, c.ub.p, sigma, c.us64.p, mixed ? c.us32.p : nullptr,
                      st);
         timer.mark(PH_LINSOL);
@@ -711,6 +744,7 @@ void gcg_eigensolver(void *Ah, void *Bh, double *eval, void **evec, int nevGiven
         c->pub.eval = eval;
         c->pub.nevGiven = nevGiven;
         GCGE_REQUIRE(V->ld == R->ld, GCGE_ERR_ARG, "EigenSolver: leading dimensions differ");
+        c->escalated = false;
         GcgRun run(*c, A, B, V, R);
         c->pcg.timing_reset(st);
         const int status = run.run(eval, nevGiven, nevConv);
@@ -721,6 +755,7 @@ void gcg_eigensolver(void *Ah, void *Bh, double *eval, void **evec, int nevGiven
         c->info.pcg_kernel_launches = c->pcg.launches;
         c->info.pcg_kernel_ms = c->pcg.kernel_ms;
         c->info.pcg_kernel_bytes = c->pcg.kernel_bytes;
+        c->info.precision_escalation_iter = run.escalated_at;
         run.pcg_iters = (int)c->pcg.total_iters;
         run.spmm_calls += (int)c->pcg.total_iters;
         c->info.nconv = *nevConv;

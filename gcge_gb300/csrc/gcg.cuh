@@ -9,6 +9,9 @@ namespace gcge {
 struct SolverCtx {
     GCGSolver pub;  // first member: ops->eigen_solver_workspace points here
     int precision = GCGE_PREC_FP64;
+    // mixed solve that fell back to FP64 for its remaining iterations (reset
+    // at the start of every solve)
+    bool escalated = false;
     int refine_steps = 8;  // upper bound; the refinement stops on convergence
     gcge_solve_info info{};
     int last_status = GCGE_OK;

@@ -100,6 +100,9 @@ typedef struct gcge_solve_info {
     double pcg_kernel_ms;    /* their summed device time (CUDA events around each launch) */
     double pcg_kernel_bytes; /* their summed algorithmic bytes: per iteration the matrix once
                                 + 12 n k_active v (p update, SpMM, x/r update), plus the setup */
+    int precision_escalation_iter; /* mixed solve: outer iteration from which the solve
+                                      ran in FP64 because its residuals stalled just
+                                      above the tolerance (0: never) */
 } gcge_solve_info;
 
 /* One-call solve of A x = lambda B x for the nev smallest pairs from host

@@ -96,3 +96,30 @@ def test_prepared_solve_is_repeatable(gpu_lib):
     assert np.array_equal(r1.eval, r2.eval) and r1.niter == r2.niter
     assert np.array_equal(r1.evec, r2.evec)
     assert r1.info["kernel_launches"] > 0 and r1.info["spmm_calls"] > 0
+
+
+def test_mixed_escalates_to_fp64_inner_solve_when_fp32_stalls(gpu_lib):
+    """A shifted random-geometric-graph Laplacian (eigenvalues from 1e-3, |A| ~ 20)
+    at relative tolerance 4.6e-10: the FP32 inner solve's operator rounding,
+    amplified by the near-singular shift, and the digit products stall the
+    residuals just above the tolerance; the mixed solve must notice, finish in
+    FP64 and converge like the FP64 solve (the reference converges in ~100
+    iterations on this input)."""
+    G = gpu_lib
+    import scipy.sparse.linalg as sla
+    c = P.serving_requests(3, seed=5, rate=8.0, max_n=100_000)[1]
+    assert c["name"].startswith("rgg_9745") and c["B"] is None
+    X0 = P.initial_block(c["A"].n, c["nev_init"], seed=1)
+    kw = dict(X0=X0, tol=c["tol"], want_evec=False)
+    mixed = G.solve(c["A"], c["B"], c["nev"], c["block_size"], c["nev_init"], c["nev_max"],
+                    precision=G.PREC_MIXED, **kw)
+    fp64 = G.solve(c["A"], c["B"], c["nev"], c["block_size"], c["nev_init"], c["nev_max"],
+                   precision=G.PREC_FP64, **kw)
+    nev = c["nev"]
+    assert fp64.status == G.GCGE_OK and mixed.status == G.GCGE_OK, (fp64.status, mixed.status)
+    assert mixed.nconv >= nev and mixed.info["precision_escalation_iter"] > 20
+    assert fp64.info["precision_escalation_iter"] == 0
+    w = np.sort(sla.eigsh(c["A"].to_scipy().tocsc(), k=nev, sigma=0, which="LM",
+                          return_eigenvectors=False))
+    np.testing.assert_allclose(mixed.eval[:nev], w, rtol=1e-9, atol=0)
+    np.testing.assert_allclose(mixed.eval[:nev], fp64.eval[:nev], rtol=1e-10, atol=0)
