@@ -38,6 +38,7 @@ class GCGParams:
     num_iter_max: int = 500
     gap_min: float = 1e-5
     check_conv_max_num: int = 50
+    orth_method: str = "mgs"      # InitializeX / ComputeW orthogonalisation: "mgs" or "bgs"
     orth_block_size: int = -1
     orth_max_reorth: int = 2
     orth_zero_tol: float = 2 * DBL_EPSILON
@@ -48,6 +49,7 @@ class GCGParams:
     cg_tol_type: str = "abs"
     cg_auto_shift: int = 1
     cg_shift: float = 0.0
+    cg_order: int = 1                             # compW_cg_order: 1 ComputeW, 2 ComputeW12
     compRR_tol: float = 2 * DBL_EPSILON
 
 
@@ -106,8 +108,8 @@ class GCGOracle:
         while k < end_x:
             Bxk = self.matdot(B, x[:, k:k + 1])
             r = x[:, k:end_x].T @ Bxk[:, 0]
-            rk = math.sqrt(r[0]) if r[0] > 0 else 0.0 if r[0] == 0 else float("nan")
-            if not (rk >= p.orth_zero_tol):
+            rk = math.sqrt(r[0]) if r[0] >= 0 else float("nan")
+            if rk < p.orth_zero_tol:   # a NaN norm is kept, as in the reference
                 # drop column k: move the last column into its place (:64-74)
                 if k < end_x - 1:
                     x[:, k] = x[:, end_x - 1]
@@ -166,6 +168,94 @@ class GCGOracle:
             bsz = min(bsz, end_x - init_start)
         return end_x
 
+    def _orth_self_evp(self, x, start_x, end_x, B):
+        """OrthSelfEVP, src/ops_orth.c:122-201: G = X^T B X = V diag(w) V^T
+        (ascending, dsyev), X <- X V diag(w^-1/2) with the eigenvalues whose
+        magnitude is at most orth_zero_tol dropped; repeated until nothing is
+        dropped and sum |w^-1/2| = k to reorth_tol."""
+        p = self.p
+        for _ in range(1 + p.orth_max_reorth):
+            if end_x == start_x:
+                return end_x
+            X = x[:, start_x:end_x]
+            N = end_x - start_x
+            G = X.T @ self.matdot(B, X)
+            w, V = np.linalg.eigh(0.5 * (G + G.T))
+            lin_dep = 0
+            for k in range(N):
+                if abs(w[k]) > p.orth_zero_tol:
+                    w[k] = 1.0 / np.sqrt(w[k])
+                else:
+                    lin_dep += 1
+            Y = (X @ V[:, lin_dep:]) * w[lin_dep:]
+            end_x -= lin_dep
+            x[:, start_x:end_x] = Y
+            if lin_dep == 0 and abs(np.sum(np.abs(w)) - N) < p.reorth_tol:
+                break
+        return end_x
+
+    def _orth_binary(self, x, start_x, end_x, B, bsz, evp):
+        """OrthBinary, src/ops_orth.c:416-518: leaves of at most bsz columns by
+        OrthSelfEVP (evp) or OrthSelf; otherwise the first half, CGS of the
+        second half against it, the second half, and the second half's last
+        columns moved into the first half's dropped slots."""
+        p = self.p
+        ncols = end_x - start_x
+        if ncols <= 0:
+            return end_x
+        if ncols <= bsz:
+            if evp:
+                return self._orth_self_evp(x, start_x, end_x, B)
+            return self._orth_self(x, start_x, end_x, B)
+        s0, mid = start_x, start_x + ncols // 2
+        e0 = self._orth_binary(x, s0, mid, B, bsz, evp)
+        s1, e1 = mid, end_x
+        if e0 > s0:
+            BX0 = self.matdot(B, x[:, s0:e0])   # kept from the first pass (:451-463)
+            for _ in range(1 + p.orth_max_reorth):
+                coef = BX0.T @ x[:, s1:e1]
+                x[:, s1:e1] -= x[:, s0:e0] @ coef
+                if np.max(np.abs(coef)) < p.reorth_tol:
+                    break
+        e1 = self._orth_binary(x, s1, e1, B, bsz, evp)
+        gap = mid - e0
+        new_end = e1 - gap
+        ln = min(gap, e1 - s1)
+        if ln > 0:
+            x[:, e0:e0 + ln] = x[:, e1 - ln:e1].copy()
+        return new_end
+
+    def bgs(self, x, start_x, end_x, B):
+        """BinaryGramSchmidt, src/ops_orth.c:519-623.  Returns the new end_x."""
+        p = self.p
+        if end_x <= start_x:
+            return end_x
+        if start_x > 0:   # against the prefix, checked every pass (:540-561)
+            for _ in range(1 + p.orth_max_reorth):
+                coef = x[:, :start_x].T @ self.matdot(B, x[:, start_x:end_x])
+                x[:, start_x:end_x] -= x[:, :start_x] @ coef
+                if np.max(np.abs(coef)) < p.reorth_tol:
+                    break
+        # leaf method and size (:575-591): blocks under 16 columns use OrthSelf
+        # with leaves of 4 (or the given size); wider ones OrthSelfEVP with
+        # leaves of at most a quarter of the block
+        k = end_x - start_x
+        bsz = p.orth_block_size
+        if k < 16:
+            bsz = 4 if bsz <= 0 else bsz
+            evp = False
+        else:
+            bsz = k // 4 if (bsz <= 0 or bsz > k // 4) else bsz
+            evp = True
+        return self._orth_binary(x, start_x, end_x, B, bsz, evp)
+
+    def orth(self, x, start_x, end_x, B):
+        """MultiVecOrth with the method of InitializeX / ComputeW
+        (src/ops_eig_sol_gcg.c:119-141, :650-668)."""
+        if self.p.orth_method == "bgs":
+            return self.bgs(x, start_x, end_x, B)
+        return self.mgs(x, start_x, end_x, B)
+
     # ------------------------------------------------------------------
     # BlockPCG: src/ops_lin_sol.c:140-437
     # ------------------------------------------------------------------
@@ -216,13 +306,13 @@ class GCGOracle:
     def initialize_x(self, V, ritz_vec, nev_given):
         """InitializeX, :102-159."""
         V[:, :nev_given] = ritz_vec[:, :nev_given]
-        nev_given = self.mgs(V, 0, nev_given, self.B)
+        nev_given = self.orth(V, 0, nev_given, self.B)
         if self.sizeX > nev_given:
             # libc rand() fill (app/app_lapack.c:322-333); not reached when
             # the caller supplies nevInit independent vectors
             rng = np.random.default_rng(0)
             V[:, nev_given:self.sizeX] = rng.random((self.n, self.sizeX - nev_given))
-        self.endX = self.mgs(V, nev_given, self.sizeX, self.B)
+        self.endX = self.orth(V, nev_given, self.sizeX, self.B)
         assert self.endX == self.sizeX
 
     def compute_ritz_vec(self, ritz_vec, V):
@@ -340,7 +430,51 @@ class GCGOracle:
         self.times["linsol"] += time.perf_counter() - t0
         # b aliases ritz_vec columns [offset[1], offset[1]+bsz) and is clobbered
         # there (:484, :527); ComputeRitzVec rewrites those columns later
-        self.endW = self.mgs(V, self.startW, self.endW, self.B)
+        self.endW = self.orth(V, self.startW, self.endW, self.B)
+        self.sizeW = self.endW - self.startW
+
+    def compute_w12(self, V, ritz_vec, offset):
+        """ComputeW12 (compW_cg_order 2), :703-929, on the branch app_ccs takes
+        (no MatAxpby): the first total/2 unconverged columns (:757-790) get the
+        BlockPCG solution x1 from their Ritz vectors (:807) and a second solve of
+        the same system restarted from x1 (:815-901; the right-hand side is
+        rebuilt there only because the shifted product used it as scratch)."""
+        p = self.p
+        sigma = 0.0
+        if p.cg_auto_shift == 1:
+            sc = self.sizeC
+            sigma = -self.ss_eval[sc] + (self.ss_eval[sc + 1] - self.ss_eval[sc]) * 0.01
+        self.sigma = p.cg_shift + sigma
+        self.startW = self.endP
+        total = sum(offset[2 * i + 2] - offset[2 * i + 1] for i in range(offset[0]))
+        half = total // 2
+        bsz = 0
+        bcols = []
+        for i in range(offset[0]):
+            o1 = offset[2 * i + 1]
+            ln = offset[2 * i + 2] - o1
+            if bsz + ln >= half:
+                ln = half - bsz
+            V[:, self.startW + bsz:self.startW + bsz + ln] = ritz_vec[:, o1:o1 + ln]
+            bcols.append(self.matdot(self.B, V[:, o1:o1 + ln])
+                         * (self.ss_eval[o1:o1 + ln] + self.sigma)[None, :])
+            bsz += ln
+            if bsz >= half:
+                break
+        t0 = time.perf_counter()
+        w0 = self.startW
+        if bsz > 0:
+            b = np.asfortranarray(np.concatenate(bcols, axis=1))
+            for _ in range(2):
+                xw = np.asfortranarray(V[:, w0:w0 + bsz])
+                self.block_pcg(b, xw)
+                V[:, w0:w0 + bsz] = xw
+                if w0 == self.startW:      # x2 starts from x1 (:810-814)
+                    V[:, w0 + bsz:w0 + 2 * bsz] = xw
+                w0 += bsz
+        self.times["linsol"] += time.perf_counter() - t0
+        self.endW = self.startW + 2 * bsz
+        self.endW = self.orth(V, self.startW, self.endW, self.B)
         self.sizeW = self.endW - self.startW
 
     def compute_rayleigh_ritz(self, V, nev_conv):
@@ -483,7 +617,10 @@ class GCGOracle:
             self.compute_x(V, ritz_vec)
             self.times["compX"] += time.perf_counter() - t
             t = time.perf_counter()
-            self.compute_w(V, ritz_vec, offsetW)
+            if self.p.cg_order != 1:   # (:1456-1461)
+                self.compute_w12(V, ritz_vec, offsetW)
+            else:
+                self.compute_w(V, ritz_vec, offsetW)
             self.times["compW"] += time.perf_counter() - t
             offsetP, offsetW = offsetW, offsetP
             t = time.perf_counter()
@@ -505,10 +642,15 @@ class GCGOracle:
 
 
 def gcg_solve(A, B, X0, nev, block_size, nev_init, nev_max, tol=(1e300, 1e-8),
-              max_iter=500, gap_min=1e-5, auto_shift=1) -> GCGResult:
-    """Convenience wrapper: the reference's default GCGE parameter set."""
+              max_iter=500, gap_min=1e-5, auto_shift=1, orth=None, w_order=1) -> GCGResult:
+    """Convenience wrapper: the reference's default GCGE parameter set;
+    orth = (method, block_size) as EigenSolverSetParameters_GCG sets it for
+    InitializeX and ComputeW; w_order = compW_cg_order."""
     p = GCGParams(nev_init=nev_init, nev_max=nev_max, block_size=block_size, tol=tuple(tol),
-                  num_iter_max=max_iter, gap_min=gap_min, cg_auto_shift=auto_shift)
+                  num_iter_max=max_iter, gap_min=gap_min, cg_auto_shift=auto_shift,
+                  cg_order=w_order)
+    if orth is not None:
+        p.orth_method, p.orth_block_size = orth
     return GCGOracle(A, B, p).solve(np.asfortranarray(X0), nev)
 
 

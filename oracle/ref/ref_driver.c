@@ -19,13 +19,21 @@
 #include "app_ccs.h"
 #include "ops_eig_sol_gcg.h"
 
-int ref_gcg_solve(int n,
+/* As ref_gcg_solve, with the orthogonalisation method of InitializeX and
+ * ComputeW chosen through the reference's own setter
+ * (EigenSolverSetParameters_GCG, src/ops_eig_sol_gcg.c:1684-1741): orth_method
+ * "mgs" or "bgs" (NULL: the GCGE_Setparameters default) and its block size;
+ * then argv (argc entries, may be 0) through the reference's command-line
+ * setter (EigenSolverSetParametersFromCommandLine_GCG, :1743-1862), e.g.
+ * {"-gcge_compW_cg_order", "2"}. */
+int ref_gcg_solve_opts(int n,
                   const int *a_colptr, const int *a_rowind, const double *a_val,
                   const int *b_colptr, const int *b_rowind, const double *b_val,
                   int nev, int block_size, int nev_init, int nev_max, int max_iter,
                   double abs_tol, double rel_tol, double gap_min, int auto_shift,
                   const double *x0, int nev_given,
-                  double *eval_out, double *evec_out, int *nconv_out, int *niter_out)
+                  double *eval_out, double *evec_out, int *nconv_out, int *niter_out,
+                  const char *orth_method, int orth_block_size, int argc, char **argv)
 {
     OPS *ops = NULL;
     OPS_Create(&ops);
@@ -63,6 +71,13 @@ int ref_gcg_solve(int n,
     EigenSolverSetup_GCG(gap_min, nev_init, nev_max, block_size, tol, max_iter, 0, 0, 0,
                          mv_ws, dbl_ws, int_ws, ops);
     GCGE_Setparameters(gap_min, auto_shift, ops);
+    if (orth_method != NULL)
+        EigenSolverSetParameters_GCG(0, orth_method, orth_block_size, -1, 0.0,
+                                     NULL, -1, -1, 0.0,
+                                     orth_method, orth_block_size, -1, 0.0,
+                                     0, 0.0, 0.0, NULL, auto_shift, 0, 0.0, 0.0, ops);
+    if (argc > 0)
+        EigenSolverSetParametersFromCommandLine_GCG(argc, argv, ops);
     int nconv = nev;
     ops->EigenSolver(&A, matB, eval, evec, nev_given, &nconv, ops);
 
@@ -75,6 +90,57 @@ int ref_gcg_solve(int n,
     GCGE_Destroymvws(mv_ws, dbl_ws, int_ws, nev_max, block_size, ops);
     ops->MultiVecDestroy(&evec, nev_max, ops);
     free(eval);
+    OPS_Destroy(&ops);
+    return 0;
+}
+
+int ref_gcg_solve(int n,
+                  const int *a_colptr, const int *a_rowind, const double *a_val,
+                  const int *b_colptr, const int *b_rowind, const double *b_val,
+                  int nev, int block_size, int nev_init, int nev_max, int max_iter,
+                  double abs_tol, double rel_tol, double gap_min, int auto_shift,
+                  const double *x0, int nev_given,
+                  double *eval_out, double *evec_out, int *nconv_out, int *niter_out)
+{
+    return ref_gcg_solve_opts(n, a_colptr, a_rowind, a_val, b_colptr, b_rowind, b_val, nev,
+                              block_size, nev_init, nev_max, max_iter, abs_tol, rel_tol, gap_min,
+                              auto_shift, x0, nev_given, eval_out, evec_out, nconv_out,
+                              niter_out, NULL, 0, 0, NULL);
+}
+
+#include "ops_orth.h"
+/* One call of the reference's MultiVecOrth on a column-major block x (n x m,
+ * leading dimension n) through the app_ccs backend: "bgs" or "mgs" with the
+ * given block size / reorthogonalisations / zero tolerance; B (CCS) may be
+ * NULL.  Columns [start, *end) are orthogonalised against [0, start). */
+int ref_orth(int n, int m, double *x, int start, int *end, const char *method, int block_size,
+             int max_reorth, double zero_tol,
+             const int *b_colptr, const int *b_rowind, const double *b_val)
+{
+    OPS *ops = NULL;
+    OPS_Create(&ops);
+    OPS_CCS_Set(ops);
+    OPS_Setup(ops);
+    CCSMAT B;
+    void *matB = NULL;
+    if (b_colptr != NULL) {
+        B.data = (double *)b_val; B.i_row = (int *)b_rowind; B.j_col = (int *)b_colptr;
+        B.nrows = n; B.ncols = n;
+        matB = &B;
+    }
+    LAPACKVEC X = {x, n, m, n};
+    double *ws_data = calloc((size_t)n * (size_t)m, sizeof(double));
+    LAPACKVEC WS = {ws_data, n, m, n};
+    double *dbl_ws = calloc((size_t)(8 * m * m + 64 * m + 1024), sizeof(double));
+    if (strcmp(method, "bgs") == 0)
+        MultiVecOrthSetup_BinaryGramSchmidt(block_size, max_reorth, zero_tol, (void **)&WS, dbl_ws,
+                                            ops);
+    else
+        MultiVecOrthSetup_ModifiedGramSchmidt(block_size, max_reorth, zero_tol, (void **)&WS, dbl_ws,
+                                              ops);
+    ops->MultiVecOrth((void **)&X, start, end, matB, ops);
+    free(ws_data);
+    free(dbl_ws);
     OPS_Destroy(&ops);
     return 0;
 }

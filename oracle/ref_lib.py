@@ -40,10 +40,14 @@ def _ptr(a):
 
 
 def ref_solve(A, B, X0, nev, block_size, nev_init, nev_max, tol=(1e300, 1e-8), max_iter=500,
-              gap_min=1e-5, auto_shift=1):
+              gap_min=1e-5, auto_shift=1, orth=None, args=()):
     """Run the reference GCG (app_ccs backend) on CSRMatrix inputs.
 
     A and B are symmetric, so their CSR arrays are also their CCS arrays.
+    orth = (method, block_size), e.g. ("bgs", 8), selects the orthogonalisation
+    of InitializeX and ComputeW through EigenSolverSetParameters_GCG; args
+    (strings, e.g. ("-gcge_compW_cg_order", "2")) go through
+    EigenSolverSetParametersFromCommandLine_GCG.
     Returns (eval[nev_max], evec[n, nev_max], nconv, niter, seconds).
     """
     lib = _load()
@@ -54,12 +58,29 @@ def ref_solve(A, B, X0, nev, block_size, nev_init, nev_max, tol=(1e300, 1e-8), m
     nc = ctypes.c_int()
     it = ctypes.c_int()
     t = time.perf_counter()
-    lib.ref_gcg_solve(
+    argv = (ctypes.c_char_p * max(1, len(args)))(*[a.encode() for a in args])
+    lib.ref_gcg_solve_opts(
         ctypes.c_int(n), _ptr(A.indptr), _ptr(A.indices), _ptr(A.data),
         _ptr(None if B is None else B.indptr), _ptr(None if B is None else B.indices),
         _ptr(None if B is None else B.data),
         ctypes.c_int(nev), ctypes.c_int(block_size), ctypes.c_int(nev_init), ctypes.c_int(nev_max),
         ctypes.c_int(max_iter), ctypes.c_double(tol[0]), ctypes.c_double(tol[1]),
         ctypes.c_double(gap_min), ctypes.c_int(auto_shift), _ptr(X0), ctypes.c_int(X0.shape[1]),
-        _ptr(ev), _ptr(evec), ctypes.byref(nc), ctypes.byref(it))
+        _ptr(ev), _ptr(evec), ctypes.byref(nc), ctypes.byref(it),
+        None if orth is None else orth[0].encode(), ctypes.c_int(0 if orth is None else orth[1]),
+        ctypes.c_int(len(args)), argv)
     return ev, evec, nc.value, it.value, time.perf_counter() - t
+
+
+def ref_orth(x, start, end, method, block_size, B=None, max_reorth=2,
+             zero_tol=2 * np.finfo(float).eps):
+    """The reference's MultiVecOrth ("bgs" or "mgs" setup) on a copy of x
+    (n x m); returns (x[:, :new_end], new_end)."""
+    lib = _load()
+    x = np.array(x, dtype=np.float64, order="F", copy=True)
+    e = ctypes.c_int(end)
+    arrs = [None, None, None] if B is None else [B.indptr, B.indices, B.data]
+    lib.ref_orth(ctypes.c_int(x.shape[0]), ctypes.c_int(x.shape[1]), _ptr(x), ctypes.c_int(start),
+                 ctypes.byref(e), method.encode(), ctypes.c_int(block_size),
+                 ctypes.c_int(max_reorth), ctypes.c_double(zero_tol), *[_ptr(a) for a in arrs])
+    return x[:, :e.value].copy(), e.value

@@ -27,6 +27,35 @@ def golden_vectors():
     return dict(np.load(os.path.join(GOLDEN_DIR, "golden_vectors.npz")))
 
 
+@pytest.fixture(scope="session")
+def golden_orth():
+    with open(os.path.join(GOLDEN_DIR, "golden_orth.json")) as f:
+        meta = json.load(f)
+    meta["arrays"] = dict(np.load(os.path.join(GOLDEN_DIR, "golden_orth.npz")))
+    return meta
+
+
+def orth_case(name):
+    """Inputs of an orthogonalisation fixture (tests/golden/orth_cases.py)."""
+    if GOLDEN_DIR not in sys.path:
+        sys.path.insert(0, GOLDEN_DIR)
+    import orth_cases
+    return orth_cases.build(name)
+
+
+def orth_solve_case(name):
+    """The generator call of each bgs / ComputeW12 solve fixture (make_golden_orth.py)."""
+    if GOLDEN_DIR not in sys.path:
+        sys.path.insert(0, GOLDEN_DIR)
+    from make_golden_orth import solve_cases
+    return solve_cases()[name][0]()
+
+
+def b_projector(X, B):
+    """X X^T B: the B-orthogonal projector onto span(X) for B-orthonormal X."""
+    return X @ (X if B is None else B @ X).T
+
+
 def build_case(name):
     """The generator call of each golden case (mirrors tests/golden/make_golden.py)."""
     sys.path.insert(0, os.path.join(ROOT, "tests", "golden"))

@@ -1,0 +1,99 @@
+"""Generate the orthogonalisation and ComputeW12 fixtures from the reference
+GCGE CPU path.
+
+Three parts, all from the reference's own C sources compiled into
+oracle/_ref/libgcge_ref.so (oracle/ref/Makefile):
+  * MultiVecOrth on the inputs of orth_cases.py, once with the binary
+    Gram-Schmidt setup (MultiVecOrthSetup_BinaryGramSchmidt, src/ops_orth.c:625)
+    and once with the modified one (:395): the new end and the block after;
+  * whole GCG solves with "bgs" selected for InitializeX and ComputeW through
+    EigenSolverSetParameters_GCG;
+  * whole GCG solves with compW_cg_order 2 (ComputeW12) set through
+    EigenSolverSetParametersFromCommandLine_GCG;
+the solves store eigenvalues, converged and iteration counts.
+
+    make -C oracle/ref && OPENBLAS_NUM_THREADS=1 python tests/golden/make_golden_orth.py
+
+Writes golden_orth.json and golden_orth.npz beside this file.
+"""
+from __future__ import annotations
+
+import json
+import os
+import sys
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, HERE)
+
+import orth_cases as OC  # noqa: E402
+from gcge_gb300 import problems as P  # noqa: E402
+from oracle import ref_lib  # noqa: E402
+
+ZERO_TOL = 2 * np.finfo(float).eps   # GCGE_Setparameters' orth_zero_tol
+MAX_REORTH = 2
+
+
+def _aniso():
+    return P.aniso2d(40, 30, 10.0), P.diag_matrix(0.5 + 1.5 * P.splitmix_uniform(11, 1200, 0))
+
+
+def solve_cases():
+    """name -> (builder, nev, bs, nev_init, nev_max, orth or None, command-line args)."""
+    rule = P.gcge_block_rule
+    w12 = ("-gcge_compW_cg_order", "2")
+    out = {"laplace2d_24x24_nev8_bgs": (lambda: (P.laplace2d(24, 24), None), 8, 4, 12, 20,
+                                        ("bgs", -1), ())}
+    bs, ni, nm = rule(16)
+    out["aniso2d_40x30_eps10_diagB_bgs"] = (_aniso, 16, bs, ni, nm, ("bgs", -1), ())
+    bs3, ni3, nm3 = rule(100)
+    out["laplace3d_mass_16_bgs"] = (lambda: (P.laplace3d(16), P.mass3d(16)), 100, bs3, ni3, nm3,
+                                    ("bgs", -1), ())
+    out["laplace3d_mass_16_bgs_leaf8"] = (lambda: (P.laplace3d(16), P.mass3d(16)), 100, bs3, ni3,
+                                          nm3, ("bgs", 8), ())
+    out["laplace2d_24x24_nev8_w12"] = (lambda: (P.laplace2d(24, 24), None), 8, 4, 12, 20, None,
+                                       w12)
+    out["aniso2d_40x30_eps10_diagB_w12"] = (_aniso, 16, bs, ni, nm, None, w12)
+    out["aniso2d_40x30_eps10_diagB_w12_bgs"] = (_aniso, 16, bs, ni, nm, ("bgs", -1), w12)
+    out["laplace3d_mass_16_w12"] = (lambda: (P.laplace3d(16), P.mass3d(16)), 100, bs3, ni3, nm3,
+                                    None, w12)
+    return out
+
+
+def main():
+    if not ref_lib.available():
+        raise SystemExit("oracle/_ref/libgcge_ref.so missing: run make -C oracle/ref")
+    meta, arrays = {"orth": {}, "solve": {}}, {}
+    for name in OC.CASES:
+        x, start, end, bs, B = OC.build(name)
+        for method in ("bgs", "mgs"):
+            xo, eo = ref_lib.ref_orth(x, start, end, method, bs, B, MAX_REORTH, ZERO_TOL)
+            meta["orth"][f"{name}/{method}"] = dict(start=start, end_in=end, end=eo, block_size=bs,
+                                                  zero_tol=ZERO_TOL, max_reorth=MAX_REORTH)
+            arrays[f"{name}/{method}"] = xo
+            print(f"{name}/{method}: end {end} -> {eo}", file=sys.stderr, flush=True)
+    for name, (builder, nev, bs, ni, nm, orth, args) in solve_cases().items():
+        A, B = builder()
+        X0 = P.initial_block(A.n, ni, seed=1)
+        t = time.time()
+        ev, _, nc, it, sec = ref_lib.ref_solve(A, B, X0, nev, bs, ni, nm, tol=(1e300, 1e-8),
+                                               max_iter=500, gap_min=1e-5, auto_shift=1,
+                                               orth=orth, args=args)
+        print(f"{name}: n={A.n} nconv={nc} niter={it} {time.time() - t:.1f}s", file=sys.stderr,
+              flush=True)
+        meta["solve"][name] = dict(n=A.n, nev=nev, block_size=bs, nev_init=ni, nev_max=nm,
+                                   orth=None if orth is None else list(orth), args=list(args),
+                                   tol=[1e300, 1e-8], auto_shift=1, gap_min=1e-5, max_iter=500,
+                                   x0_seed=1, nconv=nc, niter=it,
+                                   eval=[float(v) for v in ev], ref_seconds=sec)
+    with open(os.path.join(HERE, "golden_orth.json"), "w") as f:
+        json.dump(meta, f, indent=1)
+    np.savez_compressed(os.path.join(HERE, "golden_orth.npz"), **arrays)
+
+
+if __name__ == "__main__":
+    main()

@@ -83,3 +83,57 @@ def test_oracle_matches_live_reference_on_new_input():
     r = gcg_solve(A.to_scipy(), B.to_scipy(), X0, 10, 3, 9, 19)
     assert nc >= 10 and r.nconv >= 10
     assert np.max(np.abs(ev[:10] - r.eval[:10]) / np.abs(ev[:10])) < 1e-10
+
+
+# ---------------------------------------------------------------------------
+# Binary Gram-Schmidt (src/ops_orth.c:416-641) and ComputeW12
+# (src/ops_eig_sol_gcg.c:703-929) against the reference's outputs
+# ---------------------------------------------------------------------------
+ORTH_CASES = ["mleaf_plain", "mleaf_prefix_diagB_zero", "mleaf_near_prefix", "mleaf_prefix_dep",
+              "evp_plain", "evp_prefix_diagB_dep", "evp_wide_massB_zero", "evp_prefix_zero"]
+
+
+@pytest.mark.parametrize("case", ORTH_CASES)
+def test_oracle_bgs_matches_reference_fixture(case, golden_orth):
+    import scipy.sparse as sp
+    from conftest import b_projector, orth_case
+    x, start, end, bs, B = orth_case(case)
+    meta = golden_orth["orth"][f"{case}/bgs"]
+    ref = golden_orth["arrays"][f"{case}/bgs"]
+    Bs = None if B is None else B.to_scipy()
+    o = GCGOracle(sp.identity(x.shape[0], format="csr"), Bs,
+                  GCGParams(nev_init=1, nev_max=1, block_size=1, orth_method="bgs",
+                            orth_block_size=bs))
+    got_end = o.bgs(x, start, end, Bs)
+    assert got_end == meta["end"]
+    X = x[:, :got_end]
+    G = X.T @ (X if Bs is None else Bs @ X)
+    assert np.abs(G - np.eye(got_end)).max() < 1e-13
+    # the same subspace; leaves of OrthSelf (blocks under 16 columns) also the same basis
+    tol = 5e-9 if "near" in case else 1e-13
+    assert np.abs(b_projector(X, Bs) - b_projector(ref, Bs)).max() < tol
+    if case.startswith("mleaf"):
+        assert np.abs(X - ref).max() < tol
+
+
+SOLVE_CASES_CPU = ["laplace2d_24x24_nev8_bgs", "aniso2d_40x30_eps10_diagB_bgs",
+                   "laplace2d_24x24_nev8_w12", "aniso2d_40x30_eps10_diagB_w12",
+                   "aniso2d_40x30_eps10_diagB_w12_bgs"]
+
+
+@pytest.mark.parametrize("case", SOLVE_CASES_CPU)
+def test_oracle_orth_and_w12_solves_match_reference_fixture(case, golden_orth):
+    from conftest import orth_solve_case
+    g = golden_orth["solve"][case]
+    A, B = orth_solve_case(case)
+    X0 = P.initial_block(A.n, g["nev_init"], seed=g["x0_seed"])
+    r = gcg_solve(A.to_scipy(), None if B is None else B.to_scipy(), X0, g["nev"], g["block_size"],
+                  g["nev_init"], g["nev_max"], tol=tuple(g["tol"]), max_iter=g["max_iter"],
+                  gap_min=g["gap_min"], auto_shift=g["auto_shift"],
+                  orth=None if g["orth"] is None else tuple(g["orth"]),
+                  w_order=2 if "-gcge_compW_cg_order" in g["args"] else 1)
+    nev = g["nev"]
+    ref = np.array(g["eval"][:nev])
+    assert r.nconv >= nev
+    assert np.max(np.abs(r.eval[:nev] - ref) / np.abs(ref)) < 1e-10
+    assert abs(r.niter - g["niter"]) <= max(3, g["niter"] // 5)
