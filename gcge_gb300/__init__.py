@@ -43,6 +43,8 @@ EXPORTED_SYMBOLS = [
     "GCGE_TimerStart", "GCGE_TimerStop", "GCGE_GramNoAlloc", "GCGE_DenseGram",
     "GCGE_DenseLinComb", "GCGE_HostAlloc", "GCGE_HostFree", "GCGE_ServerCreate",
     "GCGE_ServerSubmit", "GCGE_ServerWait", "GCGE_ServerDestroy", "GCGE_SolveBatch",
+    "MultiVecOrthSetup_ModifiedGramSchmidt", "MultiVecOrthSetup_BinaryGramSchmidt",
+    "EigenSolverSetParametersFromCommandLine_GCG",
 ]
 
 _lib = None
@@ -211,6 +213,72 @@ def solve(A, B, nev, block_size, nev_init, nev_max, X0=None, tol=(1e300, 1e-8), 
     if st not in (GCGE_OK, GCGE_ERR_NOT_CONVERGED):
         raise GCGEError(st, "GCGE_Solve")
     return SolveResult(ev, evec, info.nconv, info.niter, st, info.as_dict())
+
+
+def solve_ops(A, B, nev, block_size, nev_init, nev_max, X0=None, tol=(1e300, 1e-8), max_iter=500,
+              gap_min=1e-5, auto_shift=1, precision=PREC_FP64, orth=None,
+              args=(), linear_solver=None) -> SolveResult:
+    """One GCG solve driven slot by slot through the OPS entry points, in the
+    order of the reference's front end (gcge.c:490-531): OPS_CUDA_Set,
+    MultiVecCreateByMat for evec, GCGE_Create, EigenSolverSetup_GCG,
+    GCGE_Setparameters, then ops->EigenSolver.  orth = (method, block_size),
+    e.g. ("bgs", -1), selects the orthogonalisation of InitializeX and
+    ComputeW through EigenSolverSetParameters_GCG (src/ops_eig_sol_gcg.c:1684-1741);
+    args, e.g. ("-gcge_compW_cg_order", "2"), then go through
+    EigenSolverSetParametersFromCommandLine_GCG (:1743-1862).  linear_solver,
+    a Python callable (mat, b, x, start, end, ops) with start/end int[2], is
+    installed as ops->MultiLinearSolver for -gcge_user_defined_multi_lin_sol
+    1 or 2 (:590-592)."""
+    ops = CudaOps()
+    lib = ops.lib
+    try:
+        hA = ops.mat(A)
+        hB = ops.mat(B) if B is not None else None
+        evec = ops.multivec(hA, nev_max)
+        ng = 0
+        if X0 is not None:
+            ops.upload(evec, X0)
+            ng = X0.shape[1]
+        mv_ws = (_VP * 4)()
+        lib.GCGE_Create(hA, ctypes.c_int(nev_max), ctypes.c_int(block_size), ctypes.c_int(nev_init),
+                        mv_ws, None, None, ops.ptr)
+        ops.check("GCGE_Create")
+        t = (ctypes.c_double * 2)(*tol)
+        lib.EigenSolverSetup_GCG(ctypes.c_double(gap_min), ctypes.c_int(nev_init),
+                                 ctypes.c_int(nev_max), ctypes.c_int(block_size), t,
+                                 ctypes.c_int(max_iter), 0, 0, 0, mv_ws, None, None, ops.ptr)
+        lib.GCGE_Setparameters(ctypes.c_double(gap_min), ctypes.c_int(auto_shift), ops.ptr)
+        if orth is not None:
+            m, bs = orth[0].encode(), ctypes.c_int(orth[1])
+            z = ctypes.c_double(0.0)
+            lib.EigenSolverSetParameters_GCG(0, m, bs, -1, z, None, -1, -1, z, m, bs, -1, z, 0, z, z,
+                                             None, ctypes.c_int(auto_shift), 0, z, z, ops.ptr)
+        if args:
+            argv = (ctypes.c_char_p * len(args))(*[a.encode() for a in args])
+            lib.EigenSolverSetParametersFromCommandLine_GCG(ctypes.c_int(len(args)), argv, ops.ptr)
+        st = lib.GCGE_SetPrecision(ops.ptr, ctypes.c_int(precision))
+        if st != GCGE_OK:
+            raise GCGEError(st, "GCGE_SetPrecision")
+        ops.check("GCG setup")
+        if linear_solver is not None:
+            cb = _LINSOL(linear_solver)
+            ops._keep = cb
+            ops.ptr.contents.MultiLinearSolver = ctypes.cast(cb, _VP)
+        ev = np.zeros(nev_max)
+        nconv = ctypes.c_int(nev)
+        ops._fn("EigenSolver")(hA, hB, ev.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), evec, ng,
+                               ctypes.byref(nconv), ctypes.cast(ops.ptr, _VP))
+        err = lib.ops_cuda_last_error()
+        if err != GCGE_OK:
+            raise GCGEError(err, "ops->EigenSolver")
+        info = SolveInfo()
+        lib.GCGE_GetSolveInfo(ops.ptr, ctypes.byref(info))
+        X = ops.download(evec, 0, nev_max)
+        lib.GCGE_Destroymvws(mv_ws, None, None, ctypes.c_int(nev_max), ctypes.c_int(block_size),
+                             ops.ptr)
+        return SolveResult(ev, X, nconv.value, info.niter, info.status, info.as_dict())
+    finally:
+        ops.close()
 
 
 class Prepared:
@@ -393,7 +461,16 @@ _FT = {
                                      ctypes.c_int, _I2, _I2, ctypes.POINTER(ctypes.c_double),
                                      ctypes.c_int, _VP, _VP),
     "MultiVecSetRandomValue": ctypes.CFUNCTYPE(None, _VP, ctypes.c_int, ctypes.c_int, _VP),
+    "MultiVecOrth": ctypes.CFUNCTYPE(None, _VP, ctypes.c_int, ctypes.POINTER(ctypes.c_int), _VP,
+                                     _VP),
+    "EigenSolver": ctypes.CFUNCTYPE(None, _VP, _VP, ctypes.POINTER(ctypes.c_double), _VP,
+                                    ctypes.c_int, ctypes.POINTER(ctypes.c_int), _VP),
 }
+
+
+# ops->MultiLinearSolver (src/ops.h:121-122)
+_LINSOL = ctypes.CFUNCTYPE(None, _VP, _VP, _VP, ctypes.POINTER(ctypes.c_int),
+                           ctypes.POINTER(ctypes.c_int), _VP)
 
 
 class CudaOps:
@@ -494,6 +571,23 @@ class CudaOps:
                                  ctypes.cast(self.ptr, _VP))
         self.check("MultiVecQtAP")
         return out
+
+    def orth_setup(self, method="bgs", block_size=-1, max_reorth=2,
+                   zero_tol=2 * np.finfo(float).eps):
+        """MultiVecOrthSetup_BinaryGramSchmidt / _ModifiedGramSchmidt
+        (src/ops_orth.c:395-414, :625-641): installs ops->MultiVecOrth."""
+        fn = {"bgs": self.lib.MultiVecOrthSetup_BinaryGramSchmidt,
+              "mgs": self.lib.MultiVecOrthSetup_ModifiedGramSchmidt}[method]
+        fn(ctypes.c_int(block_size), ctypes.c_int(max_reorth), ctypes.c_double(zero_tol), None,
+           None, self.ptr)
+        self.check("MultiVecOrthSetup")
+
+    def orth(self, x, start, end, B=None):
+        """ops->MultiVecOrth(x, start, &end, B): returns the new end."""
+        e = ctypes.c_int(end)
+        self._fn("MultiVecOrth")(x, start, ctypes.byref(e), B, ctypes.cast(self.ptr, _VP))
+        self.check("MultiVecOrth")
+        return e.value
 
     def set_random(self, x, start, end):
         self._fn("MultiVecSetRandomValue")(x, start, end, ctypes.cast(self.ptr, _VP))

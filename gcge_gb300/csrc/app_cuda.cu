@@ -13,6 +13,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <mutex>
+#include <unordered_map>
 
 #include "gcg.cuh"
 
@@ -524,6 +525,77 @@ static int default_option(const char *name, char type, void *value, int argc, ch
     return 0;
 }
 
+// ---------------------------------------------------------------- MultiVecOrth
+// State behind ops->orth_workspace after MultiVecOrthSetup_*: the method, its
+// parameters and the device work buffers of the orthogonalisation.
+struct OrthSetup {
+    bool bgs = false;
+    int block_size = -1, max_reorth = 1;
+    double zero_tol = 1e-14;
+    SolverCtx work;
+};
+static std::mutex g_orth_mu;
+static std::unordered_map<OPS *, OrthSetup *> g_orth;
+
+static OrthSetup *orth_for(OPS *ops, bool create) {
+    std::lock_guard<std::mutex> lk(g_orth_mu);
+    auto it = g_orth.find(ops);
+    if (it != g_orth.end()) return it->second;
+    if (!create) return nullptr;
+    OrthSetup *o = new OrthSetup();
+    g_orth[ops] = o;
+    return o;
+}
+static void orth_release(OPS *ops) {
+    OrthSetup *o = nullptr;
+    {
+        std::lock_guard<std::mutex> lk(g_orth_mu);
+        auto it = g_orth.find(ops);
+        if (it == g_orth.end()) return;
+        o = it->second;
+        g_orth.erase(it);
+    }
+    delete o;
+}
+
+// ops->MultiVecOrth (src/ops_orth.c:203-394 "mgs", :519-623 "bgs"): columns
+// [start_x, *end_x) of x B-orthonormalised against [0, start_x) and among
+// themselves; *end_x shrinks by the columns dropped as dependent.
+static void cuda_multivec_orth(void **x, int start_x, int *end_x, void *B, OPS *ops) {
+    try {
+        OrthSetup *o = orth_for(ops, false);
+        GCGE_REQUIRE(o && ops->orth_workspace == (void *)o, GCGE_ERR_ARG,
+                     "MultiVecOrth: no MultiVecOrthSetup_* on this ops");
+        MultiVec *xv = as_mv(x);
+        SparseMat *Bm = B ? as_mat(B) : nullptr;
+        GCGE_REQUIRE(xv && end_x && (!B || Bm), GCGE_ERR_HANDLE, "MultiVecOrth: handles");
+        GCGE_REQUIRE(start_x >= 0 && *end_x >= start_x && *end_x <= xv->ncols, GCGE_ERR_ARG,
+                     "MultiVecOrth: range");
+        GCGE_REQUIRE(!Bm || Bm->n == xv->nrows, GCGE_ERR_ARG, "MultiVecOrth: B size");
+        if (*end_x == start_x) return;
+        o->work.reserve(xv->nrows, xv->ncols, xv->ncols, 1, 1);
+        if (o->bgs)
+            *end_x = bgs_orth(o->work, Bm, xv->data, xv->ld, xv->nrows, start_x, *end_x,
+                              Bm != nullptr, o->zero_tol, o->max_reorth, o->block_size, nullptr);
+        else
+            *end_x = borth(o->work, Bm, xv->data, xv->ld, xv->nrows, start_x, *end_x, Bm != nullptr,
+                           o->zero_tol, o->max_reorth, nullptr);
+        GCGE_CUDA(cudaStreamSynchronize(lib_stream()));
+    } catch (const CudaError &e) {
+        set_error(e.status, e.where.c_str());
+    }
+}
+
+static void orth_setup(bool bgs, int block_size, int max_reorth, double orth_zero_tol, OPS *ops) {
+    OrthSetup *o = orth_for(ops, true);
+    o->bgs = bgs;
+    o->block_size = block_size;
+    o->max_reorth = max_reorth;
+    o->zero_tol = orth_zero_tol;
+    ops->orth_workspace = (void *)o;
+    ops->MultiVecOrth = cuda_multivec_orth;
+}
+
 static void init_solver_defaults(GCGSolver &g) {
     // static defaults of EigenSolverSetup_GCG (src/ops_eig_sol_gcg.c:1573-1603)
     std::memset(&g, 0, sizeof(g));
@@ -583,10 +655,27 @@ void OPS_Setup(OPS *ops) {
 }
 void OPS_Destroy(OPS **ops) {
     if (!ops || !*ops) return;
+    orth_release(*ops);
     ctx_release(*ops);
     if ((*ops)->lapack_ops) OPS_Destroy(&(*ops)->lapack_ops);
     free(*ops);
     *ops = nullptr;
+}
+
+// src/ops_orth.c:395-414 (mgs) and :625-641 (bgs).  mv_ws and dbl_ws are
+// accepted for signature compatibility; the device work buffers belong to the
+// ops object and are freed by OPS_Destroy.
+void MultiVecOrthSetup_ModifiedGramSchmidt(int block_size, int max_reorth, double orth_zero_tol,
+                                           void **mv_ws, double *dbl_ws, OPS *ops) {
+    (void)mv_ws;
+    (void)dbl_ws;
+    orth_setup(false, block_size, max_reorth, orth_zero_tol, ops);
+}
+void MultiVecOrthSetup_BinaryGramSchmidt(int block_size, int max_reorth, double orth_zero_tol,
+                                         void **mv_ws, double *dbl_ws, OPS *ops) {
+    (void)mv_ws;
+    (void)dbl_ws;
+    orth_setup(true, block_size, max_reorth, orth_zero_tol, ops);
 }
 
 void OPS_CUDA_Set(OPS *ops) {
@@ -710,10 +799,12 @@ void EigenSolverSetup_GCG(double gapMin, int nevInit, int nevMax, int block_size
                           int numIterMax, int print, int printtime,
                           int user_defined_multi_linear_solver, void **mv_ws[4], double *dbl_ws,
                           int *int_ws, OPS *ops) {
-    bool fresh = ctx_for(ops, false) == nullptr;
     SolverCtx *c = ctx_for(ops, true);
     GCGSolver &g = c->pub;
-    if (fresh) init_solver_defaults(g);
+    if (!c->pub_init) {
+        init_solver_defaults(g);
+        c->pub_init = true;
+    }
     g.gapMin = gapMin;
     g.nevInit = nevInit;
     g.nevMax = nevMax;
@@ -773,6 +864,63 @@ void EigenSolverSetParameters_GCG(
     if (compRR_min_gap > 0) g.compRR_min_gap = compRR_min_gap;
     if (compRR_min_num > 0) g.compRR_min_num = compRR_min_num;
     if (compRR_tol > 0) g.compRR_tol = compRR_tol;
+}
+
+// src/ops_eig_sol_gcg.c:1743-1862: every "-gcge_*" option present in argv
+// overrides its parameter, read with ops->GetOptionFromCommandLine.  Option
+// names and types are the reference's, with two exceptions: -gcge_compRR_min_gap
+// is read as a double (the reference reads an int into the double), and the
+// reference's "-gcge_compRR_tol    " carries four trailing spaces, kept here,
+// so a plain -gcge_compRR_tol is ignored by both.  String values longer than
+// the 7 characters of the solver's fields are cut.  The usage table the
+// reference prints is not printed.
+void EigenSolverSetParametersFromCommandLine_GCG(int argc, char *argv[], OPS *ops) {
+    SolverCtx *c = ctx_for(ops, false);
+    if (!c || !ops->GetOptionFromCommandLine) {
+        set_error(GCGE_ERR_ARG,
+                  "EigenSolverSetParametersFromCommandLine_GCG before EigenSolverSetup_GCG");
+        return;
+    }
+    GCGSolver &g = c->pub;
+    auto opt = [&](const char *name, char type, void *v) {
+        ops->GetOptionFromCommandLine(name, type, v, argc, argv, ops);
+    };
+    auto opt_s = [&](const char *name, char *dst) {
+        char buf[256] = {0};
+        if (ops->GetOptionFromCommandLine(name, 's', buf, argc, argv, ops)) {
+            std::strncpy(dst, buf, 7);
+            dst[7] = 0;
+        }
+    };
+    opt("-gcge_min_gap", 'f', &g.gapMin);
+    opt("-gcge_given_nevec", 'i', &g.nevGiven);
+    opt("-gcge_max_niter", 'i', &g.numIterMax);
+    opt("-gcge_abs_tol", 'f', &g.tol[0]);
+    opt("-gcge_rel_tol", 'f', &g.tol[1]);
+    opt("-gcge_user_defined_multi_lin_sol", 'i', &g.user_defined_multi_linear_solver);
+    opt_s("-gcge_initX_orth_method", g.initX_orth_method);
+    opt("-gcge_initX_orth_block_size", 'i', &g.initX_orth_block_size);
+    opt("-gcge_initX_orth_max_reorth", 'i', &g.initX_orth_max_reorth);
+    opt("-gcge_initX_orth_zero_tol", 'f', &g.initX_orth_zero_tol);
+    opt("-gcge_check_conv_max_num", 'i', &g.check_conv_max_num);
+    opt_s("-gcge_compP_orth_method", g.compP_orth_method);
+    opt("-gcge_compP_orth_block_size", 'i', &g.compP_orth_block_size);
+    opt("-gcge_compP_orth_max_reorth", 'i', &g.compP_orth_max_reorth);
+    opt("-gcge_compP_orth_zero_tol", 'f', &g.compP_orth_zero_tol);
+    opt_s("-gcge_compW_orth_method", g.compW_orth_method);
+    opt("-gcge_compW_orth_block_size", 'i', &g.compW_orth_block_size);
+    opt("-gcge_compW_orth_max_reorth", 'i', &g.compW_orth_max_reorth);
+    opt("-gcge_compW_orth_zero_tol", 'f', &g.compW_orth_zero_tol);
+    opt("-gcge_compW_cg_max_iter", 'i', &g.compW_cg_max_iter);
+    opt("-gcge_compW_cg_rate", 'f', &g.compW_cg_rate);
+    opt("-gcge_compW_cg_tol", 'f', &g.compW_cg_tol);
+    opt_s("-gcge_compW_cg_tol_type", g.compW_cg_tol_type);
+    opt("-gcge_compW_cg_auto_shift", 'i', &g.compW_cg_auto_shift);
+    opt("-gcge_compW_cg_shift", 'f', &g.compW_cg_shift);
+    opt("-gcge_compW_cg_order", 'i', &g.compW_cg_order);
+    opt("-gcge_compRR_min_num", 'i', &g.compRR_min_num);
+    opt("-gcge_compRR_min_gap", 'f', &g.compRR_min_gap);
+    opt("-gcge_compRR_tol    ", 'f', &g.compRR_tol);
 }
 
 void GCGE_Setparameters(double gapMin, int shift, OPS *ops) {

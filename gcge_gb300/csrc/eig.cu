@@ -306,6 +306,25 @@ static void host_jacobi(int n, std::vector<double> &a, std::vector<double> &v) {
     }
 }
 
+void host_eigh(int n, const double *G, double *w, double *V) {
+    std::vector<double> a(G, G + (size_t)n * n), v;
+    for (int i = 0; i < n; ++i)  // symmetrise (column-major in, row-major work)
+        for (int j = 0; j < i; ++j) {
+            const double m = 0.5 * (a[(size_t)i * n + j] + a[(size_t)j * n + i]);
+            a[(size_t)i * n + j] = a[(size_t)j * n + i] = m;
+        }
+    host_jacobi(n, a, v);
+    std::vector<int> ord(n);
+    for (int i = 0; i < n; ++i) ord[i] = i;
+    std::stable_sort(ord.begin(), ord.end(), [&](int x, int y) {
+        return a[(size_t)x * n + x] < a[(size_t)y * n + y];
+    });
+    for (int j = 0; j < n; ++j) {
+        w[j] = a[(size_t)ord[j] * n + ord[j]];
+        for (int i = 0; i < n; ++i) V[i + (size_t)j * n] = v[(size_t)i * n + ord[j]];
+    }
+}
+
 // Eigen-decomposition of the symmetric s x s matrix M (device, ld) into
 // ascending eigenvalues eval (host) and eigenvectors Z (device, ldz).
 //

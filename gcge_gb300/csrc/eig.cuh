@@ -19,6 +19,12 @@ struct EigWork {
 size_t jacobi_smem_bytes(int s);
 int jacobi_max_dim();
 
+// Eigenpairs of a small symmetric n x n matrix G on the host (column-major):
+// ascending eigenvalues w, orthonormal eigenvectors in the columns of V
+// (column-major n x n).  FP64 cyclic Jacobi; an exactly zero row of G gives an
+// exactly zero eigenvalue.
+void host_eigh(int n, const double *G, double *w, double *V);
+
 // Eigenpairs of the symmetric s x s matrix M (device, leading dim ld):
 // ascending eigenvalues to eval_host, orthonormal eigenvectors to Z
 // (device, ldz).  refine_steps Ogita-Aishima steps follow the FP32 Jacobi.

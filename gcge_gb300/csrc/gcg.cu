@@ -261,6 +261,210 @@ int borth(SolverCtx &c, SparseMat *B, double *x, int ldx, int nrows, int start, 
     return start + k;
 }
 
+// ---------------------------------------------------------------- BGS
+// BinaryGramSchmidt (src/ops_orth.c:416-641): classical Gram-Schmidt of the
+// new columns against the prefix, then recursive halving; the leaves are
+// orthonormalised column by column (OrthSelf, :45-118) when the whole block
+// has fewer than 16 columns, else by the eigen-decomposition of their Gram
+// matrix (OrthSelfEVP, :122-201).  Tall products run on the device, the leaf
+// decisions (drops, eigen-decompositions of k x k Gram matrices) on the host.
+struct BgsOrth {
+    SolverCtx &c;
+    SparseMat *B;
+    int nrows;
+    bool useB;
+    double zero_tol;
+    int max_reorth;
+    int block_size;
+    int *spmm_calls;
+    cudaStream_t st;
+    bool evp = true;  // leaf method: OrthSelfEVP (true) or OrthSelf
+    static constexpr double kReorthTol = 50.0 * 2.220446049250313e-16;  // src/ops_orth.c:631
+
+    void applyB(const double *X, int lx, double *Y, int ly, int k) {
+        if (k <= 0) return;
+        if (B) {
+            spmm<double>(B->pat, B->val.p, X, lx, Y, ly, k, st);
+            if (spmm_calls) ++*spmm_calls;
+        } else {
+            copy_cols(nrows, k, X, lx, Y, ly, st);
+        }
+    }
+    double absmax_dev(int m, int w, const double *C, int ldc) {
+        absmax(m, w, C, ldc, c.dmax.p, st);
+        GCGE_CUDA(cudaMemcpyAsync(c.hmax.p, c.dmax.p, sizeof(double), cudaMemcpyDeviceToHost, st));
+        GCGE_CUDA(cudaStreamSynchronize(st));
+        return c.hmax.p[0];
+    }
+    // X1 -= X0 (X0^T B X1), up to 1 + max_reorth passes, until the
+    // coefficients fall below the reorthogonalisation tolerance; B X0 is formed
+    // once (:446-481)
+    void cgs(double *X0, int n0, double *X1, int n1, int ldx) {
+        if (n0 <= 0 || n1 <= 0) return;
+        const double *BX0 = X0;
+        int ldb = ldx;
+        if (useB) {
+            applyB(X0, ldx, c.T2.p, c.ld, n0);
+            BX0 = c.T2.p;
+            ldb = c.ld;
+        }
+        for (int pass = 0; pass < 1 + max_reorth; ++pass) {
+            dgram(c, nrows, n0, n1, BX0, ldb, X1, ldx, c.dC.p, n0, c.gscr.p, c.gscr.n, st);
+            dlincomb(c, nrows, n0, n1, X0, ldx, c.dC.p, n0, X1, ldx, c.one.p, 0, st, -1.0);
+            if (absmax_dev(n0, n1, c.dC.p, n0) < kReorthTol) break;
+        }
+    }
+    // OrthSelf: column by column, normalise x_k by its B-norm (drop it, moving
+    // the last column into its place, when the norm is below the zero
+    // tolerance) and remove it from the later columns
+    int self_mgs(double *x, int ldx, int lo, int hi) {
+        for (int k = lo; k < hi; ++k) {
+            double *xk = x + (size_t)k * ldx;
+            const double *Bxk = xk;
+            int ldb = ldx;
+            if (useB) {
+                applyB(xk, ldx, c.T2.p, c.ld, 1);
+                Bxk = c.T2.p;
+                ldb = c.ld;
+            }
+            const int len = hi - k;
+            dgram(c, nrows, len, 1, xk, ldx, Bxk, ldb, c.dC.p, len, c.gscr.p, c.gscr.n, st);
+            GCGE_CUDA(cudaMemcpyAsync(c.hbuf.p, c.dC.p, sizeof(double) * len,
+                                      cudaMemcpyDeviceToHost, st));
+            GCGE_CUDA(cudaStreamSynchronize(st));
+            const double r = std::sqrt(c.hbuf.p[0]);  // NaN (kept) for a negative square
+            if (r < zero_tol) {
+                if (k < hi - 1) copy_cols(nrows, 1, x + (size_t)(hi - 1) * ldx, ldx, xk, ldx, st);
+                --k;
+                --hi;
+                continue;
+            }
+            const double inv = 1.0 / r;
+            double *hc = c.hbuf.p + len;  // [1/r, coefficients of the later columns]
+            hc[0] = inv;
+            for (int i = 1; i < len; ++i) hc[i] = c.hbuf.p[i] * -inv;
+            GCGE_CUDA(cudaMemcpyAsync(c.dC.p, hc, sizeof(double) * len, cudaMemcpyHostToDevice, st));
+            scale_columns(nrows, 1, xk, ldx, c.dC.p, st);
+            if (len > 1)
+                dlincomb(c, nrows, 1, len - 1, xk, ldx, c.dC.p + 1, 1, xk + ldx, ldx, c.one.p, 0, st);
+            // further passes against x_k (:93-113; none for max_reorth <= 2)
+            for (int idx = 1; idx < max_reorth - 1 && len > 1; ++idx) {
+                if (useB) applyB(xk, ldx, c.T2.p, c.ld, 1);
+                dgram(c, nrows, len - 1, 1, xk + ldx, ldx, Bxk, ldb, c.dC.p, len - 1, c.gscr.p,
+                      c.gscr.n, st);
+                const double amax = absmax_dev(len - 1, 1, c.dC.p, len - 1);
+                dlincomb(c, nrows, 1, len - 1, xk, ldx, c.dC.p, 1, xk + ldx, ldx, c.one.p, 0, st,
+                         -1.0);
+                if (amax < kReorthTol) break;
+            }
+            GCGE_CUDA(cudaStreamSynchronize(st));  // the host buffer is reused next column
+        }
+        return hi;
+    }
+    // OrthSelfEVP: X <- X V diag(w^-1/2) from G = X^T B X = V diag(w) V^T
+    // (ascending), eigenvalues of magnitude at most the zero tolerance dropped
+    int self_evp(double *x, int ldx, int lo, int hi) {
+        for (int pass = 0; pass < 1 + max_reorth; ++pass) {
+            const int k = hi - lo;
+            if (k <= 0) return hi;
+            double *X = x + (size_t)lo * ldx;
+            const double *BX = X;
+            int ldb = ldx;
+            if (useB) {
+                applyB(X, ldx, c.T2.p, c.ld, k);
+                BX = c.T2.p;
+                ldb = c.ld;
+            }
+            dgram(c, nrows, k, k, X, ldx, BX, ldb, c.dC.p, k, c.gscr.p, c.gscr.n, st);
+            GCGE_CUDA(cudaMemcpyAsync(c.hbuf.p, c.dC.p, sizeof(double) * k * k,
+                                      cudaMemcpyDeviceToHost, st));
+            GCGE_CUDA(cudaStreamSynchronize(st));
+            for (int i = 0; i < k * k; ++i)
+                GCGE_REQUIRE(std::isfinite(c.hbuf.p[i]), GCGE_ERR_NUMERIC,
+                             "orth: non-finite Gram matrix");
+            std::vector<double> w(k), V((size_t)k * k);
+            host_eigh(k, c.hbuf.p, w.data(), V.data());
+            int lin_dep = 0;
+            double wsum = 0.0;
+            for (int j = 0; j < k; ++j) {
+                if (std::fabs(w[j]) > zero_tol)
+                    w[j] = 1.0 / std::sqrt(w[j]);
+                else
+                    ++lin_dep;
+                wsum += std::fabs(w[j]);
+            }
+            const int kk = k - lin_dep;  // ascending: the dropped ones come first
+            double *Cf = c.hbuf.p + (size_t)k * k;
+            for (int j = 0; j < kk; ++j)
+                for (int i = 0; i < k; ++i)
+                    Cf[i + (size_t)j * k] = V[i + (size_t)(lin_dep + j) * k] * w[lin_dep + j];
+            if (kk > 0) {
+                GCGE_CUDA(cudaMemcpyAsync(c.dC.p, Cf, sizeof(double) * k * kk,
+                                          cudaMemcpyHostToDevice, st));
+                dlincomb(c, nrows, k, kk, X, ldx, c.dC.p, k, c.T1.p, c.ld, nullptr, 0, st);
+                copy_cols(nrows, kk, c.T1.p, c.ld, X, ldx, st);
+            }
+            GCGE_CUDA(cudaStreamSynchronize(st));  // the host buffer is reused next pass
+            hi = lo + kk;
+            if (lin_dep == 0 && std::fabs(wsum - k) < kReorthTol) break;
+        }
+        return hi;
+    }
+    // OrthBinary (:416-518)
+    int binary(double *x, int ldx, int lo, int hi) {
+        if (hi <= lo) return hi;
+        const int ncols = hi - lo;
+        if (ncols <= block_size) return evp ? self_evp(x, ldx, lo, hi) : self_mgs(x, ldx, lo, hi);
+        const int mid = lo + ncols / 2;
+        const int end0 = binary(x, ldx, lo, mid);
+        cgs(x + (size_t)lo * ldx, end0 - lo, x + (size_t)mid * ldx, hi - mid, ldx);
+        const int end1 = binary(x, ldx, mid, hi);
+        const int gap = mid - end0;
+        const int len = std::min(gap, end1 - mid);
+        if (len > 0) {  // refill the gap with the last columns of the second half
+            copy_cols(nrows, len, x + (size_t)(end1 - len) * ldx, ldx, c.T1.p, c.ld, st);
+            copy_cols(nrows, len, c.T1.p, c.ld, x + (size_t)end0 * ldx, ldx, st);
+        }
+        return end1 - gap;
+    }
+    int run(double *x, int ldx, int start, int end) {
+        if (end <= start) return end;
+        // against the prefix (:540-561): coefficients checked every pass
+        if (start > 0) {
+            const int k = end - start;
+            double *X1 = x + (size_t)start * ldx;
+            for (int pass = 0; pass < 1 + max_reorth; ++pass) {
+                const double *BX1 = X1;
+                int ldb = ldx;
+                if (useB) {
+                    applyB(X1, ldx, c.T2.p, c.ld, k);
+                    BX1 = c.T2.p;
+                    ldb = c.ld;
+                }
+                dgram(c, nrows, start, k, x, ldx, BX1, ldb, c.dC.p, start, c.gscr.p, c.gscr.n, st);
+                dlincomb(c, nrows, start, k, x, ldx, c.dC.p, start, X1, ldx, c.one.p, 0, st, -1.0);
+                if (absmax_dev(start, k, c.dC.p, start) < kReorthTol) break;
+            }
+        }
+        // leaf method and size (:575-591): under 16 columns OrthSelf with leaves of
+        // 4 (or the given size), else OrthSelfEVP with leaves of at most a quarter
+        const int k = end - start;
+        if (k < 16) {
+            if (block_size <= 0) block_size = 4;
+            evp = false;
+        } else {
+            if (block_size <= 0 || block_size > k / 4) block_size = k / 4;
+            evp = true;
+        }
+        return binary(x, ldx, start, end);
+    }
+};
+
+int bgs_orth(SolverCtx &c, SparseMat *B, double *x, int ldx, int nrows, int start, int end,
+             bool useB, double zero_tol, int max_reorth, int block_size, int *spmm_calls) {
+    BgsOrth o{c, B, nrows, useB, zero_tol, max_reorth, block_size, spmm_calls, lib_stream()};
+    return o.run(x, ldx, start, end);
+}
 
 // ---------------------------------------------------------------- the solve
 struct GcgRun {
@@ -279,6 +483,9 @@ struct GcgRun {
     int s_old = 0;
     double sigma = 0.0;
     int pcg_iters = 0, spmm_calls = 0;
+    // the caller's handles, for a user-defined MultiLinearSolver
+    OPS *ops = nullptr;
+    void *Ah = nullptr, **Vh = nullptr, **Rh = nullptr;
 
     GcgRun(SolverCtx &c_, SparseMat *A_, SparseMat *B_, MultiVec *V_, MultiVec *r_)
         : c(c_), g(c_.pub), A(A_), B(B_), V(V_), ritz(r_), st(lib_stream()), n(A_->n),
@@ -301,8 +508,14 @@ struct GcgRun {
         return c.hmax.p[0];
     }
 
+    // MultiVecOrth with the method the parameters select ("bgs": binary
+    // Gram-Schmidt; anything else: the GPU counterpart of modified
+    // Gram-Schmidt, src/ops_eig_sol_gcg.c:119-141, :396-419, :650-668)
     int orth(double *x, int ldx, int nrows, int start, int end, bool useB, double zero_tol,
-             int max_reorth) {
+             int max_reorth, const char *method, int block_size) {
+        if (method && std::strcmp(method, "bgs") == 0)
+            return bgs_orth(c, useB ? B : nullptr, x, ldx, nrows, start, end, useB, zero_tol,
+                            max_reorth, block_size, &spmm_calls);
         return borth(c, useB ? B : nullptr, x, ldx, nrows, start, end, useB, zero_tol, max_reorth,
                      &spmm_calls);
     }
@@ -312,12 +525,12 @@ struct GcgRun {
         timer.mark(PH_INITX);
         copy_cols(n, nevGiven, colp(ritz, 0), ritz->ld, colp(V, 0), ld, st);
         nevGiven = orth(colp(V, 0), ld, n, 0, nevGiven, B != nullptr, g.initX_orth_zero_tol,
-                        g.initX_orth_max_reorth);
+                        g.initX_orth_max_reorth, g.initX_orth_method, g.initX_orth_block_size);
         int filled = nevGiven;
         for (int attempt = 0; attempt < 4 && filled < sizeX; ++attempt) {
             fill_uniform(n, sizeX - filled, colp(V, filled), ld, 0x5eed + attempt * 7919 + filled, st);
             filled = orth(colp(V, 0), ld, n, filled, sizeX, B != nullptr, g.initX_orth_zero_tol,
-                          g.initX_orth_max_reorth);
+                          g.initX_orth_max_reorth, g.initX_orth_method, g.initX_orth_block_size);
         }
         GCGE_REQUIRE(filled == sizeX, GCGE_ERR_NUMERIC, "InitializeX: could not fill the basis");
         endX = sizeX;
@@ -464,7 +677,8 @@ struct GcgRun {
         GCGE_CUDA(cudaStreamSynchronize(st));  // hbuf reuse
         // small-space orthonormalisation against the X coefficients (B = I)
         const int endP_local = orth(wk, s, s, base, base + np, false, g.compP_orth_zero_tol,
-                                    g.compP_orth_max_reorth);
+                                    g.compP_orth_max_reorth, g.compP_orth_method,
+                                    g.compP_orth_block_size);
         np = endP_local - base;
         startP = base + sizeC;
         endP = endP_local + sizeC;
@@ -507,15 +721,45 @@ struct GcgRun {
         shift_values(c.upat.padded, c.ua.p, c.ub.p, sigma, c.us64.p, mixed ? c.us32.p : nullptr,
                      st);
         timer.mark(PH_LINSOL);
+        const int ud = g.user_defined_multi_linear_solver;
+        if (ud == 1 || ud == 2) {
+            // the caller's solver (:590-592) on b = (lambda + sigma) B x, which
+            // the reference keeps in the Ritz-vector columns [offset[1], +bsz)
+            // (:484, :527), solving into V[:, startW:endW]
+            GCGE_REQUIRE(ops && ops->MultiLinearSolver, GCGE_ERR_ARG,
+                         "ComputeW: user_defined_multi_linear_solver without MultiLinearSolver");
+            GCGE_REQUIRE(g.compW_cg_auto_shift == 0, GCGE_ERR_ARG,  // (:503)
+                         "ComputeW: a user-defined solver excludes the automatic shift");
+            copy_cols(n, bsz, c.bbuf.p, ld, colp(ritz, offset[1]), ritz->ld, st);
+            GCGE_CUDA(cudaStreamSynchronize(st));
+            int s2[2] = {offset[1], startW}, e2[2] = {offset[1] + bsz, endW};
+            ops->MultiLinearSolver(Ah, Rh, Vh, s2, e2, ops);
+            const int err = take_error();
+            if (err != GCGE_OK) throw CudaError{err, "ComputeW: user-defined MultiLinearSolver"};
+            // BlockPCG after it (ud == 2) starts from its x with its b
+            copy_cols(n, bsz, colp(ritz, offset[1]), ritz->ld, c.bbuf.p, ld, st);
+        }
+        if (ud != 1) w_solve(colp(V, startW), bsz, mixed);
+        timer.mark(PH_W);
+        endW = orth(colp(V, 0), ld, n, startW, endW, B != nullptr, g.compW_orth_zero_tol,
+                    g.compW_orth_max_reorth, g.compW_orth_method, g.compW_orth_block_size);
+        sizeW = endW - startW;
+    }
+
+    // BlockPCG on S x = b (b in c.bbuf, S = A + sigma B on the union pattern,
+    // its values already formed) for bsz columns, starting from and overwriting
+    // x (V columns, leading dimension ld).
+    void w_solve(double *x, int bsz, bool mixed) {
+        if (bsz <= 0) return;
         const bool rel = std::strcmp(g.compW_cg_tol_type, "rel") == 0;
         if (!mixed) {
             const int kp = rows_width(bsz, 8);
-            col_to_rows<double, double>(n, bsz, kp, colp(V, startW), ld, c.xr64.p, st);
+            col_to_rows<double, double>(n, bsz, kp, x, ld, c.xr64.p, st);
             col_to_rows<double, double>(n, bsz, kp, c.bbuf.p, ld, c.br64.p, st);
             block_pcg_rows<double>(c.pcg, c.upat, c.us64.p, c.br64.p, c.xr64.p, c.rr64.p,
                                    c.pr64.p, c.wr64.p, kp, bsz, g.compW_cg_max_iter,
                                    g.compW_cg_rate, g.compW_cg_tol, rel, false, st);
-            rows_to_col<double, double>(n, bsz, kp, c.xr64.p, colp(V, startW), ld, false, st);
+            rows_to_col<double, double>(n, bsz, kp, c.xr64.p, x, ld, false, st);
             spmm_calls++;  // the residual b - S x0 inside the solve
         } else {
             // CG from x0 on S x = b is CG from 0 on S d = b - S x0: the residual
@@ -523,18 +767,64 @@ struct GcgRun {
             // the Ritz vectors converge), the correction d is iterated in FP32,
             // and x = x0 + d is accumulated in FP64.
             const int kp = rows_width(bsz, 4);
-            spmm<double>(c.upat, c.us64.p, colp(V, startW), ld, c.r64.p, ld, bsz, st);
+            spmm<double>(c.upat, c.us64.p, x, ld, c.r64.p, ld, bsz, st);
             axpby(n, bsz, 1.0, c.bbuf.p, ld, -1.0, c.r64.p, ld, st);
             col_to_rows<double, float>(n, bsz, kp, c.r64.p, ld, c.br32.p, st);
             block_pcg_rows<float>(c.pcg, c.upat, c.us32.p, c.br32.p, c.xr32.p, c.rr32.p,
                                   c.pr32.p, c.wr32.p, kp, bsz, g.compW_cg_max_iter,
                                   g.compW_cg_rate, g.compW_cg_tol, rel, true, st);
-            rows_to_col<float, double>(n, bsz, kp, c.xr32.p, colp(V, startW), ld, true, st);
+            rows_to_col<float, double>(n, bsz, kp, c.xr32.p, x, ld, true, st);
             spmm_calls++;
         }
+    }
+
+    // ---------------- ComputeW12 (:703-929), compW_cg_order 2: the first half
+    // of the unconverged columns gets two W directions, the BlockPCG solution
+    // x1 of S x = b from the Ritz vectors and x2, the same solve restarted from
+    // x1 (the right-hand side is the same for both; the reference rebuilds it
+    // only because its shifted product used it as scratch).
+    void compute_w12(const std::vector<int> &offset) {
+        GCGE_REQUIRE(g.user_defined_multi_linear_solver == 0, GCGE_ERR_ARG,  // (:709)
+                     "ComputeW12 runs BlockPCG only (user_defined_multi_linear_solver must be 0)");
+        timer.mark(PH_W);
+        double sg = 0.0;
+        if (g.compW_cg_auto_shift == 1)
+            sg = -ss_eval[sizeC] + (ss_eval[sizeC + 1] - ss_eval[sizeC]) * 0.01;
+        g.sigma = g.compW_cg_shift + sg;
+        sigma = g.sigma;
+        startW = endP;
+        int total = 0;
+        for (int i = 0; i < offset[0]; ++i) total += offset[2 * i + 2] - offset[2 * i + 1];
+        const int half = total / 2;
+        int bsz = 0;
+        double *hscale = c.hbuf.p;
+        for (int i = 0; i < offset[0]; ++i) {
+            const int o1 = offset[2 * i + 1];
+            int len = offset[2 * i + 2] - o1;
+            if (bsz + len >= half) len = half - bsz;
+            copy_cols(n, len, colp(ritz, o1), ritz->ld, colp(V, startW + bsz), ld, st);
+            applyB(colp(V, o1), ld, c.bbuf.p + (size_t)bsz * ld, ld, len);
+            for (int j = 0; j < len; ++j) hscale[bsz + j] = ss_eval[o1 + j] + sigma;
+            bsz += len;
+            if (bsz >= half) break;
+        }
+        if (bsz > 0) {
+            GCGE_CUDA(cudaMemcpyAsync(c.dvec.p, hscale, sizeof(double) * bsz,
+                                      cudaMemcpyHostToDevice, st));
+            scale_columns(n, bsz, c.bbuf.p, ld, c.dvec.p, st);
+        }
+        const bool mixed = c.precision == GCGE_PREC_MIXED && !c.escalated;
+        shift_values(c.upat.padded, c.ua.p, c.ub.p, sigma, c.us64.p, mixed ? c.us32.p : nullptr,
+                     st);
+        timer.mark(PH_LINSOL);
+        w_solve(colp(V, startW), bsz, mixed);
+        endW = startW + bsz;
+        copy_cols(n, bsz, colp(V, startW), ld, colp(V, endW), ld, st);
+        w_solve(colp(V, endW), bsz, mixed);
+        endW += bsz;
         timer.mark(PH_W);
         endW = orth(colp(V, 0), ld, n, startW, endW, B != nullptr, g.compW_orth_zero_tol,
-                    g.compW_orth_max_reorth);
+                    g.compW_orth_max_reorth, g.compW_orth_method, g.compW_orth_block_size);
         sizeW = endW - startW;
     }
 
@@ -673,7 +963,10 @@ struct GcgRun {
                 compute_p(offsetP);
             }
             compute_x();
-            compute_w(offsetW);
+            if (g.compW_cg_order != 1)  // (:1456-1461)
+                compute_w12(offsetW);
+            else
+                compute_w(offsetW);
             std::swap(offsetP, offsetW);
             compute_rr(nevc);
             for (int i = sizeV; i < nevMax + 2 * bs; ++i) ss_eval[i] = ss_eval[sizeV - 1];
@@ -746,6 +1039,10 @@ void gcg_eigensolver(void *Ah, void *Bh, double *eval, void **evec, int nevGiven
         GCGE_REQUIRE(V->ld == R->ld, GCGE_ERR_ARG, "EigenSolver: leading dimensions differ");
         c->escalated = false;
         GcgRun run(*c, A, B, V, R);
+        run.ops = ops;
+        run.Ah = Ah;
+        run.Vh = c->pub.mv_ws[0];
+        run.Rh = evec;
         c->pcg.timing_reset(st);
         const int status = run.run(eval, nevGiven, nevConv);
         c->pcg.collect(st);

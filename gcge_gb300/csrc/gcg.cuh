@@ -8,6 +8,7 @@ namespace gcge {
 
 struct SolverCtx {
     GCGSolver pub;  // first member: ops->eigen_solver_workspace points here
+    bool pub_init = false;  // pub holds the EigenSolverSetup_GCG defaults
     int precision = GCGE_PREC_FP64;
     // mixed solve that fell back to FP64 for its remaining iterations (reset
     // at the start of every solve)
@@ -52,6 +53,11 @@ unsigned long long mat_serial(const SparseMat *m);
 // (blocked CGS with re-orthogonalisation + Cholesky-QR2 with dropping).
 int borth(SolverCtx &c, SparseMat *B, double *x, int ldx, int nrows, int start, int end,
           bool useB, double zero_tol, int max_reorth, int *spmm_calls);
+// Binary Gram-Schmidt of src/ops_orth.c:416-623 (CGS against the prefix, then
+// recursive halving with OrthSelf / OrthSelfEVP leaves); same arguments as
+// borth plus the leaf size (<= 0: the reference's default choice).
+int bgs_orth(SolverCtx &c, SparseMat *B, double *x, int ldx, int nrows, int start, int end,
+             bool useB, double zero_tol, int max_reorth, int block_size, int *spmm_calls);
 // Union pattern of A, B (B NULL = identity) and the diagonal, with A's and B's
 // values on it; cached on the context by matrix identity.
 void prepare_union(SolverCtx &c, SparseMat *A, SparseMat *B, cudaStream_t st);

@@ -133,6 +133,24 @@ void OPS_Create(OPS **ops);
 void OPS_Setup(OPS *ops);
 void OPS_Destroy(OPS **ops);
 
+/* MultiVecOrth setup: src/ops_orth.h:36-41, src/ops_orth.c:395-414 (modified
+ * Gram-Schmidt) and :625-641 (binary Gram-Schmidt).  Each installs the GPU
+ * orthogonalisation as ops->MultiVecOrth with its parameters in
+ * ops->orth_workspace: MultiVecOrth(x, start_x, &end_x, B, ops) B-orthonormalises
+ * columns [start_x, end_x) of a CUDA multivector against [0, start_x) and among
+ * themselves (B NULL = identity), shrinking end_x by the columns dropped as
+ * dependent (B-norm below orth_zero_tol).  The binary variant follows the
+ * reference's recursion and leaf choice (OrthSelf under 16 columns, else
+ * OrthSelfEVP; block_size <= 0 picks the reference's default); the modified
+ * variant is the GPU's blocked CGS + Cholesky-QR2 with the same dropping rule
+ * (block_size unused).  mv_ws / dbl_ws are accepted for signature
+ * compatibility; the device workspace belongs to ops (freed by OPS_Destroy),
+ * so, unlike the reference's single static setting, each ops keeps its own. */
+void MultiVecOrthSetup_ModifiedGramSchmidt(int block_size, int max_reorth, double orth_zero_tol,
+                                           void **mv_ws, double *dbl_ws, struct OPS_ *ops);
+void MultiVecOrthSetup_BinaryGramSchmidt(int block_size, int max_reorth, double orth_zero_tol,
+                                         void **mv_ws, double *dbl_ws, struct OPS_ *ops);
+
 /* GCG entry points: src/ops_eig_sol_gcg.c:1565-1628 (Setup), :1684-1741
  * (SetParameters), :1865-1877 (GCGE_Create), :1878-1918 (GCGE_Setparameters),
  * :1919-1927 (GCGE_Destroymvws), :1630-1680 (workspace create/destroy).
@@ -158,6 +176,11 @@ void EigenSolverSetParameters_GCG(
     double compW_orth_zero_tol, int compW_cg_max_iter, double compW_cg_rate, double compW_cg_tol,
     const char *compW_cg_tol_type, int compW_cg_auto_shift, int compRR_min_num,
     double compRR_min_gap, double compRR_tol, struct OPS_ *ops);
+/* src/ops_eig_sol_gcg.c:1743-1862 (declared at src/ops_eig_sol_gcg.h:83): the
+ * "-gcge_*" options of argv override the solver parameters, e.g.
+ * -gcge_compW_orth_method bgs, -gcge_compW_cg_order 2 (ComputeW12).
+ * -gcge_compRR_min_gap is read as a double; the usage table is not printed. */
+void EigenSolverSetParametersFromCommandLine_GCG(int argc, char *argv[], struct OPS_ *ops);
 void GCGE_Create(void *A, int nevMax, int block_size, int nevInit, void ***gcg_mv_ws,
                  double *dbl_ws, int *int_ws, struct OPS_ *ops);
 void GCGE_Setparameters(double gapMin, int shift, struct OPS_ *ops);

@@ -65,6 +65,36 @@ def test_ops_create_and_cuda_set_without_gpu(lib):
     lib.OPS_Destroy(ctypes.byref(ops))
 
 
+def test_orth_setup_installs_multivec_orth_without_gpu(lib):
+    """MultiVecOrthSetup_* (src/ops_orth.c:395-414, :625-641) fill
+    ops->MultiVecOrth and ops->orth_workspace; each ops keeps its own
+    setting, and OPS_Destroy releases it.  No device work happens here."""
+    a, b = ctypes.POINTER(G.OPSStruct)(), ctypes.POINTER(G.OPSStruct)()
+    for ops in (a, b):
+        lib.OPS_Create(ctypes.byref(ops))
+        lib.OPS_CUDA_Set(ops)
+        assert not ops.contents.MultiVecOrth and not ops.contents.orth_workspace
+    lib.MultiVecOrthSetup_BinaryGramSchmidt(ctypes.c_int(-1), ctypes.c_int(2),
+                                            ctypes.c_double(4.4e-16), None, None, a)
+    lib.MultiVecOrthSetup_ModifiedGramSchmidt(ctypes.c_int(-1), ctypes.c_int(2),
+                                              ctypes.c_double(4.4e-16), None, None, b)
+    assert a.contents.MultiVecOrth and b.contents.MultiVecOrth
+    assert a.contents.orth_workspace and a.contents.orth_workspace != b.contents.orth_workspace
+    assert lib.ops_cuda_last_error() == 0
+    for ops in (a, b):
+        lib.OPS_Destroy(ctypes.byref(ops))
+
+
+def test_command_line_setter_before_setup_is_an_error(lib):
+    ops = ctypes.POINTER(G.OPSStruct)()
+    lib.OPS_Create(ctypes.byref(ops))
+    lib.OPS_CUDA_Set(ops)
+    argv = (ctypes.c_char_p * 2)(b"-gcge_compW_cg_order", b"2")
+    lib.EigenSolverSetParametersFromCommandLine_GCG(2, argv, ops)
+    assert lib.ops_cuda_last_error() == G.GCGE_ERR_ARG
+    lib.OPS_Destroy(ctypes.byref(ops))
+
+
 LAYOUT_PROBE = r"""
 #include <stdio.h>
 #include <stddef.h>
