@@ -136,10 +136,20 @@ enum { PH_CHECK = 0, PH_P, PH_RR, PH_RRW, PH_EIG, PH_RV, PH_W, PH_LINSOL, PH_X, 
 // Products over the long (vector-length) dimension: FP64 FMA kernels in the
 // FP64 solve, FP64-accurate digit products on the tensor cores in the mixed
 // solve (same results to FP64 accuracy).
+// The mixed solve runs the long products (contraction over, or output of, at
+// least kDigitMinRows rows: the n-row blocks) on the digit-plane tensor-core
+// kernels.  Their error bound is relative to the largest |x| |y| of each
+// 64-row chunk, which is FP64-level for the n-row blocks but not for the
+// s-dimensional coefficient vectors of the small space (ComputeP's
+// orthogonalisation), whose entries mix O(1) and ~1e-8 values in one chunk:
+// there a small x small product would lose its relative accuracy and the P
+// block its B-orthogonality to X.  Those short products stay FP64.
+constexpr int kDigitMinRows = 2048;
+
 static void dgram(const SolverCtx &c, int n, int m, int w, const double *Q, int ldq,
                   const double *P, int ldp, double *C, int ldc, double *scratch, size_t elems,
                   cudaStream_t st) {
-    if (c.precision == GCGE_PREC_MIXED && !c.escalated)
+    if (c.precision == GCGE_PREC_MIXED && !c.escalated && n >= kDigitMinRows)
         oz_gram(n, m, w, Q, ldq, P, ldp, C, ldc, scratch, elems, st);
     else
         gram(n, m, w, Q, ldq, P, ldp, C, ldc, scratch, elems, st);
@@ -147,7 +157,7 @@ static void dgram(const SolverCtx &c, int n, int m, int w, const double *Q, int 
 static void dlincomb(const SolverCtx &c, int n, int k, int m, const double *X, int ldx,
                      const double *C, int ldc, double *Y, int ldy, const double *beta, int incb,
                      cudaStream_t st, double alpha = 1.0) {
-    if (c.precision == GCGE_PREC_MIXED && !c.escalated)
+    if (c.precision == GCGE_PREC_MIXED && !c.escalated && n >= kDigitMinRows)
         oz_lincomb(n, k, m, X, ldx, C, ldc, Y, ldy, beta, incb, st, alpha);
     else
         lincomb(n, k, m, X, ldx, C, ldc, Y, ldy, beta, incb, st, alpha);
@@ -179,84 +189,97 @@ int borth(SolverCtx &c, SparseMat *B, double *x, int ldx, int nrows, int start, 
     int k = end - start;
     double *X1 = x + (size_t)start * ldx;
     const double reorth_tol = 50.0 * 2.220446049250313e-16;  // src/ops_orth.c:404
-    if (start > 0) {
-        for (int pass = 0; pass < 1 + max_reorth; ++pass) {
+    // Two rounds at most.  Cholesky-QR multiplies the block by R^-1, which
+    // scales the rounding-level remainder of the prefix components by up to
+    // kappa(R); when the first factor of a round was ill-conditioned
+    // (nearly dependent columns, e.g. the two W directions of ComputeW12 or a
+    // W column of a nearly converged pair) the prefix projection and the
+    // factorisation run once more on the now well-conditioned block.
+    for (int round = 0; round < 2 && k > 0; ++round) {
+        if (start > 0) {
+            for (int pass = 0; pass < 1 + max_reorth; ++pass) {
+                const double *BX1 = X1;
+                if (useB) {
+                    applyB(X1, ldx, c.T2.p, ld, k);
+                    BX1 = c.T2.p;
+                }
+                dgram(c, nrows, start, k, x, ldx, BX1, useB ? ld : ldx, c.dC.p, start, c.gscr.p,
+                      c.gscr.n, st);
+                dlincomb(c, nrows, start, k, x, ldx, c.dC.p, start, X1, ldx, c.one.p, 0, st, -1.0);
+                if (pass >= 1 || max_reorth == 0) {
+                    if (device_absmax(start, k, c.dC.p, start) < reorth_tol) break;
+                }
+            }
+        }
+        double kappa = 1.0;  // max over kept columns of |x_j| / |new part of x_j| (first pass)
+        // Cholesky-QR of the new block with column dropping, repeated until its
+        // Gram matrix is the identity to 1e-13
+        for (int pass = 0; pass < 4 && k > 0; ++pass) {
             const double *BX1 = X1;
             if (useB) {
                 applyB(X1, ldx, c.T2.p, ld, k);
                 BX1 = c.T2.p;
             }
-            dgram(c, nrows, start, k, x, ldx, BX1, useB ? ld : ldx, c.dC.p, start, c.gscr.p,
-                  c.gscr.n, st);
-            dlincomb(c, nrows, start, k, x, ldx, c.dC.p, start, X1, ldx, c.one.p, 0, st, -1.0);
-            if (pass >= 1 || max_reorth == 0) {
-                if (device_absmax(start, k, c.dC.p, start) < reorth_tol) break;
+            dgram(c, nrows, k, k, X1, ldx, BX1, useB ? ld : ldx, c.dC.p, k, c.gscr.p, c.gscr.n, st);
+            GCGE_CUDA(cudaMemcpyAsync(c.hbuf.p, c.dC.p, sizeof(double) * k * k,
+                                      cudaMemcpyDeviceToHost, st));
+            GCGE_CUDA(cudaStreamSynchronize(st));
+            const double *G = c.hbuf.p;
+            double offmax = 0.0;
+            for (int a = 0; a < k; ++a)
+                for (int b = 0; b < k; ++b)
+                    offmax = std::max(offmax, std::fabs(G[a + (size_t)b * k] - (a == b ? 1.0 : 0.0)));
+            if (pass >= 1 && offmax < 1e-13) break;
+            // upper Cholesky R^T R = G restricted to the kept columns
+            std::vector<int> kept;
+            std::vector<double> R((size_t)k * k, 0.0);  // R[a + b*k], a = kept row index
+            for (int j = 0; j < k; ++j) {
+                GCGE_REQUIRE(std::isfinite(G[j + (size_t)j * k]), GCGE_ERR_NUMERIC,
+                             "orth: non-finite Gram matrix");
+                const int nk = (int)kept.size();
+                std::vector<double> rj(nk);
+                double d = G[j + (size_t)j * k];
+                for (int a = 0; a < nk; ++a) {
+                    double v = G[kept[a] + (size_t)j * k];
+                    for (int b = 0; b < a; ++b) v -= R[b + (size_t)a * k] * rj[b];
+                    v /= R[a + (size_t)a * k];
+                    rj[a] = v;
+                    d -= v * v;
+                }
+                const double gjj = std::max(G[j + (size_t)j * k], 0.0);
+                const double thr = std::max(zero_tol, 1e-7 * std::sqrt(gjj));
+                if (!(d > thr * thr)) continue;  // dependent column: drop
+                if (pass == 0) kappa = std::max(kappa, std::sqrt(gjj / d));
+                for (int a = 0; a < nk; ++a) R[a + (size_t)nk * k] = rj[a];
+                R[nk + (size_t)nk * k] = std::sqrt(d);
+                kept.push_back(j);
             }
-        }
-    }
-    // Cholesky-QR2 of the new block with column dropping
-    for (int pass = 0; pass < 3 && k > 0; ++pass) {
-        const double *BX1 = X1;
-        if (useB) {
-            applyB(X1, ldx, c.T2.p, ld, k);
-            BX1 = c.T2.p;
-        }
-        dgram(c, nrows, k, k, X1, ldx, BX1, useB ? ld : ldx, c.dC.p, k, c.gscr.p, c.gscr.n, st);
-        GCGE_CUDA(cudaMemcpyAsync(c.hbuf.p, c.dC.p, sizeof(double) * k * k,
-                                  cudaMemcpyDeviceToHost, st));
-        GCGE_CUDA(cudaStreamSynchronize(st));
-        const double *G = c.hbuf.p;
-        double offmax = 0.0;
-        for (int a = 0; a < k; ++a)
-            for (int b = 0; b < k; ++b)
-                offmax = std::max(offmax, std::fabs(G[a + (size_t)b * k] - (a == b ? 1.0 : 0.0)));
-        if (pass >= 1 && offmax < 1e-13) break;
-        // upper Cholesky R^T R = G restricted to the kept columns
-        std::vector<int> kept;
-        std::vector<double> R((size_t)k * k, 0.0);  // R[a + b*k], a = kept row index
-        for (int j = 0; j < k; ++j) {
-            GCGE_REQUIRE(std::isfinite(G[j + (size_t)j * k]), GCGE_ERR_NUMERIC,
-                         "orth: non-finite Gram matrix");
-            const int nk = (int)kept.size();
-            std::vector<double> rj(nk);
-            double d = G[j + (size_t)j * k];
-            for (int a = 0; a < nk; ++a) {
-                double v = G[kept[a] + (size_t)j * k];
-                for (int b = 0; b < a; ++b) v -= R[b + (size_t)a * k] * rj[b];
-                v /= R[a + (size_t)a * k];
-                rj[a] = v;
-                d -= v * v;
+            const int kk = (int)kept.size();
+            // coefficient matrix Cf (k x kk): Cf[kept[a], b] = (R^{-1})[a, b]
+            std::vector<double> Ri((size_t)kk * kk, 0.0);
+            for (int b = 0; b < kk; ++b) {
+                Ri[b + (size_t)b * kk] = 1.0 / R[b + (size_t)b * k];
+                for (int a = b - 1; a >= 0; --a) {
+                    double v = 0.0;
+                    for (int l = a + 1; l <= b; ++l) v += R[a + (size_t)l * k] * Ri[l + (size_t)b * kk];
+                    Ri[a + (size_t)b * kk] = -v / R[a + (size_t)a * k];
+                }
             }
-            const double thr = std::max(zero_tol, 1e-7 * std::sqrt(std::max(G[j + (size_t)j * k], 0.0)));
-            if (!(d > thr * thr)) continue;  // dependent column: drop
-            for (int a = 0; a < nk; ++a) R[a + (size_t)nk * k] = rj[a];
-            R[nk + (size_t)nk * k] = std::sqrt(d);
-            kept.push_back(j);
-        }
-        const int kk = (int)kept.size();
-        // coefficient matrix Cf (k x kk): Cf[kept[a], b] = (R^{-1})[a, b]
-        std::vector<double> Ri((size_t)kk * kk, 0.0);
-        for (int b = 0; b < kk; ++b) {
-            Ri[b + (size_t)b * kk] = 1.0 / R[b + (size_t)b * k];
-            for (int a = b - 1; a >= 0; --a) {
-                double v = 0.0;
-                for (int l = a + 1; l <= b; ++l) v += R[a + (size_t)l * k] * Ri[l + (size_t)b * kk];
-                Ri[a + (size_t)b * kk] = -v / R[a + (size_t)a * k];
+            double *Cf = c.hbuf.p + (size_t)k * k;
+            std::fill(Cf, Cf + (size_t)k * std::max(kk, 1), 0.0);
+            for (int a = 0; a < kk; ++a)
+                for (int b = 0; b < kk; ++b) Cf[kept[a] + (size_t)b * k] = Ri[a + (size_t)b * kk];
+            if (kk > 0) {
+                GCGE_CUDA(cudaMemcpyAsync(c.dC.p, Cf, sizeof(double) * k * kk,
+                                          cudaMemcpyHostToDevice, st));
+                dlincomb(c, nrows, k, kk, X1, ldx, c.dC.p, k, c.T1.p, ld, nullptr, 0, st);
+                copy_cols(nrows, kk, c.T1.p, ld, X1, ldx, st);
             }
+            k = kk;
+            // the host buffer is reused next pass: wait for the upload
+            GCGE_CUDA(cudaStreamSynchronize(st));
         }
-        double *Cf = c.hbuf.p + (size_t)k * k;
-        std::fill(Cf, Cf + (size_t)k * std::max(kk, 1), 0.0);
-        for (int a = 0; a < kk; ++a)
-            for (int b = 0; b < kk; ++b) Cf[kept[a] + (size_t)b * k] = Ri[a + (size_t)b * kk];
-        if (kk > 0) {
-            GCGE_CUDA(cudaMemcpyAsync(c.dC.p, Cf, sizeof(double) * k * kk,
-                                      cudaMemcpyHostToDevice, st));
-            dlincomb(c, nrows, k, kk, X1, ldx, c.dC.p, k, c.T1.p, ld, nullptr, 0, st);
-            copy_cols(nrows, kk, c.T1.p, ld, X1, ldx, st);
-        }
-        k = kk;
-        // the host buffer is reused next pass: wait for the upload
-        GCGE_CUDA(cudaStreamSynchronize(st));
+        if (start == 0 || kappa < 1e3) break;
     }
     return start + k;
 }

@@ -116,7 +116,8 @@ def test_user_defined_linear_solver_hook(gpu_lib):
     the caller's MultiLinearSolver runs on b = (lambda + sigma) B x in the
     Ritz-vector columns [offset[1], ...) with x in V[:, startW:endW], then
     BlockPCG from its result.  A solver that leaves x alone gives the plain
-    solve; one that zeroes x changes only BlockPCG's starting point."""
+    solve.  With 1 the caller's solver alone builds W: five Richardson steps
+    run through the backend's own OPS slots still converge, more slowly."""
     G = gpu_lib
     A = P.laplace2d(24, 24)
     X0 = P.initial_block(A.n, 12, seed=1)
@@ -135,16 +136,29 @@ def test_user_defined_linear_solver_hook(gpu_lib):
         assert e0 - s0 == e1 - s1 > 0 and s1 >= 12   # W after X (and P)
 
     ops_lib = G.load()
+    n, omega = A.n, 0.125   # 1 / (largest Gershgorin bound of the 5-point operator)
 
-    def zero_x(mat, b, x, start, end, ops):
-        # the caller's solver uses the backend's own slots on the handles
+    def richardson(mat, b, x, start, end, ops):
+        """Five Richardson steps x <- x + omega (b - A x) through the backend's slots."""
         o = ctypes.cast(ops, ctypes.POINTER(G.OPSStruct)).contents
+        create = ctypes.cast(o.MultiVecCreateByMat, G._FT["MultiVecCreateByMat"])
+        destroy = ctypes.cast(o.MultiVecDestroy, G._FT["MultiVecDestroy"])
+        matvec = ctypes.cast(o.MatDotMultiVec, G._FT["MatDotMultiVec"])
         axpby = ctypes.cast(o.MultiVecAxpby, G._FT["MultiVecAxpby"])
-        s = (ctypes.c_int * 2)(start[1], start[1])
-        e = (ctypes.c_int * 2)(end[1], end[1])
-        axpby(0.0, None, 0.0, x, s, e, ops)
+        I2 = ctypes.c_int * 2
+        k = end[1] - start[1]
+        tmp = ctypes.c_void_p()
+        create(ctypes.byref(tmp), k, mat, ops)
+        for _ in range(5):
+            matvec(mat, x, tmp, I2(start[1], 0), I2(end[1], k), ops)
+            axpby(1.0, b, -1.0, tmp, I2(start[0], 0), I2(end[0], k), ops)
+            axpby(omega, tmp, 1.0, x, I2(0, start[1]), I2(k, end[1]), ops)
+        destroy(ctypes.byref(tmp), k, ops)
 
-    z = G.solve_ops(A, None, 8, 4, 12, 20, X0=X0, auto_shift=0, args=args, linear_solver=zero_x)
+    # user_defined_multi_linear_solver 1: the caller's solver alone builds W
+    z = G.solve_ops(A, None, 8, 4, 12, 20, X0=X0, auto_shift=0, max_iter=2000,
+                    args=("-gcge_user_defined_multi_lin_sol", "1"), linear_solver=richardson)
     assert ops_lib.ops_cuda_last_error() == 0
-    assert z.nconv >= 8
+    assert z.status == G.GCGE_OK and z.nconv >= 8 and z.niter > base.niter
     np.testing.assert_allclose(z.eval[:8], base.eval[:8], rtol=1e-10, atol=0)
+    assert n == 576
