@@ -136,20 +136,10 @@ enum { PH_CHECK = 0, PH_P, PH_RR, PH_RRW, PH_EIG, PH_RV, PH_W, PH_LINSOL, PH_X, 
 // Products over the long (vector-length) dimension: FP64 FMA kernels in the
 // FP64 solve, FP64-accurate digit products on the tensor cores in the mixed
 // solve (same results to FP64 accuracy).
-// The mixed solve runs the long products (contraction over, or output of, at
-// least kDigitMinRows rows: the n-row blocks) on the digit-plane tensor-core
-// kernels.  Their error bound is relative to the largest |x| |y| of each
-// 64-row chunk, which is FP64-level for the n-row blocks but not for the
-// s-dimensional coefficient vectors of the small space (ComputeP's
-// orthogonalisation), whose entries mix O(1) and ~1e-8 values in one chunk:
-// there a small x small product would lose its relative accuracy and the P
-// block its B-orthogonality to X.  Those short products stay FP64.
-constexpr int kDigitMinRows = 2048;
-
 static void dgram(const SolverCtx &c, int n, int m, int w, const double *Q, int ldq,
                   const double *P, int ldp, double *C, int ldc, double *scratch, size_t elems,
                   cudaStream_t st) {
-    if (c.precision == GCGE_PREC_MIXED && !c.escalated && n >= kDigitMinRows)
+    if (c.precision == GCGE_PREC_MIXED && !c.escalated)
         oz_gram(n, m, w, Q, ldq, P, ldp, C, ldc, scratch, elems, st);
     else
         gram(n, m, w, Q, ldq, P, ldp, C, ldc, scratch, elems, st);
@@ -157,7 +147,7 @@ static void dgram(const SolverCtx &c, int n, int m, int w, const double *Q, int 
 static void dlincomb(const SolverCtx &c, int n, int k, int m, const double *X, int ldx,
                      const double *C, int ldc, double *Y, int ldy, const double *beta, int incb,
                      cudaStream_t st, double alpha = 1.0) {
-    if (c.precision == GCGE_PREC_MIXED && !c.escalated && n >= kDigitMinRows)
+    if (c.precision == GCGE_PREC_MIXED && !c.escalated)
         oz_lincomb(n, k, m, X, ldx, C, ldc, Y, ldy, beta, incb, st, alpha);
     else
         lincomb(n, k, m, X, ldx, C, ldc, Y, ldy, beta, incb, st, alpha);
@@ -911,6 +901,94 @@ struct GcgRun {
         timer.mark(PH_RR);
     }
 
+    // Mixed solve: the returned eigenvalues are the FP64 Rayleigh quotients
+    // x^T A x / x^T B x of the returned vectors.  The Ritz values of the last
+    // projection carry the basis' B-orthonormality error, which the digit-plane
+    // products and the FP32 inner solve leave larger than the FP64 solve does
+    // (it reached ~3e-9 with ComputeW12); the quotients of vectors whose
+    // relative residual is below the tolerance are accurate to its square.
+    // If the converged vectors X_c themselves are B-orthonormal only to worse
+    // than 1e-10, a last Rayleigh-Ritz step on span(X_c) restores it:
+    // X_c <- X_c Z with H Z = G Z diag(lambda), G = X_c^T B X_c, H = X_c^T A X_c
+    // (Cholesky of G and FP64 Jacobi of the reduced matrix on the host).  The
+    // converged block ends at a gap (the back-off of CheckConvergence), so the
+    // rotation does not mix in unconverged vectors.
+    void final_rayleigh_ritz(double *eval, int k, int kc) {
+        if (k <= 0) return;
+        spmm<double>(A->pat, A->val.p, ritz->data, ritz->ld, c.T1.p, ld, k, st);
+        spmm_calls++;
+        applyB(ritz->data, ritz->ld, c.T2.p, ld, k);
+        double *dG = c.dtmp.p, *dH = c.dC.p;
+        dgram(c, n, k, k, ritz->data, ritz->ld, c.T2.p, ld, dG, k, c.gscr.p, c.gscr.n, st);
+        dgram(c, n, k, k, ritz->data, ritz->ld, c.T1.p, ld, dH, k, c.gscr.p, c.gscr.n, st);
+        std::vector<double> Gf((size_t)k * k), Hf((size_t)k * k);
+        GCGE_CUDA(cudaMemcpyAsync(Gf.data(), dG, sizeof(double) * k * k, cudaMemcpyDeviceToHost, st));
+        GCGE_CUDA(cudaMemcpyAsync(Hf.data(), dH, sizeof(double) * k * k, cudaMemcpyDeviceToHost, st));
+        GCGE_CUDA(cudaStreamSynchronize(st));
+        for (int j = 0; j < k; ++j) {
+            const double q = Hf[j + (size_t)j * k] / Gf[j + (size_t)j * k];
+            if (Gf[j + (size_t)j * k] > 0.0 && std::isfinite(q)) eval[j] = q;
+        }
+        kc = std::min(kc, k);
+        if (kc <= 0) return;
+        double e = 0.0;
+        for (int a = 0; a < kc; ++a)
+            for (int b = 0; b < kc; ++b)
+                e = std::max(e, std::fabs(Gf[a + (size_t)b * k] - (a == b ? 1.0 : 0.0)));
+        if (!std::isfinite(e) || e < 1e-10) return;
+        const int kf = k;
+        k = kc;  // the leading kc x kc blocks
+        std::vector<double> G((size_t)k * k), H((size_t)k * k);
+        for (int b = 0; b < k; ++b)
+            for (int a = 0; a < k; ++a) {
+                G[a + (size_t)b * k] = Gf[a + (size_t)b * kf];
+                H[a + (size_t)b * k] = Hf[a + (size_t)b * kf];
+            }
+        // G = L L^T (lower, column-major); C = L^-1 H L^-T
+        std::vector<double> L((size_t)k * k, 0.0);
+        for (int j = 0; j < k; ++j) {
+            double d = 0.5 * (G[j + (size_t)j * k] + G[j + (size_t)j * k]);
+            for (int l = 0; l < j; ++l) d -= L[j + (size_t)l * k] * L[j + (size_t)l * k];
+            if (!(d > 0.0)) return;  // not positive definite: keep the vectors as they are
+            L[j + (size_t)j * k] = std::sqrt(d);
+            for (int i = j + 1; i < k; ++i) {
+                double v = 0.5 * (G[i + (size_t)j * k] + G[j + (size_t)i * k]);
+                for (int l = 0; l < j; ++l) v -= L[i + (size_t)l * k] * L[j + (size_t)l * k];
+                L[i + (size_t)j * k] = v / L[j + (size_t)j * k];
+            }
+        }
+        auto lsolve = [&](std::vector<double> &Mx) {  // Mx <- L^-1 Mx (column by column)
+            for (int col = 0; col < k; ++col)
+                for (int i = 0; i < k; ++i) {
+                    double v = Mx[i + (size_t)col * k];
+                    for (int l = 0; l < i; ++l) v -= L[i + (size_t)l * k] * Mx[l + (size_t)col * k];
+                    Mx[i + (size_t)col * k] = v / L[i + (size_t)i * k];
+                }
+        };
+        std::vector<double> Cm(H);
+        lsolve(Cm);  // L^-1 H
+        std::vector<double> Ct((size_t)k * k);
+        for (int a = 0; a < k; ++a)
+            for (int b = 0; b < k; ++b) Ct[a + (size_t)b * k] = Cm[b + (size_t)a * k];
+        lsolve(Ct);  // L^-1 (L^-1 H)^T = L^-1 H L^-T (H symmetric)
+        std::vector<double> w(k), Y((size_t)k * k);
+        host_eigh(k, Ct.data(), w.data(), Y.data());
+        // Z = L^-T Y (back substitution with L^T)
+        std::vector<double> Z(Y);
+        for (int col = 0; col < k; ++col)
+            for (int i = k - 1; i >= 0; --i) {
+                double v = Z[i + (size_t)col * k];
+                for (int l = i + 1; l < k; ++l) v -= L[l + (size_t)i * k] * Z[l + (size_t)col * k];
+                Z[i + (size_t)col * k] = v / L[i + (size_t)i * k];
+            }
+        GCGE_CUDA(cudaMemcpyAsync(c.dC.p, Z.data(), sizeof(double) * k * k, cudaMemcpyHostToDevice,
+                                  st));
+        dlincomb(c, n, k, k, ritz->data, ritz->ld, c.dC.p, k, c.T1.p, ld, nullptr, 0, st);
+        copy_cols(n, k, c.T1.p, ld, ritz->data, ritz->ld, st);
+        GCGE_CUDA(cudaStreamSynchronize(st));
+        for (int j = 0; j < k; ++j) eval[j] = w[j];
+    }
+
     // ---------------- GCG outer loop (:1259-1562)
     int run(double *eval, int nevGiven, int *nevConvIO) {
         const int nevInit = g.nevInit, nevMax = g.nevMax, bs = g.block_size;
@@ -999,6 +1077,7 @@ struct GcgRun {
         } while (numIter < numIterMax);
         g.numIter = numIter + (g.numIterMax - numIterMax);
         for (int i = 0; i < sizeX; ++i) eval[i] = ss_eval[i];
+        if (c.precision == GCGE_PREC_MIXED) final_rayleigh_ritz(eval, sizeX, std::min(nevc, sizeX));
         *nevConvIO = nevc;
         g.nevConv = nevc;
         timer.mark(PH_NONE);
