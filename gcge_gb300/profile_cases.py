@@ -1,0 +1,63 @@
+"""Single-kernel cases for profiling, at the shapes of the benchmark solve
+(n = 262144 rows, the 64^3 generalized problem: nev_max + 2 bs = 200 basis
+columns, blocks of bs = 20).
+
+    python -m gcge_gb300.profile_cases gram      # Q^T P, Q n x 180, P n x 20
+    python -m gcge_gb300.profile_cases lincomb   # X C, X n x 180, C 180 x 20
+    python -m gcge_gb300.profile_cases both
+
+Each case runs the FP64-accurate digit-plane product once after one warm-up
+call, through the same C-ABI entry points the parity tests use
+(GCGE_DenseGram / GCGE_DenseLinComb), and checks the result against the FP64
+kernel's.  Under ncu, select the product kernel with -k regex:k_oz_gemm.
+"""
+from __future__ import annotations
+
+import sys
+
+import numpy as np
+
+import gcge_gb300 as G
+
+N, M, W = 262144, 180, 20
+
+
+def _data(seed):
+    rng = np.random.default_rng(seed)
+    return rng.standard_normal((N, M)), rng.standard_normal((N, W))
+
+
+def gram():
+    Q, P = _data(1)
+    G.dense_gram(Q, P, emulated=True)
+    C = G.dense_gram(Q, P, emulated=True)
+    ref = G.dense_gram(Q, P, emulated=False)
+    err = float(np.max(np.abs(C - ref)) / np.max(np.abs(Q).T @ np.abs(P)))
+    print(f"gram n={N} m={M} w={W}: max |emulated - fp64| / max(|Q|^T |P|) = {err:.2e}")
+    return err < 1e-14
+
+
+def lincomb():
+    X, _ = _data(2)
+    C = np.random.default_rng(3).standard_normal((M, W))
+    Y0 = np.zeros((N, W))
+    G.dense_lincomb(X, C, Y0, emulated=True)
+    Y = G.dense_lincomb(X, C, Y0, emulated=True)
+    ref = G.dense_lincomb(X, C, Y0, emulated=False)
+    err = float(np.max(np.abs(Y - ref)) / np.max(np.abs(X) @ np.abs(C)))
+    print(f"lincomb n={N} k={M} m={W}: max |emulated - fp64| / max(|X| |C|) = {err:.2e}")
+    return err < 1e-14
+
+
+def main(argv):
+    what = argv[1] if len(argv) > 1 else "both"
+    ok = True
+    if what in ("gram", "both"):
+        ok &= gram()
+    if what in ("lincomb", "both"):
+        ok &= lincomb()
+    return 0 if ok else 1
+
+
+if __name__ == "__main__":
+    sys.exit(main(sys.argv))
