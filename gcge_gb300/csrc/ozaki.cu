@@ -58,22 +58,50 @@ __device__ __forceinline__ int exp_field(double x) {
     return max((int)((__double_as_longlong(x) >> 52) & 0x7FF), 1);
 }
 
-// The 8 signed 7-bit digits of x relative to 2^(emax - 1022) as bf16 bit
-// patterns (emax >= exp_field(x)).
-__device__ __forceinline__ void split_digits(double x, int emax, uint16_t (&d)[kDigits]) {
+// x as a 56-bit fixed-point magnitude relative to 2^(emax - 1022) (emax >=
+// exp_field(x)), split into 32-bit words, and the bias word of its digits:
+// +2^23 or -2^23 as an FP32 bit pattern, carrying x's sign.
+struct Fixed56 {
+    uint32_t hi, lo;
+    uint32_t magic;
+};
+__device__ __forceinline__ Fixed56 fixed56(double x, int emax) {
     const unsigned long long b = (unsigned long long)__double_as_longlong(x);
     const int ef = (int)((b >> 52) & 0x7FF);
     unsigned long long mant = b & 0x000FFFFFFFFFFFFFull;
     if (ef != 0) mant |= 0x0010000000000000ull;
     const int sh = max(ef, 1) - emax + 3;  // <= 3: the value < 2^56 in fixed point
     const unsigned long long X = sh >= 0 ? (mant << sh) : (sh > -64 ? (mant >> (-sh)) : 0ull);
-    const uint16_t sgn = (uint16_t)((b >> 48) & 0x8000u);
-#pragma unroll
-    for (int i = 0; i < kDigits; ++i) {
-        const unsigned v = (unsigned)(X >> (49 - kDigitBits * i)) & 127u;
-        // exact small-integer float: (2^23 + v) - 2^23; bf16 = its top 16 bits
-        const float f = __uint_as_float(0x4B000000u | v) - 8388608.0f;
-        d[i] = (uint16_t)(__float_as_uint(f) >> 16) | (v ? sgn : (uint16_t)0);
+    Fixed56 f;
+    f.hi = (uint32_t)(X >> 32);
+    f.lo = (uint32_t)X;
+    f.magic = 0x4B000000u | ((uint32_t)(b >> 32) & 0x80000000u);
+    return f;
+}
+
+// Digit i (bits 49-7i .. 55-7i of the fixed-point value) as an FP32 number
+// +-d, d in [0, 127]: (bias | d) read as FP32 is +-(2^23 + d), and subtracting
+// the bias +-2^23 leaves +-d exactly.  Its upper 16 bits are its bf16 pattern.
+template <int I>
+__device__ __forceinline__ uint32_t digit_f32(const Fixed56 &f) {
+    constexpr int s = 49 - 7 * I;
+    uint32_t t;
+    if constexpr (s >= 32)
+        t = f.hi >> (s - 32);
+    else
+        t = __funnelshift_r(f.lo, f.hi, s);
+    const float v = __uint_as_float((t & 127u) | f.magic) - __uint_as_float(f.magic);
+    return __float_as_uint(v);
+}
+
+// The 8 digit planes of two values (consecutive k of one row): word i holds
+// digit i of x0 in its low and of x1 in its high bf16 half.
+template <int I = 0>
+__device__ __forceinline__ void digit_pairs(const Fixed56 &a, const Fixed56 &b,
+                                            uint32_t (&w)[kDigits]) {
+    if constexpr (I < kDigits) {
+        w[I] = __byte_perm(digit_f32<I>(a), digit_f32<I>(b), 0x7632);
+        digit_pairs<I + 1>(a, b, w);
     }
 }
 
@@ -155,13 +183,11 @@ __device__ __forceinline__ void planes_kcontig(const double *__restrict__ p, siz
             if (k + 1 < kend) v1 = q[k + 1];
         }
         const int em = e[r];
-        uint16_t d0[kDigits], d1[kDigits];
-        split_digits(v0, em, d0);
-        split_digits(v1, em, d1);
+        uint32_t w[kDigits];
+        digit_pairs(fixed56(v0, em), fixed56(v1, em), w);
 #pragma unroll
         for (int i = 0; i < kDigits; ++i)
-            *reinterpret_cast<uint32_t *>(&planes[i][r][2 * lane]) =
-                (uint32_t)d0[i] | ((uint32_t)d1[i] << 16);
+            *reinterpret_cast<uint32_t *>(&planes[i][r][2 * lane]) = w[i];
     }
 }
 
@@ -187,12 +213,10 @@ __device__ __forceinline__ void planes_mcontig(const double *__restrict__ p, siz
                 if (k < kend) v0 = p[gr + (size_t)k * ld];
                 if (k + 1 < kend) v1 = p[gr + (size_t)(k + 1) * ld];
             }
-            uint16_t d0[kDigits], d1[kDigits];
-            split_digits(v0, em, d0);
-            split_digits(v1, em, d1);
+            uint32_t wp[kDigits];
+            digit_pairs(fixed56(v0, em), fixed56(v1, em), wp);
 #pragma unroll
-            for (int i = 0; i < kDigits; ++i)
-                w[i][q / 2] = (uint32_t)d0[i] | ((uint32_t)d1[i] << 16);
+            for (int i = 0; i < kDigits; ++i) w[i][q / 2] = wp[i];
         }
 #pragma unroll
         for (int i = 0; i < kDigits; ++i)
