@@ -496,6 +496,10 @@ struct GcgRun {
     int s_old = 0;
     double sigma = 0.0;
     int pcg_iters = 0, spmm_calls = 0;
+    // Ritz-vector columns [chk_lo, chk_lo + chk_n) whose A x and B x
+    // CheckConvergence left in c.chkA / c.chkB (the vectors do not change
+    // until the next Rayleigh-Ritz step)
+    int chk_lo = 0, chk_n = 0;
     // the caller's handles, for a user-defined MultiLinearSolver
     OPS *ops = nullptr;
     void *Ah = nullptr, **Vh = nullptr, **Rh = nullptr;
@@ -563,12 +567,17 @@ struct GcgRun {
         const double *tol = g.tol;
         GCGE_REQUIRE(c.has_union, GCGE_ERR_ARG, "operator not prepared");
         std::vector<double> res(numCheck);
+        c.chkA.alloc((size_t)ld * numCheck);
+        c.chkB.alloc((size_t)ld * numCheck);
+        chk_lo = startN;
+        chk_n = numCheck;
         for (int c0 = 0; c0 < numCheck; c0 += 40) {
             const int kc = std::min(40, numCheck - c0);
             GCGE_CUDA(cudaMemcpyAsync(c.dvec.p, &ss_eval[startN + c0], sizeof(double) * kc,
                                       cudaMemcpyHostToDevice, st));
             const int nb = residual_norms(c.upat, c.ua.p, c.ub.p, colp(ritz, startN + c0), ritz->ld,
-                                          c.dvec.p, kc, c.part.p, 64, st);
+                                          c.dvec.p, kc, c.part.p, 64, st, c.chkA.p + (size_t)c0 * ld,
+                                          c.chkB.p + (size_t)c0 * ld, ld);
             spmm_calls++;
             reduce_partials(c.part.p, nb, 64, kc, c.dvec.p + 64, st);
             GCGE_CUDA(cudaMemcpyAsync(c.hbuf.p + c0, c.dvec.p + 64, sizeof(double) * kc,
@@ -719,10 +728,17 @@ struct GcgRun {
         startW = endP;
         int bsz = 0;
         double *hscale = c.hbuf.p;
+        bool stored = true;  // every column's A x and B x kept by CheckConvergence
         for (int i = 0; i < offset[0]; ++i) {
             const int o1 = offset[2 * i + 1], o2 = offset[2 * i + 2], len = o2 - o1;
             copy_cols(n, len, colp(ritz, o1), ritz->ld, colp(V, startW + bsz), ld, st);
-            applyB(colp(V, o1), ld, c.bbuf.p + (size_t)bsz * ld, ld, len);
+            if (have_products(o1, o2))
+                copy_cols(n, len, c.chkB.p + (size_t)(o1 - chk_lo) * ld, ld,
+                          c.bbuf.p + (size_t)bsz * ld, ld, st);
+            else {
+                applyB(colp(V, o1), ld, c.bbuf.p + (size_t)bsz * ld, ld, len);
+                stored = false;
+            }
             for (int j = 0; j < len; ++j) hscale[bsz + j] = ss_eval[o1 + j] + sigma;
             bsz += len;
         }
@@ -752,7 +768,23 @@ struct GcgRun {
             // BlockPCG after it (ud == 2) starts from its x with its b
             copy_cols(n, bsz, colp(ritz, offset[1]), ritz->ld, c.bbuf.p, ld, st);
         }
-        if (ud != 1) w_solve(colp(V, startW), bsz, mixed);
+        if (ud != 1) {
+            bool have_sx = false;
+            if (mixed && stored && ud == 0) {
+                // S x0 = A x0 + sigma B x0 from the stored products
+                int off = 0;
+                for (int i = 0; i < offset[0]; ++i) {
+                    const int o1 = offset[2 * i + 1], len = offset[2 * i + 2] - o1;
+                    copy_cols(n, len, c.chkA.p + (size_t)(o1 - chk_lo) * ld, ld,
+                              c.r64.p + (size_t)off * ld, ld, st);
+                    axpby(n, len, sigma, c.chkB.p + (size_t)(o1 - chk_lo) * ld, ld, 1.0,
+                          c.r64.p + (size_t)off * ld, ld, st);
+                    off += len;
+                }
+                have_sx = true;
+            }
+            w_solve(colp(V, startW), bsz, mixed, have_sx);
+        }
         timer.mark(PH_W);
         endW = orth(colp(V, 0), ld, n, startW, endW, B != nullptr, g.compW_orth_zero_tol,
                     g.compW_orth_max_reorth, g.compW_orth_method, g.compW_orth_block_size);
@@ -762,7 +794,7 @@ struct GcgRun {
     // BlockPCG on S x = b (b in c.bbuf, S = A + sigma B on the union pattern,
     // its values already formed) for bsz columns, starting from and overwriting
     // x (V columns, leading dimension ld).
-    void w_solve(double *x, int bsz, bool mixed) {
+    void w_solve(double *x, int bsz, bool mixed, bool have_sx = false) {
         if (bsz <= 0) return;
         const bool rel = std::strcmp(g.compW_cg_tol_type, "rel") == 0;
         if (!mixed) {
@@ -780,15 +812,22 @@ struct GcgRun {
             // the Ritz vectors converge), the correction d is iterated in FP32,
             // and x = x0 + d is accumulated in FP64.
             const int kp = rows_width(bsz, 4);
-            spmm<double>(c.upat, c.us64.p, x, ld, c.r64.p, ld, bsz, st);
+            if (!have_sx) {  // else r64 already holds S x
+                spmm<double>(c.upat, c.us64.p, x, ld, c.r64.p, ld, bsz, st);
+                spmm_calls++;
+            }
             axpby(n, bsz, 1.0, c.bbuf.p, ld, -1.0, c.r64.p, ld, st);
             col_to_rows<double, float>(n, bsz, kp, c.r64.p, ld, c.br32.p, st);
             block_pcg_rows<float>(c.pcg, c.upat, c.us32.p, c.br32.p, c.xr32.p, c.rr32.p,
                                   c.pr32.p, c.wr32.p, kp, bsz, g.compW_cg_max_iter,
                                   g.compW_cg_rate, g.compW_cg_tol, rel, true, st);
             rows_to_col<float, double>(n, bsz, kp, c.xr32.p, x, ld, true, st);
-            spmm_calls++;
         }
+    }
+
+    // The A x and B x of Ritz-vector columns [o1, o2) are in c.chkA / c.chkB.
+    bool have_products(int o1, int o2) const {
+        return o1 >= chk_lo && o2 <= chk_lo + chk_n && c.chkB.p != nullptr;
     }
 
     // ---------------- ComputeW12 (:703-929), compW_cg_order 2: the first half
@@ -816,7 +855,11 @@ struct GcgRun {
             int len = offset[2 * i + 2] - o1;
             if (bsz + len >= half) len = half - bsz;
             copy_cols(n, len, colp(ritz, o1), ritz->ld, colp(V, startW + bsz), ld, st);
-            applyB(colp(V, o1), ld, c.bbuf.p + (size_t)bsz * ld, ld, len);
+            if (have_products(o1, o1 + len))
+                copy_cols(n, len, c.chkB.p + (size_t)(o1 - chk_lo) * ld, ld,
+                          c.bbuf.p + (size_t)bsz * ld, ld, st);
+            else
+                applyB(colp(V, o1), ld, c.bbuf.p + (size_t)bsz * ld, ld, len);
             for (int j = 0; j < len; ++j) hscale[bsz + j] = ss_eval[o1 + j] + sigma;
             bsz += len;
             if (bsz >= half) break;

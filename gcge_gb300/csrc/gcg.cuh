@@ -31,6 +31,9 @@ struct SolverCtx {
     DevBuf<double> xr64, br64, rr64, pr64, wr64;
     DevBuf<float> xr32, br32, rr32, pr32, wr32;
     DevBuf<double> M0, M1, evec, work, coefP, ptap, dC, dtmp, gscr, part, dvec, dmax, one;
+    // A x and B x of the Ritz vectors CheckConvergence tested (n x numCheck),
+    // reused by ComputeW for its right-hand side and initial residual
+    DevBuf<double> chkA, chkB;
     DevBuf<int> dmask, didx;
     PinnedBuf<double> hbuf, hmax;
     EigWork eig;

@@ -13,6 +13,7 @@
 // PCG kernel's grid, so the cooperative kernels of concurrent solves always
 // fit on the device together.  Results do not depend on what else runs: every
 // kernel's work split depends on the problem (and the share), not on timing.
+#include <algorithm>
 #include <atomic>
 #include <chrono>
 #include <condition_variable>
@@ -53,6 +54,7 @@ size_t footprint(const gcge_request *r) {
     size_t b = 8 * ld * (cols + r->nev_max);          // V, Ritz vectors
     b += 8 * ld * (3 * cols + 4 * r->block_size);     // workspaces, T1/T2, b, r
     b += 5 * ld * kp * (8 + 4);                       // PCG blocks (FP64 and FP32)
+    b += 2 * 8 * ld * std::min<size_t>(50, (size_t)r->nev_max);  // A x, B x of the check
     b += 64 * (nnz_a + nnz_b + r->n);                 // CSR, SELL, union, staging
     return b + ((size_t)64 << 20);
 }

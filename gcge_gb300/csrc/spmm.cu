@@ -55,7 +55,8 @@ __global__ void __launch_bounds__(kSpmmThreads)
 k_residual(const long long *__restrict__ sp, const int *__restrict__ col,
            const double *__restrict__ a, const double *__restrict__ b, int n, int nslices,
            const double *__restrict__ X, int ldx, const double *__restrict__ lam, int k,
-           double *__restrict__ partial, int kmax) {
+           double *__restrict__ partial, int kmax, double *__restrict__ ax,
+           double *__restrict__ bx, int ldo) {
     __shared__ double red[kSpmmThreads / 32][K];
     __shared__ double slam[K];
     const int slice = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -95,6 +96,14 @@ k_residual(const long long *__restrict__ sp, const int *__restrict__ col,
                     if (c < k) bcc[c] = fma(bv, __ldg(xj + (size_t)c * ldx), bcc[c]);
             }
         }
+    }
+    if (ax != nullptr && row < n) {  // keep A x and B x for the W step
+#pragma unroll
+        for (int c = 0; c < K; ++c)
+            if (c < k) {
+                ax[row + (size_t)c * ldo] = acc[c];
+                bx[row + (size_t)c * ldo] = bcc[c];
+            }
     }
 #pragma unroll
     for (int c = 0; c < K; ++c) {
@@ -141,13 +150,14 @@ void spmm(const SellPattern &pat, const T *val, const T *X, int ldx, T *Y, int l
 }
 
 int residual_norms(const SellPattern &pat, const double *a, const double *b, const double *X,
-                   int ldx, const double *lam, int k, double *partial, int kmax, cudaStream_t st) {
+                   int ldx, const double *lam, int k, double *partial, int kmax, cudaStream_t st,
+                   double *ax, double *bx, int ldo) {
     GCGE_REQUIRE(k <= kMaxChunk && k <= kmax, GCGE_ERR_ARG, "residual_norms: too many columns");
     const int blocks = spmm_blocks(pat);
     if (k <= 0) return 0;
     GCGE_K_DISPATCH(k, (k_residual<KT><<<blocks, kSpmmThreads, 0, st>>>(
                            pat.slice_ptr.p, pat.col.p, a, b, pat.n, pat.nslices, X, ldx, lam, k,
-                           partial, kmax)));
+                           partial, kmax, ax, bx, ldo)));
     GCGE_CHECK_LAUNCH();
     count_launch();
     return blocks;
