@@ -268,6 +268,10 @@ int borth(SolverCtx &c, SparseMat *B, double *x, int ldx, int nrows, int start, 
             k = kk;
             // the host buffer is reused next pass: wait for the upload
             GCGE_CUDA(cudaStreamSynchronize(st));
+            // two factorisations of a block with kappa < 1e5 leave it orthonormal
+            // to rounding (Cholesky-QR2 is stable for kappa^2 eps < 1): its
+            // Gram matrix need not be formed again to check
+            if (pass == 1 && kappa < 1e5) break;
         }
         if (start == 0 || kappa < 1e3) break;
     }
@@ -769,7 +773,7 @@ struct GcgRun {
             copy_cols(n, bsz, colp(ritz, offset[1]), ritz->ld, c.bbuf.p, ld, st);
         }
         if (ud != 1) {
-            bool have_sx = false;
+            bool have_sx = false;  // r64 holds S x0
             if (mixed && stored && ud == 0) {
                 // S x0 = A x0 + sigma B x0 from the stored products
                 int off = 0;
@@ -786,9 +790,30 @@ struct GcgRun {
             w_solve(colp(V, startW), bsz, mixed, have_sx);
         }
         timer.mark(PH_W);
+        if (mixed) normalise_w(colp(V, startW), endW - startW);
         endW = orth(colp(V, 0), ld, n, startW, endW, B != nullptr, g.compW_orth_zero_tol,
                     g.compW_orth_max_reorth, g.compW_orth_method, g.compW_orth_block_size);
         sizeW = endW - startW;
+    }
+
+    // Mixed solve: scale the new W columns to unit 2-norm before their
+    // B-orthogonalisation.  The span is unchanged; the CGS passes stop on an
+    // absolute coefficient bound (50 eps, src/ops_orth.c:404), which the
+    // block-PCG solutions (norms up to 1e3) miss by their norm, costing a
+    // third pass that unit columns do not need.
+    void normalise_w(double *x, int k) {
+        if (k <= 0) return;
+        coldot(n, k, x, ld, x, ld, c.dvec.p, c.gscr.p, c.gscr.n, st);
+        GCGE_CUDA(cudaMemcpyAsync(c.hbuf.p, c.dvec.p, sizeof(double) * k, cudaMemcpyDeviceToHost, st));
+        GCGE_CUDA(cudaStreamSynchronize(st));
+        for (int j = 0; j < k; ++j) {
+            const double v = c.hbuf.p[j];
+            c.hbuf.p[k + j] = (v > 0.0 && std::isfinite(v)) ? 1.0 / std::sqrt(v) : 1.0;
+        }
+        GCGE_CUDA(cudaMemcpyAsync(c.dvec.p, c.hbuf.p + k, sizeof(double) * k, cudaMemcpyHostToDevice,
+                                  st));
+        scale_columns(n, k, x, ld, c.dvec.p, st);
+        GCGE_CUDA(cudaStreamSynchronize(st));  // hbuf reuse
     }
 
     // BlockPCG on S x = b (b in c.bbuf, S = A + sigma B on the union pattern,
@@ -879,6 +904,7 @@ struct GcgRun {
         w_solve(colp(V, endW), bsz, mixed);
         endW += bsz;
         timer.mark(PH_W);
+        if (mixed) normalise_w(colp(V, startW), endW - startW);
         endW = orth(colp(V, 0), ld, n, startW, endW, B != nullptr, g.compW_orth_zero_tol,
                     g.compW_orth_max_reorth, g.compW_orth_method, g.compW_orth_block_size);
         sizeW = endW - startW;
@@ -948,88 +974,25 @@ struct GcgRun {
     // x^T A x / x^T B x of the returned vectors.  The Ritz values of the last
     // projection carry the basis' B-orthonormality error, which the digit-plane
     // products and the FP32 inner solve leave larger than the FP64 solve does
-    // (it reached ~3e-9 with ComputeW12); the quotients of vectors whose
-    // relative residual is below the tolerance are accurate to its square.
-    // If the converged vectors X_c themselves are B-orthonormal only to worse
-    // than 1e-10, a last Rayleigh-Ritz step on span(X_c) restores it:
-    // X_c <- X_c Z with H Z = G Z diag(lambda), G = X_c^T B X_c, H = X_c^T A X_c
-    // (Cholesky of G and FP64 Jacobi of the reduced matrix on the host).  The
-    // converged block ends at a gap (the back-off of CheckConvergence), so the
-    // rotation does not mix in unconverged vectors.
-    void final_rayleigh_ritz(double *eval, int k, int kc) {
+    // (up to ~1e-9 with ComputeW12); the quotients of vectors whose relative
+    // residual is below the tolerance are accurate to its square.  The vectors
+    // are returned as the iteration left them: a last Rayleigh-Ritz or Lowdin
+    // step would restore B-orthonormality but mixes vectors of a cluster,
+    // which can lift a residual just above the tolerance.
+    void rayleigh_quotients(double *eval, int k) {
         if (k <= 0) return;
         spmm<double>(A->pat, A->val.p, ritz->data, ritz->ld, c.T1.p, ld, k, st);
         spmm_calls++;
         applyB(ritz->data, ritz->ld, c.T2.p, ld, k);
-        double *dG = c.dtmp.p, *dH = c.dC.p;
-        dgram(c, n, k, k, ritz->data, ritz->ld, c.T2.p, ld, dG, k, c.gscr.p, c.gscr.n, st);
-        dgram(c, n, k, k, ritz->data, ritz->ld, c.T1.p, ld, dH, k, c.gscr.p, c.gscr.n, st);
-        std::vector<double> Gf((size_t)k * k), Hf((size_t)k * k);
-        GCGE_CUDA(cudaMemcpyAsync(Gf.data(), dG, sizeof(double) * k * k, cudaMemcpyDeviceToHost, st));
-        GCGE_CUDA(cudaMemcpyAsync(Hf.data(), dH, sizeof(double) * k * k, cudaMemcpyDeviceToHost, st));
+        coldot(n, k, ritz->data, ritz->ld, c.T1.p, ld, c.dvec.p, c.gscr.p, c.gscr.n, st);
+        coldot(n, k, ritz->data, ritz->ld, c.T2.p, ld, c.dvec.p + k, c.gscr.p, c.gscr.n, st);
+        GCGE_CUDA(cudaMemcpyAsync(c.hbuf.p, c.dvec.p, sizeof(double) * 2 * k,
+                                  cudaMemcpyDeviceToHost, st));
         GCGE_CUDA(cudaStreamSynchronize(st));
         for (int j = 0; j < k; ++j) {
-            const double q = Hf[j + (size_t)j * k] / Gf[j + (size_t)j * k];
-            if (Gf[j + (size_t)j * k] > 0.0 && std::isfinite(q)) eval[j] = q;
+            const double num = c.hbuf.p[j], den = c.hbuf.p[k + j];
+            if (den > 0.0 && std::isfinite(num / den)) eval[j] = num / den;
         }
-        kc = std::min(kc, k);
-        if (kc <= 0) return;
-        double e = 0.0;
-        for (int a = 0; a < kc; ++a)
-            for (int b = 0; b < kc; ++b)
-                e = std::max(e, std::fabs(Gf[a + (size_t)b * k] - (a == b ? 1.0 : 0.0)));
-        if (!std::isfinite(e) || e < 1e-10) return;
-        const int kf = k;
-        k = kc;  // the leading kc x kc blocks
-        std::vector<double> G((size_t)k * k), H((size_t)k * k);
-        for (int b = 0; b < k; ++b)
-            for (int a = 0; a < k; ++a) {
-                G[a + (size_t)b * k] = Gf[a + (size_t)b * kf];
-                H[a + (size_t)b * k] = Hf[a + (size_t)b * kf];
-            }
-        // G = L L^T (lower, column-major); C = L^-1 H L^-T
-        std::vector<double> L((size_t)k * k, 0.0);
-        for (int j = 0; j < k; ++j) {
-            double d = 0.5 * (G[j + (size_t)j * k] + G[j + (size_t)j * k]);
-            for (int l = 0; l < j; ++l) d -= L[j + (size_t)l * k] * L[j + (size_t)l * k];
-            if (!(d > 0.0)) return;  // not positive definite: keep the vectors as they are
-            L[j + (size_t)j * k] = std::sqrt(d);
-            for (int i = j + 1; i < k; ++i) {
-                double v = 0.5 * (G[i + (size_t)j * k] + G[j + (size_t)i * k]);
-                for (int l = 0; l < j; ++l) v -= L[i + (size_t)l * k] * L[j + (size_t)l * k];
-                L[i + (size_t)j * k] = v / L[j + (size_t)j * k];
-            }
-        }
-        auto lsolve = [&](std::vector<double> &Mx) {  // Mx <- L^-1 Mx (column by column)
-            for (int col = 0; col < k; ++col)
-                for (int i = 0; i < k; ++i) {
-                    double v = Mx[i + (size_t)col * k];
-                    for (int l = 0; l < i; ++l) v -= L[i + (size_t)l * k] * Mx[l + (size_t)col * k];
-                    Mx[i + (size_t)col * k] = v / L[i + (size_t)i * k];
-                }
-        };
-        std::vector<double> Cm(H);
-        lsolve(Cm);  // L^-1 H
-        std::vector<double> Ct((size_t)k * k);
-        for (int a = 0; a < k; ++a)
-            for (int b = 0; b < k; ++b) Ct[a + (size_t)b * k] = Cm[b + (size_t)a * k];
-        lsolve(Ct);  // L^-1 (L^-1 H)^T = L^-1 H L^-T (H symmetric)
-        std::vector<double> w(k), Y((size_t)k * k);
-        host_eigh(k, Ct.data(), w.data(), Y.data());
-        // Z = L^-T Y (back substitution with L^T)
-        std::vector<double> Z(Y);
-        for (int col = 0; col < k; ++col)
-            for (int i = k - 1; i >= 0; --i) {
-                double v = Z[i + (size_t)col * k];
-                for (int l = i + 1; l < k; ++l) v -= L[l + (size_t)i * k] * Z[l + (size_t)col * k];
-                Z[i + (size_t)col * k] = v / L[i + (size_t)i * k];
-            }
-        GCGE_CUDA(cudaMemcpyAsync(c.dC.p, Z.data(), sizeof(double) * k * k, cudaMemcpyHostToDevice,
-                                  st));
-        dlincomb(c, n, k, k, ritz->data, ritz->ld, c.dC.p, k, c.T1.p, ld, nullptr, 0, st);
-        copy_cols(n, k, c.T1.p, ld, ritz->data, ritz->ld, st);
-        GCGE_CUDA(cudaStreamSynchronize(st));
-        for (int j = 0; j < k; ++j) eval[j] = w[j];
     }
 
     // ---------------- GCG outer loop (:1259-1562)
@@ -1120,7 +1083,7 @@ struct GcgRun {
         } while (numIter < numIterMax);
         g.numIter = numIter + (g.numIterMax - numIterMax);
         for (int i = 0; i < sizeX; ++i) eval[i] = ss_eval[i];
-        if (c.precision == GCGE_PREC_MIXED) final_rayleigh_ritz(eval, sizeX, std::min(nevc, sizeX));
+        if (c.precision == GCGE_PREC_MIXED) rayleigh_quotients(eval, sizeX);
         *nevConvIO = nevc;
         g.nevConv = nevc;
         timer.mark(PH_NONE);
