@@ -44,7 +44,7 @@ EXPORTED_SYMBOLS = [
     "GCGE_DenseLinComb", "GCGE_HostAlloc", "GCGE_HostFree", "GCGE_ServerCreate",
     "GCGE_ServerSubmit", "GCGE_ServerWait", "GCGE_ServerDestroy", "GCGE_SolveBatch",
     "MultiVecOrthSetup_ModifiedGramSchmidt", "MultiVecOrthSetup_BinaryGramSchmidt",
-    "EigenSolverSetParametersFromCommandLine_GCG",
+    "EigenSolverSetParametersFromCommandLine_GCG", "CUDA_MatAxpby",
 ]
 
 _lib = None
@@ -503,6 +503,11 @@ class CudaOps:
             raise GCGEError(st, "CUDA_MatCreateFromCCS")
         self._mats.append(h)
         return h
+
+    def mat_axpby(self, alpha, X, beta, Y):
+        """CUDA_MatAxpby: Y = alpha X + beta Y (the OPS MatAxpby slot)."""
+        self.lib.CUDA_MatAxpby(ctypes.c_double(alpha), X, ctypes.c_double(beta), Y, self.ptr)
+        self.check("CUDA_MatAxpby")
 
     def multivec(self, mat, ncols, host=None):
         h = _VP()

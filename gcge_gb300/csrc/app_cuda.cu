@@ -753,6 +753,45 @@ void CUDA_MatDestroy(void **mat) {
     delete A;
     *mat = nullptr;
 }
+// ops->MatAxpby (src/ops.h:52: Y = alpha X + beta Y).  app_ccs leaves the slot
+// NULL, and so does OPS_CUDA_Set, so GCG takes the same branch as with the
+// reference's CCS backend (src/ops_eig_sol_gcg.c:600-631); the GPU GCG forms
+// A + sigma B on the union pattern of A and B itself.  A caller may install
+// CUDA_MatAxpby in the slot.  Y takes the union pattern of X and Y (rebuilt
+// on the device) and a new identity, so solver caches keyed on Y rebuild.
+void CUDA_MatAxpby(double alpha, void *matX, double beta, void *matY, OPS *ops) {
+    (void)ops;
+    try {
+        SparseMat *X = as_mat(matX), *Y = as_mat(matY);
+        GCGE_REQUIRE(X && Y, GCGE_ERR_HANDLE, "MatAxpby: matrices");
+        GCGE_REQUIRE(X->n == Y->n, GCGE_ERR_ARG, "MatAxpby: sizes differ");
+        cudaStream_t st = lib_stream();
+        DevCsr U;
+        DevBuf<double> yv;
+        if (X == Y) {  // Y = (alpha + beta) Y on its own pattern
+            const double f = alpha + beta;
+            axpby((int)Y->csr.nnz, 1, 0.0, nullptr, 0, f, Y->csr.val.p, (int)Y->csr.nnz, st);
+        } else {
+            // values of X on the union in U.val, values of Y in yv
+            union_csr_device(X->csr, &Y->csr, U, yv, st);
+            axpby((int)U.nnz, 1, alpha, U.val.p, (int)U.nnz, beta, yv.p, (int)U.nnz, st);
+            std::swap(Y->csr.ptr.p, U.ptr.p);
+            std::swap(Y->csr.ptr.n, U.ptr.n);
+            std::swap(Y->csr.ind.p, U.ind.p);
+            std::swap(Y->csr.ind.n, U.ind.n);
+            std::swap(Y->csr.val.p, yv.p);
+            std::swap(Y->csr.val.n, yv.n);
+            Y->csr.nnz = U.nnz;
+            Y->nnz = U.nnz;
+        }
+        sell_from_csr_device(Y->csr, nullptr, Y->pat, Y->val, nullptr, st);
+        Y->serial = g_serial.fetch_add(1);
+        GCGE_CUDA(cudaStreamSynchronize(st));
+    } catch (const CudaError &e) {
+        set_error(e.status, e.where.c_str());
+    }
+}
+
 int CUDA_MatNnz(void *mat, long long *nnz) {
     SparseMat *A = as_mat(mat);
     if (!A) return GCGE_ERR_HANDLE;

@@ -647,6 +647,35 @@ struct GcgRun {
     }
     std::vector<double> last_res;
     int iter_print = 0;
+    bool restart_pending = false;
+
+    // At the switch to FP64: the digit-plane products and the FP32 inner solve
+    // leave the basis B-orthonormal only to ~1e-11..1e-10, and the Ritz pairs
+    // of such a basis cannot reach a relative residual below that error times
+    // the spread of the spectrum (1e-8 on anisotropic problems: pairs stall at
+    // 1.5e-8 in FP64 too, since the X block is carried from iteration to
+    // iteration and never re-orthonormalised).  The unlocked Ritz vectors are
+    // therefore B-orthonormalised against the locked ones and among themselves
+    // in FP64, re-diagonalised by a Rayleigh-Ritz step on their span, and the
+    // next iteration builds no P (the P coefficients refer to the old basis).
+    bool restart_active() {
+        const int k = sizeX - sizeC;
+        if (k <= 0) return false;
+        double *Xa = colp(ritz, sizeC);
+        const int e = borth(c, B, ritz->data, ritz->ld, n, sizeC, sizeX, B != nullptr,
+                            g.compW_orth_zero_tol, g.compW_orth_max_reorth, &spmm_calls);
+        GCGE_REQUIRE(e == sizeX, GCGE_ERR_NUMERIC, "restart: Ritz vectors became dependent");
+        spmm<double>(A->pat, A->val.p, Xa, ritz->ld, c.T1.p, ld, k, st);
+        spmm_calls++;
+        gram(n, k, k, Xa, ritz->ld, c.T1.p, ld, c.dtmp.p, k, c.gscr.p, c.gscr.n, st);
+        std::vector<double> w(k);
+        sym_eig(c.eig, k, c.dtmp.p, k, w.data(), c.evec.p, k, c.refine_steps, st);
+        lincomb(n, k, k, Xa, ritz->ld, c.evec.p, k, c.T1.p, ld, nullptr, 0, st);
+        copy_cols(n, k, c.T1.p, ld, Xa, ritz->ld, st);
+        for (int i = 0; i < k; ++i) ss_eval[sizeC + i] = w[i];
+        GCGE_CUDA(cudaStreamSynchronize(st));
+        return true;
+    }
 
     // Precision escalation of the mixed solve.  The FP32 inner solve sees the
     // shifted operator with entry errors of about eps32 |S|, which the
@@ -671,6 +700,7 @@ struct GcgRun {
         if (near_tol && cur.first <= old.first && cur.second > 0.5 * old.second) {
             c.escalated = true;
             escalated_at = iter_print + 1;
+            restart_pending = true;
             if (g.print)
                 printf("%3d mixed precision: residual %6.5e stalled near the tolerance, FP64 from here\n",
                        escalated_at, cur.second);
@@ -790,30 +820,9 @@ struct GcgRun {
             w_solve(colp(V, startW), bsz, mixed, have_sx);
         }
         timer.mark(PH_W);
-        if (mixed) normalise_w(colp(V, startW), endW - startW);
         endW = orth(colp(V, 0), ld, n, startW, endW, B != nullptr, g.compW_orth_zero_tol,
                     g.compW_orth_max_reorth, g.compW_orth_method, g.compW_orth_block_size);
         sizeW = endW - startW;
-    }
-
-    // Mixed solve: scale the new W columns to unit 2-norm before their
-    // B-orthogonalisation.  The span is unchanged; the CGS passes stop on an
-    // absolute coefficient bound (50 eps, src/ops_orth.c:404), which the
-    // block-PCG solutions (norms up to 1e3) miss by their norm, costing a
-    // third pass that unit columns do not need.
-    void normalise_w(double *x, int k) {
-        if (k <= 0) return;
-        coldot(n, k, x, ld, x, ld, c.dvec.p, c.gscr.p, c.gscr.n, st);
-        GCGE_CUDA(cudaMemcpyAsync(c.hbuf.p, c.dvec.p, sizeof(double) * k, cudaMemcpyDeviceToHost, st));
-        GCGE_CUDA(cudaStreamSynchronize(st));
-        for (int j = 0; j < k; ++j) {
-            const double v = c.hbuf.p[j];
-            c.hbuf.p[k + j] = (v > 0.0 && std::isfinite(v)) ? 1.0 / std::sqrt(v) : 1.0;
-        }
-        GCGE_CUDA(cudaMemcpyAsync(c.dvec.p, c.hbuf.p + k, sizeof(double) * k, cudaMemcpyHostToDevice,
-                                  st));
-        scale_columns(n, k, x, ld, c.dvec.p, st);
-        GCGE_CUDA(cudaStreamSynchronize(st));  // hbuf reuse
     }
 
     // BlockPCG on S x = b (b in c.bbuf, S = A + sigma B on the union pattern,
@@ -904,7 +913,6 @@ struct GcgRun {
         w_solve(colp(V, endW), bsz, mixed);
         endW += bsz;
         timer.mark(PH_W);
-        if (mixed) normalise_w(colp(V, startW), endW - startW);
         endW = orth(colp(V, 0), ld, n, startW, endW, B != nullptr, g.compW_orth_zero_tol,
                     g.compW_orth_max_reorth, g.compW_orth_method, g.compW_orth_block_size);
         sizeW = endW - startW;
@@ -1062,7 +1070,12 @@ struct GcgRun {
                 numIterMax -= numIter;
                 numIter = 0;
             }
-            if (numIter == 0) {
+            bool restarted = false;
+            if (restart_pending) {
+                restart_pending = false;
+                restarted = restart_active();
+            }
+            if (numIter == 0 || restarted) {
                 sizeP = 0;
                 startP = endX;
                 endP = startP;

@@ -65,6 +65,13 @@ int CUDA_MatCreateFromCCS(void **mat, int nrows, int ncols, const int *j_col, co
 void CUDA_MatDestroy(void **mat);
 int CUDA_MatNnz(void *mat, long long *nnz);
 
+/* Y = alpha X + beta Y for device matrices: the OPS MatAxpby slot
+ * (src/ops.h:52, used by src/ops_eig_sol_gcg.c:600-631 and :730-744 for the
+ * in-place shift A + sigma B).  Y takes the union pattern of X and Y.
+ * OPS_CUDA_Set leaves ops->MatAxpby NULL, as app_ccs does; install this
+ * function there to provide the slot.  Failures go to ops_cuda_last_error(). */
+void CUDA_MatAxpby(double alpha, void *matX, double beta, void *matY, struct OPS_ *ops);
+
 /* Copy columns [start, end) between a device multivector and a host
  * column-major array with leading dimension ldh >= nrows. */
 int CUDA_MultiVecSetFromHost(void **mv, int start, int end, const double *host, int ldh);

@@ -1,5 +1,7 @@
 """OPS slots of the CUDA backend against the reference backends' semantics
 (app/app_ccs.c, app/app_lapack.c, src/ops_multi_vec.c), restated in numpy."""
+import ctypes
+
 import numpy as np
 import pytest
 
@@ -172,3 +174,36 @@ def test_bad_handles_and_ranges_report_errors(ops, gpu_lib):
         ops.axpby(1.0, x, 1.0, y, (0, 0), (9, 9))       # out of range
     with pytest.raises(gpu_lib.GCGEError):
         ops.mat_dot(hA, x, y, (0, 0), (2, 3))            # mismatched ranges
+
+
+def test_mat_axpby_union_pattern(gpu_lib):
+    """CUDA_MatAxpby (the OPS MatAxpby slot, src/ops.h:52): Y = alpha X + beta Y
+    for matrices with different patterns, checked through MatDotMultiVec
+    against scipy; X == Y scales in place."""
+    import scipy.sparse as sp
+    G = gpu_lib
+    n = 3000
+    X = P.laplace2d(60, 50)
+    Y = P.diag_matrix(0.5 + P.splitmix_uniform(5, n, 0))
+    Xs, Ys = X.to_scipy(), Y.to_scipy()
+    rng = np.random.default_rng(7)
+    v = rng.standard_normal((n, 5))
+    ops = G.CudaOps()
+    try:
+        hX, hY = ops.mat(X), ops.mat(Y)
+        ops.mat_axpby(0.75, hX, -2.0, hY)
+        nnz = ctypes.c_longlong()
+        G.load().CUDA_MatNnz(hY, ctypes.byref(nnz))
+        assert nnz.value == (0.75 * Xs - 2.0 * Ys).nnz
+        hv = ops.multivec(hY, 5, v)
+        hw = ops.multivec(hY, 5)
+        ops.mat_dot(hY, hv, hw, (0, 0), (5, 5))
+        np.testing.assert_allclose(ops.download(hw, 0, 5), (0.75 * Xs - 2.0 * Ys) @ v,
+                                   rtol=1e-14, atol=1e-13)
+        ops.mat_axpby(1.5, hY, 0.5, hY)   # Y = 2 Y
+        ops.mat_dot(hY, hv, hw, (0, 0), (5, 5))
+        np.testing.assert_allclose(ops.download(hw, 0, 5), 2.0 * ((0.75 * Xs - 2.0 * Ys) @ v),
+                                   rtol=1e-14, atol=1e-13)
+        assert ops.ptr.contents.MatAxpby is None   # the slot stays NULL, as in app_ccs
+    finally:
+        ops.close()

@@ -94,9 +94,9 @@ def test_orth_and_w12_solves_match_reference(gpu_lib, golden_orth, case, precisi
     As, Bs = A.to_scipy(), None if B is None else B.to_scipy()
     BX = X if Bs is None else Bs @ X
     # the mixed solve's basis drifts from B-orthonormality (digit-plane
-    # products, FP32 inner solve); ComputeW12's two nearly parallel directions
-    # per pair amplify it to ~1e-9 on these cases
-    orth_tol = 1e-8 if (precision == "mixed" and "w12" in case) else 1e-10
+    # products, FP32 inner solve) to ~1e-10; ComputeW12's two nearly parallel
+    # directions per pair amplify it to ~1e-9 on these cases
+    orth_tol = 1e-10 if precision == "fp64" else (1e-8 if "w12" in case else 1e-9)
     assert np.abs(X.T @ BX - np.eye(nev)).max() < orth_tol
     res = np.linalg.norm(As @ X - BX * r.eval[:nev], axis=0)
     assert np.all(res <= g["tol"][1] * np.abs(r.eval[:nev]) * 1.0001)
