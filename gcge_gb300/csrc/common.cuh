@@ -208,7 +208,10 @@ void oz_gram(int n, int m, int w, const double *Q, int ldq, const double *P, int
              int ldc, double *scratch, size_t scratch_elems, cudaStream_t st);
 void oz_lincomb(int n, int k, int m, const double *X, int ldx, const double *C, int ldc,
                 double *Y, int ldy, const double *beta_dev, int incb, cudaStream_t st,
-                double alpha = 1.0);
+                double alpha,
+                void *scratch, size_t scratch_bytes);
+// Scratch bytes oz_lincomb needs for k terms and m columns.
+size_t oz_lincomb_scratch_bytes(int k, int m);
 // per-column dots out[c] = X(:,c) . Y(:,c)
 void coldot(int n, int k, const double *X, int ldx, const double *Y, int ldy, double *out,
             double *scratch, size_t scratch_elems, cudaStream_t st);

@@ -93,6 +93,7 @@ void SolverCtx::reserve(int n_, int nev_max, int nev_init, int bs, int spmm_nblo
                                     gram_scratch_elems(n_, cols, cols),
                                 2u << 20));
     part.alloc((size_t)std::max(spmm_nblocks, 1) * 64);
+    ozb.alloc(oz_lincomb_scratch_bytes(std::max(smax, cols), std::max(smax, cols)));
     dmax.alloc(4);
     hmax.alloc(4);
     if (one.p == nullptr) {
@@ -148,7 +149,7 @@ static void dlincomb(const SolverCtx &c, int n, int k, int m, const double *X, i
                      const double *C, int ldc, double *Y, int ldy, const double *beta, int incb,
                      cudaStream_t st, double alpha = 1.0) {
     if (c.precision == GCGE_PREC_MIXED && !c.escalated)
-        oz_lincomb(n, k, m, X, ldx, C, ldc, Y, ldy, beta, incb, st, alpha);
+        oz_lincomb(n, k, m, X, ldx, C, ldc, Y, ldy, beta, incb, st, alpha, c.ozb.p, c.ozb.n);
     else
         lincomb(n, k, m, X, ldx, C, ldc, Y, ldy, beta, incb, st, alpha);
 }

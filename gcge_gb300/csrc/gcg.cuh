@@ -34,6 +34,8 @@ struct SolverCtx {
     // A x and B x of the Ritz vectors CheckConvergence tested (n x numCheck),
     // reused by ComputeW for its right-hand side and initial residual
     DevBuf<double> chkA, chkB;
+    // right-operand digit planes of the mixed solve's linear combinations
+    DevBuf<unsigned char> ozb;
     DevBuf<int> dmask, didx;
     PinnedBuf<double> hbuf, hmax;
     EigWork eig;

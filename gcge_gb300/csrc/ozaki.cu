@@ -239,7 +239,44 @@ struct OzArgs {
     const double *beta;
     int incb;
     double alpha;
+    // lincomb: the right operand's exponent fields and digit planes, prepared
+    // once per call (k_oz_bprep) instead of by every CTA of the long operand
+    const uint16_t *bplanes;  // [tile][chunk][kDigits][BN][kBKP]
+    const int *bexps;         // [tile][super-chunk][BN]
+    int nchunks, nsup;
 };
+
+// Exponent fields and digit planes of the right operand of a linear
+// combination (C, K x N, k-contiguous), for every super-chunk and chunk of K
+// and every BN-column tile: block (super-chunk, tile).  The same device
+// functions as the product kernel fill shared memory, which is then copied
+// out, so the planes are bit for bit those the product kernel would make.
+template <int BN>
+__global__ void __launch_bounds__(oz_threads<BN>()) k_oz_bprep(const double *__restrict__ C,
+                                                              size_t ldc, int N, int K,
+                                                              uint16_t *__restrict__ planes,
+                                                              int *__restrict__ exps, int nchunks,
+                                                              int nsup) {
+    constexpr int NT = oz_threads<BN>();
+    constexpr int nwarps = NT / 32;
+    constexpr int PL = kDigits * BN * kBKP;  // uint16 per chunk
+    __shared__ __align__(16) uint16_t b[kDigits][BN][kBKP];
+    __shared__ int eb[BN];
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int s = blockIdx.x, nt = blockIdx.y, nt0 = nt * BN;
+    const int sk = s * kSuper * kBK, ske = min(K, sk + kSuper * kBK);
+    exps_kcontig<BN>(C, ldc, nt0, N, sk, ske, eb, warp, nwarps, lane);
+    __syncthreads();
+    for (int i = tid; i < BN; i += NT) exps[((size_t)nt * nsup + s) * BN + i] = eb[i];
+    for (int k0 = sk; k0 < ske; k0 += kBK) {
+        planes_kcontig<BN>(C, ldc, nt0, N, k0, ske, b, eb, warp, nwarps, lane);
+        __syncthreads();
+        const uint4 *src = reinterpret_cast<const uint4 *>(&b[0][0][0]);
+        uint4 *dst = reinterpret_cast<uint4 *>(planes + ((size_t)nt * nchunks + k0 / kBK) * PL);
+        for (int i = tid; i < PL / 8; i += NT) dst[i] = src[i];
+        __syncthreads();
+    }
+}
 
 template <int BN, bool GRAM>
 __global__ void __launch_bounds__(oz_threads<BN>(), 2) k_oz_gemm(OzArgs a) {
@@ -269,7 +306,12 @@ __global__ void __launch_bounds__(oz_threads<BN>(), 2) k_oz_gemm(OzArgs a) {
             __syncthreads();
             exps_mcontig<NT>(a.A, a.lda, mt0, a.M, sk, ske, sm.ea, tid);
         }
-        exps_kcontig<BN>(a.B, a.ldb, nt0, a.N, sk, ske, sm.eb, warp, nwarps, lane);
+        if constexpr (GRAM) {
+            exps_kcontig<BN>(a.B, a.ldb, nt0, a.N, sk, ske, sm.eb, warp, nwarps, lane);
+        } else {
+            const int *e = a.bexps + ((size_t)blockIdx.y * a.nsup + sk / (kSuper * kBK)) * BN;
+            for (int i = tid; i < BN; i += NT) sm.eb[i] = e[i];
+        }
         __syncthreads();
         long long thi[4] = {0, 0, 0, 0}, tlo[4] = {0, 0, 0, 0};
         for (int k0 = sk; k0 < ske; k0 += kBK) {
@@ -277,7 +319,15 @@ __global__ void __launch_bounds__(oz_threads<BN>(), 2) k_oz_gemm(OzArgs a) {
                 planes_kcontig<kBM>(a.A, a.lda, mt0, a.M, k0, ske, sm.a, sm.ea, warp, nwarps, lane);
             else
                 planes_mcontig<NT>(a.A, a.lda, mt0, a.M, k0, ske, sm.a, sm.ea, tid);
-            planes_kcontig<BN>(a.B, a.ldb, nt0, a.N, k0, ske, sm.b, sm.eb, warp, nwarps, lane);
+            if constexpr (GRAM) {
+                planes_kcontig<BN>(a.B, a.ldb, nt0, a.N, k0, ske, sm.b, sm.eb, warp, nwarps, lane);
+            } else {
+                constexpr int PL = kDigits * BN * kBKP;
+                const uint4 *src = reinterpret_cast<const uint4 *>(
+                    a.bplanes + ((size_t)blockIdx.y * a.nchunks + k0 / kBK) * PL);
+                uint4 *dst = reinterpret_cast<uint4 *>(&sm.b[0][0][0]);
+                for (int i = tid; i < PL / 8; i += NT) dst[i] = src[i];
+            }
             __syncthreads();
 
             float lv[kDigits][4];
@@ -396,6 +446,32 @@ void launch_oz(const OzArgs &a, dim3 grid, cudaStream_t st) {
 
 int oz_tile_n(int n) { return n <= 8 ? 8 : (n <= 16 ? 16 : 24); }
 
+// Bytes of the right-operand planes and exponent fields of a linear
+// combination with k terms and m columns in tiles of bn columns.
+size_t bprep_bytes(int k, int m, int bn) {
+    const size_t ntiles = (size_t)(m + bn - 1) / bn;
+    const size_t nchunks = (size_t)(k + kBK - 1) / kBK;
+    const size_t nsup = (size_t)(k + kSuper * kBK - 1) / (kSuper * kBK);
+    return ntiles * nchunks * kDigits * bn * kBKP * sizeof(uint16_t) +
+           ntiles * nsup * bn * sizeof(int) + 256;
+}
+
+template <int BN>
+void prep_b(OzArgs &a, int ntiles, void *scratch, cudaStream_t st) {
+    a.nchunks = (a.K + kBK - 1) / kBK;
+    a.nsup = (a.K + kSuper * kBK - 1) / (kSuper * kBK);
+    uint16_t *planes = static_cast<uint16_t *>(scratch);
+    const size_t pl = (size_t)ntiles * a.nchunks * kDigits * BN * kBKP;
+    int *exps = reinterpret_cast<int *>(
+        (reinterpret_cast<uintptr_t>(planes + pl) + 255) & ~(uintptr_t)255);
+    k_oz_bprep<BN><<<dim3(a.nsup, ntiles), oz_threads<BN>(), 0, st>>>(
+        a.B, a.ldb, a.N, a.K, planes, exps, a.nchunks, a.nsup);
+    GCGE_CHECK_LAUNCH();
+    count_launch();
+    a.bplanes = planes;
+    a.bexps = exps;
+}
+
 template <bool GRAM>
 void launch_oz_bn(const OzArgs &a, int bn, dim3 grid, cudaStream_t st) {
     switch (bn) {
@@ -445,9 +521,11 @@ void oz_gram(int n, int m, int w, const double *Q, int ldq, const double *P, int
 
 // Y (n x m, ldy) = alpha X C + Y diag(beta) for X n x k (ldx), C k x m (ldc);
 // beta == nullptr overwrites Y; incb == 0 broadcasts beta[0].
+size_t oz_lincomb_scratch_bytes(int k, int m) { return bprep_bytes(k, m, oz_tile_n(m)); }
+
 void oz_lincomb(int n, int k, int m, const double *X, int ldx, const double *C, int ldc,
                 double *Y, int ldy, const double *beta_dev, int incb, cudaStream_t st,
-                double alpha) {
+                double alpha, void *scratch, size_t scratch_bytes) {
     if (n <= 0 || m <= 0) return;
     if (k <= 0) {
         lincomb(n, k, m, X, ldx, C, ldc, Y, ldy, beta_dev, incb, st, alpha);
@@ -468,7 +546,15 @@ void oz_lincomb(int n, int k, int m, const double *X, int ldx, const double *C, 
     a.beta = beta_dev;
     a.incb = incb;
     a.alpha = alpha;
-    launch_oz_bn<false>(a, bn, dim3((n + kBM - 1) / kBM, (m + bn - 1) / bn, 1), st);
+    const int ntiles = (m + bn - 1) / bn;
+    GCGE_REQUIRE(scratch && scratch_bytes >= bprep_bytes(k, m, bn), GCGE_ERR_ARG,
+                 "oz_lincomb: scratch too small");
+    switch (bn) {
+        case 8: prep_b<8>(a, ntiles, scratch, st); break;
+        case 16: prep_b<16>(a, ntiles, scratch, st); break;
+        default: prep_b<24>(a, ntiles, scratch, st); break;
+    }
+    launch_oz_bn<false>(a, bn, dim3((n + kBM - 1) / kBM, ntiles, 1), st);
 }
 
 }  // namespace gcge

@@ -159,9 +159,12 @@ int GCGE_DenseLinComb(int n, int k, int m, const double *X, int ldx, const doubl
             GCGE_CUDA(cudaMemcpyAsync(dB.p, beta, sizeof(double) * m, cudaMemcpyHostToDevice, st));
             bp = dB.p;
         }
-        if (emulated)
-            oz_lincomb(n, k, m, dX.p, n, dC.p, std::max(k, 1), dY.p, n, bp, 1, st, alpha);
-        else
+        DevBuf<unsigned char> ozb;
+        if (emulated) {
+            ozb.alloc(oz_lincomb_scratch_bytes(k, m));
+            oz_lincomb(n, k, m, dX.p, n, dC.p, std::max(k, 1), dY.p, n, bp, 1, st, alpha, ozb.p,
+                       ozb.n);
+        } else
             lincomb(n, k, m, dX.p, n, dC.p, std::max(k, 1), dY.p, n, bp, 1, st, alpha);
         GCGE_CUDA(cudaMemcpy2DAsync(Y, sizeof(double) * ldy, dY.p, sizeof(double) * n,
                                     sizeof(double) * n, m, cudaMemcpyDeviceToHost, st));
