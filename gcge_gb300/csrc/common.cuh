@@ -181,9 +181,10 @@ template <typename T>
 void spmm(const SellPattern &pat, const T *val, const T *X, int ldx, T *Y, int ldy, int k,
           cudaStream_t st);
 // partial[block*kmax+c] = sum over the block's rows of r^2 with r = (A - lam_c B) x_c
-int residual_norms(const SellPattern &pat, const double *a, const double *b, const double *X,
-                   int ldx, const double *lam, int k, double *partial, int kmax, cudaStream_t st,
-                   double *ax = nullptr, double *bx = nullptr, int ldo = 0);
+int residual_norms(const SellPattern &pa, const double *va, const SellPattern *pb,
+                   const double *vb, const double *X, int ldx, const double *lam, int k,
+                   double *partial, int kmax, cudaStream_t st, double *ax = nullptr,
+                   double *bx = nullptr, int ldo = 0);
 int spmm_blocks(const SellPattern &pat);
 // Smallest block-PCG row width >= k (whole 16-byte column groups).
 int rows_width(int k, int elem_bytes);

@@ -580,9 +580,10 @@ struct GcgRun {
             const int kc = std::min(40, numCheck - c0);
             GCGE_CUDA(cudaMemcpyAsync(c.dvec.p, &ss_eval[startN + c0], sizeof(double) * kc,
                                       cudaMemcpyHostToDevice, st));
-            const int nb = residual_norms(c.upat, c.ua.p, c.ub.p, colp(ritz, startN + c0), ritz->ld,
-                                          c.dvec.p, kc, c.part.p, 64, st, c.chkA.p + (size_t)c0 * ld,
-                                          c.chkB.p + (size_t)c0 * ld, ld);
+            const int nb = residual_norms(A->pat, A->val.p, B ? &B->pat : nullptr,
+                                          B ? B->val.p : nullptr, colp(ritz, startN + c0),
+                                          ritz->ld, c.dvec.p, kc, c.part.p, 64, st,
+                                          c.chkA.p + (size_t)c0 * ld, c.chkB.p + (size_t)c0 * ld, ld);
             spmm_calls++;
             reduce_partials(c.part.p, nb, 64, kc, c.dvec.p + 64, st);
             GCGE_CUDA(cudaMemcpyAsync(c.hbuf.p + c0, c.dvec.p + 64, sizeof(double) * kc,

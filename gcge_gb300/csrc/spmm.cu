@@ -52,8 +52,9 @@ k_spmm(const long long *__restrict__ sp, const int *__restrict__ col, const T *_
 
 template <int K>
 __global__ void __launch_bounds__(kSpmmThreads)
-k_residual(const long long *__restrict__ sp, const int *__restrict__ col,
-           const double *__restrict__ a, const double *__restrict__ b, int n, int nslices,
+k_residual(const long long *__restrict__ sa, const int *__restrict__ ca,
+           const double *__restrict__ va, const long long *__restrict__ sb,
+           const int *__restrict__ cb, const double *__restrict__ vb, int n, int nslices,
            const double *__restrict__ X, int ldx, const double *__restrict__ lam, int k,
            double *__restrict__ partial, int kmax, double *__restrict__ ax,
            double *__restrict__ bx, int ldo) {
@@ -63,38 +64,33 @@ k_residual(const long long *__restrict__ sp, const int *__restrict__ col,
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     for (int c = threadIdx.x; c < K; c += blockDim.x) slam[c] = c < k ? lam[c] : 0.0;
     __syncthreads();
-    // A x and B x accumulated separately (as the reference's two SpMMs and
-    // axpby, src/ops_eig_sol_gcg.c:220-238), skipping stored zeros of either
-    // value array: on a union pattern most entries belong to one matrix only
+    // A x and B x, each on its own matrix's SELL pattern (as the reference's
+    // two SpMMs and axpby, src/ops_eig_sol_gcg.c:220-238); padding entries
+    // carry a zero value and the row's own column
     double acc[K], bcc[K];
 #pragma unroll
     for (int c = 0; c < K; ++c) acc[c] = bcc[c] = 0.0;
     const int row = slice * 32 + lane;
     if (slice < nslices) {
-        const long long beg = sp[slice], end = sp[slice + 1];
-        for (long long e = beg + lane; e < end; e += 32) {
-            const int j = __ldg(col + e);
-            const double av = __ldg(a + e), bv = __ldg(b + e);
-            const double *xj = X + j;
-            if (av != 0.0) {
-                if (bv != 0.0) {
+        for (long long e = sa[slice] + lane, end = sa[slice + 1]; e < end; e += 32) {
+            const double v = __ldg(va + e);
+            const double *xj = X + __ldg(ca + e);
 #pragma unroll
-                    for (int c = 0; c < K; ++c)
-                        if (c < k) {
-                            const double x = __ldg(xj + (size_t)c * ldx);
-                            acc[c] = fma(av, x, acc[c]);
-                            bcc[c] = fma(bv, x, bcc[c]);
-                        }
-                } else {
-#pragma unroll
-                    for (int c = 0; c < K; ++c)
-                        if (c < k) acc[c] = fma(av, __ldg(xj + (size_t)c * ldx), acc[c]);
-                }
-            } else if (bv != 0.0) {
+            for (int c = 0; c < K; ++c)
+                if (c < k) acc[c] = fma(v, __ldg(xj + (size_t)c * ldx), acc[c]);
+        }
+        if (sb != nullptr) {
+            for (long long e = sb[slice] + lane, end = sb[slice + 1]; e < end; e += 32) {
+                const double v = __ldg(vb + e);
+                const double *xj = X + __ldg(cb + e);
 #pragma unroll
                 for (int c = 0; c < K; ++c)
-                    if (c < k) bcc[c] = fma(bv, __ldg(xj + (size_t)c * ldx), bcc[c]);
+                    if (c < k) bcc[c] = fma(v, __ldg(xj + (size_t)c * ldx), bcc[c]);
             }
+        } else if (row < n) {  // B = I
+#pragma unroll
+            for (int c = 0; c < K; ++c)
+                if (c < k) bcc[c] = X[row + (size_t)c * ldx];
         }
     }
     if (ax != nullptr && row < n) {  // keep A x and B x for the W step
@@ -149,14 +145,17 @@ void spmm(const SellPattern &pat, const T *val, const T *X, int ldx, T *Y, int l
     }
 }
 
-int residual_norms(const SellPattern &pat, const double *a, const double *b, const double *X,
-                   int ldx, const double *lam, int k, double *partial, int kmax, cudaStream_t st,
-                   double *ax, double *bx, int ldo) {
+int residual_norms(const SellPattern &pa, const double *va, const SellPattern *pb,
+                   const double *vb, const double *X, int ldx, const double *lam, int k,
+                   double *partial, int kmax, cudaStream_t st, double *ax, double *bx, int ldo) {
     GCGE_REQUIRE(k <= kMaxChunk && k <= kmax, GCGE_ERR_ARG, "residual_norms: too many columns");
-    const int blocks = spmm_blocks(pat);
+    GCGE_REQUIRE(!pb || (pb->n == pa.n && pb->nslices == pa.nslices), GCGE_ERR_ARG,
+                 "residual_norms: patterns differ in size");
+    const int blocks = spmm_blocks(pa);
     if (k <= 0) return 0;
     GCGE_K_DISPATCH(k, (k_residual<KT><<<blocks, kSpmmThreads, 0, st>>>(
-                           pat.slice_ptr.p, pat.col.p, a, b, pat.n, pat.nslices, X, ldx, lam, k,
+                           pa.slice_ptr.p, pa.col.p, va, pb ? pb->slice_ptr.p : nullptr,
+                           pb ? pb->col.p : nullptr, vb, pa.n, pa.nslices, X, ldx, lam, k,
                            partial, kmax, ax, bx, ldo)));
     GCGE_CHECK_LAUNCH();
     count_launch();
