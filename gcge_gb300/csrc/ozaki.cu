@@ -132,20 +132,32 @@ __device__ __forceinline__ void mma_bf16(float (&d)[4], const uint32_t (&a)[4],
 }
 
 // Exponent fields (max over [k0, kend), at least 1) of R rows of a
-// k-contiguous operand: one warp per row.
-template <int R>
+// k-contiguous operand: warp w takes rows w, w + NW, ...; the loads of all of
+// a warp's rows for one k are issued together, so their latencies overlap.
+template <int R, int NW>
 __device__ __forceinline__ void exps_kcontig(const double *__restrict__ p, size_t ld, int r0,
                                              int nrows, int k0, int kend, int *e, int warp,
-                                             int nwarps, int lane) {
-    for (int r = warp; r < R; r += nwarps) {
-        const int gr = r0 + r;
-        int em = 1;
-        if (gr < nrows) {
-            const double *q = p + (size_t)gr * ld;
-            for (int k = k0 + lane; k < kend; k += 32) em = max(em, exp_field(q[k]));
-        }
-        em = (int)__reduce_max_sync(0xffffffffu, (unsigned)em);
-        if (lane == 0) e[r] = em;
+                                             int lane) {
+    constexpr int RPW = (R + NW - 1) / NW;
+    int em[RPW];
+    const double *q[RPW];
+#pragma unroll
+    for (int t = 0; t < RPW; ++t) {
+        const int r = warp + t * NW;
+        em[t] = 1;
+        q[t] = (r < R && r0 + r < nrows) ? p + (size_t)(r0 + r) * ld : nullptr;
+    }
+#pragma unroll 2
+    for (int k = k0 + lane; k < kend; k += 32) {
+#pragma unroll
+        for (int t = 0; t < RPW; ++t)
+            if (q[t]) em[t] = max(em[t], exp_field(q[t][k]));
+    }
+#pragma unroll
+    for (int t = 0; t < RPW; ++t) {
+        const int r = warp + t * NW;
+        const int m = (int)__reduce_max_sync(0xffffffffu, (unsigned)em[t]);
+        if (lane == 0 && r < R) e[r] = m;
     }
 }
 
@@ -168,23 +180,33 @@ __device__ __forceinline__ void exps_mcontig(const double *__restrict__ p, size_
 // p[k + r * ld]) for the chunk [k0, k0 + kBK) clipped to kend, relative to the
 // exponent fields e[r]; rows at or past nrows are zero.  One warp per row,
 // lane l takes k = k0 + 2l, k0 + 2l + 1.
-template <int R>
+template <int R, int NW>
 __device__ __forceinline__ void planes_kcontig(const double *__restrict__ p, size_t ld, int r0,
                                                int nrows, int k0, int kend,
                                                uint16_t (*planes)[R][kBKP], int *e, int warp,
-                                               int nwarps, int lane) {
-    for (int r = warp; r < R; r += nwarps) {
-        const int gr = r0 + r;
-        const int k = k0 + 2 * lane;
-        double v0 = 0.0, v1 = 0.0;
-        if (gr < nrows) {
+                                               int lane) {
+    // all of the warp's rows are loaded before any is split, so the loads'
+    // latencies overlap
+    constexpr int RPW = (R + NW - 1) / NW;
+    const int k = k0 + 2 * lane;
+    double v0[RPW], v1[RPW];
+#pragma unroll
+    for (int t = 0; t < RPW; ++t) {
+        const int r = warp + t * NW, gr = r0 + r;
+        v0[t] = v1[t] = 0.0;
+        if (r < R && gr < nrows) {
             const double *q = p + (size_t)gr * ld;
-            if (k < kend) v0 = q[k];
-            if (k + 1 < kend) v1 = q[k + 1];
+            if (k < kend) v0[t] = q[k];
+            if (k + 1 < kend) v1[t] = q[k + 1];
         }
+    }
+#pragma unroll
+    for (int t = 0; t < RPW; ++t) {
+        const int r = warp + t * NW;
+        if (r >= R) break;
         const int em = e[r];
         uint32_t w[kDigits];
-        digit_pairs(fixed56(v0, em), fixed56(v1, em), w);
+        digit_pairs(fixed56(v0[t], em), fixed56(v1[t], em), w);
 #pragma unroll
         for (int i = 0; i < kDigits; ++i)
             *reinterpret_cast<uint32_t *>(&planes[i][r][2 * lane]) = w[i];
@@ -265,11 +287,11 @@ __global__ void __launch_bounds__(oz_threads<BN>()) k_oz_bprep(const double *__r
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int s = blockIdx.x, nt = blockIdx.y, nt0 = nt * BN;
     const int sk = s * kSuper * kBK, ske = min(K, sk + kSuper * kBK);
-    exps_kcontig<BN>(C, ldc, nt0, N, sk, ske, eb, warp, nwarps, lane);
+    exps_kcontig<BN, nwarps>(C, ldc, nt0, N, sk, ske, eb, warp, lane);
     __syncthreads();
     for (int i = tid; i < BN; i += NT) exps[((size_t)nt * nsup + s) * BN + i] = eb[i];
     for (int k0 = sk; k0 < ske; k0 += kBK) {
-        planes_kcontig<BN>(C, ldc, nt0, N, k0, ske, b, eb, warp, nwarps, lane);
+        planes_kcontig<BN, nwarps>(C, ldc, nt0, N, k0, ske, b, eb, warp, lane);
         __syncthreads();
         const uint4 *src = reinterpret_cast<const uint4 *>(&b[0][0][0]);
         uint4 *dst = reinterpret_cast<uint4 *>(planes + ((size_t)nt * nchunks + k0 / kBK) * PL);
@@ -300,14 +322,14 @@ __global__ void __launch_bounds__(oz_threads<BN>(), 2) k_oz_gemm(OzArgs a) {
     for (int sk = kb; sk < ke; sk += kSuper * kBK) {
         const int ske = min(ke, sk + kSuper * kBK);
         if constexpr (GRAM) {
-            exps_kcontig<kBM>(a.A, a.lda, mt0, a.M, sk, ske, sm.ea, warp, nwarps, lane);
+            exps_kcontig<kBM, nwarps>(a.A, a.lda, mt0, a.M, sk, ske, sm.ea, warp, lane);
         } else {
             for (int r = tid; r < kBM; r += NT) sm.ea[r] = 1;
             __syncthreads();
             exps_mcontig<NT>(a.A, a.lda, mt0, a.M, sk, ske, sm.ea, tid);
         }
         if constexpr (GRAM) {
-            exps_kcontig<BN>(a.B, a.ldb, nt0, a.N, sk, ske, sm.eb, warp, nwarps, lane);
+            exps_kcontig<BN, nwarps>(a.B, a.ldb, nt0, a.N, sk, ske, sm.eb, warp, lane);
         } else {
             const int *e = a.bexps + ((size_t)blockIdx.y * a.nsup + sk / (kSuper * kBK)) * BN;
             for (int i = tid; i < BN; i += NT) sm.eb[i] = e[i];
@@ -316,11 +338,11 @@ __global__ void __launch_bounds__(oz_threads<BN>(), 2) k_oz_gemm(OzArgs a) {
         long long thi[4] = {0, 0, 0, 0}, tlo[4] = {0, 0, 0, 0};
         for (int k0 = sk; k0 < ske; k0 += kBK) {
             if constexpr (GRAM)
-                planes_kcontig<kBM>(a.A, a.lda, mt0, a.M, k0, ske, sm.a, sm.ea, warp, nwarps, lane);
+                planes_kcontig<kBM, nwarps>(a.A, a.lda, mt0, a.M, k0, ske, sm.a, sm.ea, warp, lane);
             else
                 planes_mcontig<NT>(a.A, a.lda, mt0, a.M, k0, ske, sm.a, sm.ea, tid);
             if constexpr (GRAM) {
-                planes_kcontig<BN>(a.B, a.ldb, nt0, a.N, k0, ske, sm.b, sm.eb, warp, nwarps, lane);
+                planes_kcontig<BN, nwarps>(a.B, a.ldb, nt0, a.N, k0, ske, sm.b, sm.eb, warp, lane);
             } else {
                 constexpr int PL = kDigits * BN * kBKP;
                 const uint4 *src = reinterpret_cast<const uint4 *>(
