@@ -82,6 +82,7 @@ k_jacobi32(int s, const double *__restrict__ M, int ldm, float2 *__restrict__ lo
     __shared__ float red_off[32], red_tot[32];
     __shared__ int stop;
     const int t = threadIdx.x, lane = t & 31, warp = t >> 5, nwarps = blockDim.x >> 5;
+    const int nq = np + (np & 1), width = nq + 1, nblk = (nq / 2) * width;
     for (int idx = t; idx < s * (s + 1) / 2; idx += blockDim.x) {
         // decode packed index -> (x, y), x <= y
         int y = (int)((sqrtf(8.0f * idx + 1.0f) - 1.0f) * 0.5f);
@@ -148,14 +149,26 @@ k_jacobi32(int s, const double *__restrict__ M, int ldm, float2 *__restrict__ lo
                 sn[i] = sv;
             }
             __syncthreads();
-            // (b) A <- J^T A J on every 2x2 block (i <= j) of the pair grid
-            for (int i = warp; i < np; i += nwarps) {
-                const int pi = pp[2 * i], qi = pp[2 * i + 1];
-                const float ci = cs[i], si = sn[i];
-                const bool qiv = qi < s;
-                for (int j = i + lane; j < np; j += 32) {
+            // (b) A <- J^T A J on every 2x2 block (i <= j) of the pair grid.  The
+            // triangle of blocks is folded into nq / 2 rows of nq + 1 blocks (row r
+            // holds pair rows r and nq - 1 - r), which the threads share evenly.
+            for (int b = t; b < nblk; b += blockDim.x) {
+                const int fr = b / width, fc = b - fr * width;
+                int i, j;
+                if (fc < nq - fr) {
+                    i = fr;
+                    j = fr + fc;
+                } else {
+                    i = nq - 1 - fr;
+                    j = i + (fc - (nq - fr));
+                }
+                if (j >= np) continue;
+                {
+                    const float ci = cs[i], si = sn[i];
                     const float cj = cs[j], sj = sn[j];
                     if (si == 0.0f && sj == 0.0f) continue;
+                    const int pi = pp[2 * i], qi = pp[2 * i + 1];
+                    const bool qiv = qi < s;
                     const int pj = pp[2 * j], qj = pp[2 * j + 1];
                     const bool qjv = qj < s;
                     if (i == j) {
@@ -212,36 +225,77 @@ static size_t jacobi_dyn_limit() {
 
 // V = J_1 J_2 ... J_T, one warp per row of V: row r starts as e_r and every
 // logged rotation (p, q, c, s) maps (v_p, v_q) -> (c v_p - s v_q, s v_p + c v_q).
+// Lane l applies the rotations of pairs l, l + 32, ... (NS slots); the log of
+// the next kRotGroup rounds is loaded while the current ones are applied, so
+// the row's updates do not wait on the log's L2 latency.
+constexpr int kRotGroup = 4;
+template <int NS>
 __global__ void __launch_bounds__(256)
 k_apply_rotations(int s, const float2 *__restrict__ log, const int *__restrict__ info,
                   double *__restrict__ V, int ldv) {
     extern __shared__ float rows[];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int r = blockIdx.x * 8 + warp;
+    if (r >= s) return;  // warp-uniform; the kernel has no block-wide barrier
     float *v = rows + (size_t)warp * s;
-    const int m = jac_m(s), np = m / 2;
+    const int m = jac_m(s), np = m / 2, m1 = m - 1;
     const int rounds = info[0];
-    if (r < s) {
-        for (int j = lane; j < s; j += 32) v[j] = (j == r) ? 1.0f : 0.0f;
-    }
+    for (int j = lane; j < s; j += 32) v[j] = (j == r) ? 1.0f : 0.0f;
     __syncwarp();
-    if (r < s) {
-        for (int t = 0; t < rounds; ++t) {
-            const int rr = t % (m - 1);
-            for (int i = lane; i < np; i += 32) {
-                const float2 cs = log[(size_t)t * np + i];
-                if (cs.y == 0.0f) continue;
-                int p, q;
-                jac_pair(m, rr, i, p, q);
+    auto load = [&](float2 (&dst)[kRotGroup][NS], int t0) {
+#pragma unroll
+        for (int g = 0; g < kRotGroup; ++g)
+#pragma unroll
+            for (int k = 0; k < NS; ++k) {
+                const int i = lane + 32 * k;
+                dst[g][k] = (t0 + g < rounds && i < np) ? log[(size_t)(t0 + g) * np + i]
+                                                        : make_float2(1.0f, 0.0f);
+            }
+    };
+    float2 cur[kRotGroup][NS], nxt[kRotGroup][NS];
+    load(cur, 0);
+    int rr = 0;  // round within the sweep
+    for (int t0 = 0; t0 < rounds; t0 += kRotGroup) {
+        load(nxt, t0 + kRotGroup);
+#pragma unroll
+        for (int g = 0; g < kRotGroup; ++g) {
+#pragma unroll
+            for (int k = 0; k < NS; ++k) {
+                const int i = lane + 32 * k;
+                const float2 cs = cur[g][k];
+                if (cs.y == 0.0f) continue;  // also every slot past np or past the last round
+                int a, b;
+                if (i == 0) {
+                    a = m1;
+                    b = rr;
+                } else {
+                    a = rr + i;
+                    if (a >= m1) a -= m1;
+                    b = rr - i;
+                    if (b < 0) b += m1;
+                }
+                const int p = min(a, b), q = max(a, b);
                 if (q >= s) continue;
                 const float vp = v[p], vq = v[q];
                 v[p] = cs.x * vp - cs.y * vq;
                 v[q] = cs.y * vp + cs.x * vq;
             }
             __syncwarp();
+            if (++rr == m1) rr = 0;
         }
-        for (int j = lane; j < s; j += 32) V[r + (size_t)j * ldv] = (double)v[j];
+#pragma unroll
+        for (int g = 0; g < kRotGroup; ++g)
+#pragma unroll
+            for (int k = 0; k < NS; ++k) cur[g][k] = nxt[g][k];
     }
+    for (int j = lane; j < s; j += 32) V[r + (size_t)j * ldv] = (double)v[j];
+}
+
+template <int NS>
+static void launch_rotations(int s, const float2 *log, const int *info, double *V, int ldv,
+                             cudaStream_t st) {
+    k_apply_rotations<NS><<<(s + 7) / 8, 256, (size_t)8 * s * sizeof(float), st>>>(s, log, info,
+                                                                                  V, ldv);
 }
 
 void EigWork::reserve(int smax) {
@@ -351,9 +405,14 @@ int sym_eig(EigWork &wk, int s, const double *M, int ld, double *eval_host, doub
     });
     k_jacobi32<<<1, kJacobiThreads, smem, st>>>(s, M, ld, wk.log.p, wk.max_rounds, wk.info.p);
     GCGE_CHECK_LAUNCH();
-    const int rows_blocks = (s + 7) / 8;
-    k_apply_rotations<<<rows_blocks, 256, (size_t)8 * s * sizeof(float), st>>>(s, wk.log.p,
-                                                                              wk.info.p, wk.X.p, s);
+    switch ((jac_m(s) / 2 + 31) / 32) {
+        case 1: launch_rotations<1>(s, wk.log.p, wk.info.p, wk.X.p, s, st); break;
+        case 2: launch_rotations<2>(s, wk.log.p, wk.info.p, wk.X.p, s, st); break;
+        case 3: launch_rotations<3>(s, wk.log.p, wk.info.p, wk.X.p, s, st); break;
+        case 4: launch_rotations<4>(s, wk.log.p, wk.info.p, wk.X.p, s, st); break;
+        case 5: launch_rotations<5>(s, wk.log.p, wk.info.p, wk.X.p, s, st); break;
+        default: launch_rotations<6>(s, wk.log.p, wk.info.p, wk.X.p, s, st); break;
+    }
     GCGE_CHECK_LAUNCH();
     count_launch(2);
     const int lds = s;
