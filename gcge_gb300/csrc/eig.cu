@@ -390,8 +390,9 @@ void host_eigh(int n, const double *G, double *w, double *V) {
 // gap is below 1e-5 max|lambda| (there E_ij would mostly amplify rounding);
 // each cluster block of S is diagonalised exactly in FP64 in the same step,
 // so near-degenerate pairs come out orthonormal and resolved to FP64
-// accuracy.  Steps repeat until max|E| < 1e-13 or stagnates at the rounding
-// level; the last step folds the ascending sort into the update and writes Z.
+// accuracy.  The update of a step with max|E| < 1e-9 is the last (its error
+// is of the order max|E|^2 / gap); that step folds the ascending sort into the
+// update and writes Z.
 int sym_eig(EigWork &wk, int s, const double *M, int ld, double *eval_host, double *Z, int ldz,
             int refine_steps, cudaStream_t st) {
     GCGE_REQUIRE(s >= 1 && s <= wk.cap, GCGE_ERR_ARG, "sym_eig: size");
@@ -430,7 +431,6 @@ int sym_eig(EigWork &wk, int s, const double *M, int ld, double *eval_host, doub
         return x;
     };
     const int steps = std::max(2, refine_steps);
-    double prev = 1e300;
     for (int step = 0; step < steps; ++step) {
         gram(s, s, s, X, lds, X, lds, wk.G.p, lds, wk.gscr.p, gs, st);
         lincomb(s, s, s, M, ld, X, lds, wk.W.p, lds, nullptr, 0, st);
@@ -506,14 +506,17 @@ int sym_eig(EigWork &wk, int s, const double *M, int ld, double *eval_host, doub
             }
             k = e;
         }
-        const bool last = (step == steps - 1) || emax < 1e-13 || (emax < 1e-9 && emax > 0.25 * prev);
-        prev = emax;
+        // the step's error is second order in emax (first order inside clusters,
+        // which are diagonalised exactly), so once emax < 1e-9 this update is
+        // the last one needed
+        const bool last = (step == steps - 1) || emax < 1e-9;
         wk.last_steps = step + 1;
         if (!last) {
             GCGE_CUDA(cudaMemcpyAsync(wk.C.p, hC, sizeof(double) * s2, cudaMemcpyHostToDevice, st));
             lincomb(s, s, s, X, lds, wk.C.p, lds, Xn, lds, nullptr, 0, st);
             std::swap(X, Xn);
-            GCGE_CUDA(cudaStreamSynchronize(st));  // hC is rewritten next step
+            // hC is rewritten only after the next step's synchronisation, which
+            // follows this copy on the stream
             continue;
         }
         // final: ascending order folded into the update
