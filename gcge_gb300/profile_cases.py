@@ -5,11 +5,17 @@ columns, blocks of bs = 20).
     python -m gcge_gb300.profile_cases gram      # Q^T P, Q n x 180, P n x 20
     python -m gcge_gb300.profile_cases lincomb   # X C, X n x 180, C 180 x 20
     python -m gcge_gb300.profile_cases both
+    python -m gcge_gb300.profile_cases pcg       # FP32 block PCG, 20 columns, 30 steps
 
 Each case runs the FP64-accurate digit-plane product once after one warm-up
 call, through the same C-ABI entry points the parity tests use
 (GCGE_DenseGram / GCGE_DenseLinComb), and checks the result against the FP64
 kernel's.  Under ncu, select the product kernel with -k regex:k_oz_gemm.
+
+The pcg case runs the persistent FP32 block PCG of the W step (30 CG steps,
+no early stop) on the shifted generalized 64^3 operator A + sigma B through
+GCGE_BlockPCG, once after one warm-up call, and checks that the residual
+dropped; select it with -k regex:k_block_pcg.
 """
 from __future__ import annotations
 
@@ -49,6 +55,20 @@ def lincomb():
     return err < 1e-14
 
 
+def pcg():
+    from gcge_gb300 import problems as Pr
+    A, B = Pr.laplace3d(64), Pr.mass3d(64)
+    b = np.random.default_rng(4).standard_normal((A.n, W))
+    x0 = np.zeros_like(b)
+    sigma = 10.0
+    G.block_pcg(A, B, sigma, b, x0, max_iter=30, rate=1e-30, tol=1e-30, fp32=True)
+    x, it = G.block_pcg(A, B, sigma, b, x0, max_iter=30, rate=1e-30, tol=1e-30, fp32=True)
+    S = A.to_scipy() + sigma * B.to_scipy()
+    red = float(np.max(np.linalg.norm(b - S @ x, axis=0) / np.linalg.norm(b, axis=0)))
+    print(f"pcg n={A.n} k={W} steps={it}: max relative residual {red:.2e}")
+    return it == 30 and red < 0.5
+
+
 def main(argv):
     what = argv[1] if len(argv) > 1 else "both"
     ok = True
@@ -56,6 +76,8 @@ def main(argv):
         ok &= gram()
     if what in ("lincomb", "both"):
         ok &= lincomb()
+    if what == "pcg":
+        ok &= pcg()
     return 0 if ok else 1
 
 
