@@ -187,6 +187,12 @@ int borth(SolverCtx &c, SparseMat *B, double *x, int ldx, int nrows, int start, 
     // W column of a nearly converged pair) the prefix projection and the
     // factorisation run once more on the now well-conditioned block.
     for (int round = 0; round < 2 && k > 0; ++round) {
+        // c.T2 holds B x1 of the block before the last projection, which
+        // changed it by a coefficient block C below reorth_tol: the Gram
+        // matrix of the first Cholesky-QR pass taken with it differs from
+        // x1^T B x1 by (X^T B x1)^T C, of order eps * reorth_tol, so that pass
+        // needs no product of its own
+        bool bx1_kept = false;
         if (start > 0) {
             for (int pass = 0; pass < 1 + max_reorth; ++pass) {
                 const double *BX1 = X1;
@@ -198,7 +204,10 @@ int borth(SolverCtx &c, SparseMat *B, double *x, int ldx, int nrows, int start, 
                       c.gscr.n, st);
                 dlincomb(c, nrows, start, k, x, ldx, c.dC.p, start, X1, ldx, c.one.p, 0, st, -1.0);
                 if (pass >= 1 || max_reorth == 0) {
-                    if (device_absmax(start, k, c.dC.p, start) < reorth_tol) break;
+                    if (device_absmax(start, k, c.dC.p, start) < reorth_tol) {
+                        bx1_kept = useB;
+                        break;
+                    }
                 }
             }
         }
@@ -208,7 +217,7 @@ int borth(SolverCtx &c, SparseMat *B, double *x, int ldx, int nrows, int start, 
         for (int pass = 0; pass < 4 && k > 0; ++pass) {
             const double *BX1 = X1;
             if (useB) {
-                applyB(X1, ldx, c.T2.p, ld, k);
+                if (!(pass == 0 && bx1_kept)) applyB(X1, ldx, c.T2.p, ld, k);
                 BX1 = c.T2.p;
             }
             dgram(c, nrows, k, k, X1, ldx, BX1, useB ? ld : ldx, c.dC.p, k, c.gscr.p, c.gscr.n, st);
