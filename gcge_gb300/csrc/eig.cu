@@ -4,9 +4,12 @@
 //
 // GB300 issues FP64 at ~1/58 of its FP32 rate, so an FP64 Jacobi on one SM
 // would take tens of milliseconds for s = 200.  The solver therefore
-//   1. runs a parallel-order (round-robin) two-sided cyclic Jacobi in FP32 in
-//      one 1024-thread CTA, with the packed upper triangle of the matrix in
-//      shared memory (s <= 336), logging each round's rotations;
+//   1. runs a parallel-order (round-robin) two-sided cyclic Jacobi in FP32,
+//      logging each round's rotations: for s >= 64 in a cluster of 8 CTAs
+//      whose shared memories hold the matrix rows of the pairs each CTA owns
+//      (distributed shared memory; rows move between neighbouring CTAs as the
+//      round-robin order advances), else in one 1024-thread CTA with the
+//      packed upper triangle in shared memory;
 //   2. rebuilds the eigenvector matrix from the rotation log with one warp
 //      per row (rows of V = J_1 J_2 ... J_T are independent);
 //   3. refines eigenvectors and eigenvalues to FP64 accuracy with the
@@ -18,6 +21,7 @@
 //      exactly on the host (tiny FP64 Jacobi) and sorts ascending.
 // The 2x2 rotation is the symmetric Schur decomposition of Golub & Van Loan
 // (Matrix Computations, Alg. 8.4.1).
+#include <cooperative_groups.h>
 #include <mutex>
 #include <algorithm>
 #include <cmath>
@@ -27,6 +31,8 @@
 #include "eig.cuh"
 
 namespace gcge {
+
+namespace cg = cooperative_groups;
 
 constexpr int kJacobiThreads = 1024;
 constexpr int kMaxSweeps = 12;
@@ -62,15 +68,19 @@ size_t jacobi_smem_bytes(int s) {
            (size_t)(m / 2) * 2 * sizeof(short) + 64;
 }
 static size_t jacobi_dyn_limit();
+static bool jacobi_cluster_usable();
+static int jacobi_cluster_max_dim();
+// one-CTA kernel capacity, and the cluster kernel's where it can run
 int jacobi_max_dim() {
     const size_t lim = jacobi_dyn_limit();
     int s = 8;
     while (jacobi_smem_bytes(s + 1) <= lim) ++s;
+    if (jacobi_cluster_usable()) s = std::max(s, jacobi_cluster_max_dim());
     return s;
 }
 
 __global__ void __launch_bounds__(kJacobiThreads)
-k_jacobi32(int s, const double *__restrict__ M, int ldm, float2 *__restrict__ log, int max_rounds,
+k_jacobi32(int s, const double *__restrict__ M, int ldm, float4 *__restrict__ log, int max_rounds,
            int *__restrict__ info /* [0]=rounds, [1]=sweeps, [2]=converged */) {
     extern __shared__ float sm[];
     const int m = jac_m(s);
@@ -195,7 +205,8 @@ k_jacobi32(int s, const double *__restrict__ M, int ldm, float2 *__restrict__ lo
             }
             // (c) log the round
             for (int i = t; i < np; i += blockDim.x)
-                log[(size_t)round * np + i] = make_float2(cs[i], sn[i]);
+                log[(size_t)round * np + i] = make_float4(cs[i], sn[i], __int_as_float(pp[2 * i]),
+                                                          __int_as_float(pp[2 * i + 1]));
             ++round;
             __syncthreads();
         }
@@ -205,6 +216,214 @@ k_jacobi32(int s, const double *__restrict__ M, int ldm, float2 *__restrict__ lo
         info[1] = sweep;
         info[2] = converged;
     }
+}
+
+// ---------------------------------------------------------------- cluster Jacobi
+// The same rotations in a cluster of kJC CTAs.  Indices are arranged by the
+// circle method: with P_r[0] = 0 and P_r[i] = 1 + ((i - 1 - r) mod (m - 1)),
+// pair slot k of round r is (P_r[k], P_r[m - 1 - k]); after m - 1 rounds P is
+// the identity again.  CTA c owns the slots [c np / kJC, (c + 1) np / kJC) and
+// holds the two full rows (m floats each) of each of its slots.  A round:
+//   (a) every CTA computes the rotations of its slots and writes them into the
+//       round table of every CTA of the cluster;
+//   (b) after a cluster barrier, each CTA updates every 2x2 block (own slot i,
+//       any slot j) of its rows, A <- J^T A J, and writes the new rows into
+//       the other row buffer at the slots they hold in the next round, which
+//       for at most two rows per CTA is in the neighbouring CTA's shared
+//       memory;
+//   (c) a second cluster barrier makes the next buffers complete.
+// Rotations and the stopping test are those of k_jacobi32; every CTA sums the
+// per-CTA off-diagonal masses in the same order, so all take the same decision.
+constexpr int kJC = 8;
+constexpr int kJacClusterMin = 64;  // smaller matrices use the one-CTA kernel
+
+__host__ __device__ inline int jc_slots(int np) { return (np + kJC - 1) / kJC; }
+
+size_t jacobi_cluster_smem_bytes(int s) {
+    const int m = jac_m(s), np = m / 2, ks = jc_slots(np);
+    return (size_t)2 * np * sizeof(float4) + (size_t)2 * 2 * ks * m * sizeof(float) +
+           (size_t)2 * kJC * 2 * sizeof(float) + 64;
+}
+
+// index at position i of the circle arrangement after r rounds
+__device__ __forceinline__ int circle_index(int i, int r, int m1) {
+    if (i == 0) return 0;
+    int v = i - 1 - r;
+    v %= m1;
+    if (v < 0) v += m1;
+    return 1 + v;
+}
+
+// CTA owning slot k (slots [c np / kJC, (c + 1) np / kJC) belong to CTA c)
+__device__ __forceinline__ int slot_owner(int k, int np) { return ((k + 1) * kJC - 1) / np; }
+
+__global__ void __launch_bounds__(kJacobiThreads, 1)
+k_jacobi32_cluster(int s, const double *__restrict__ M, int ldm, float4 *__restrict__ log,
+                   int max_rounds, int *__restrict__ info) {
+    cg::cluster_group cl = cg::this_cluster();
+    const int rank = (int)cl.block_rank();
+    extern __shared__ __align__(16) unsigned char jsm[];
+    const int m = jac_m(s), np = m / 2, ks = jc_slots(np), m1 = m - 1;
+    float4 *table = reinterpret_cast<float4 *>(jsm);  // [2][np]
+    float *rows = reinterpret_cast<float *>(table + 2 * np);  // [2][2 ks][m]
+    float *red = rows + (size_t)2 * 2 * ks * m;                 // [2][kJC][2]
+    __shared__ float wsum[kJacobiThreads / 32][2];
+    __shared__ int stop;
+    const size_t bufsz = (size_t)2 * ks * m;
+    const int k0 = (rank * np) / kJC, k1 = ((rank + 1) * np) / kJC, nloc = k1 - k0;
+    const int t = threadIdx.x, lane = t & 31, warp = t >> 5, nwarps = blockDim.x >> 5;
+    // rows of round 0 (P = identity): slot k holds rows k and m - 1 - k
+    for (int idx = t; idx < 2 * nloc * m; idx += blockDim.x) {
+        const int lr = idx / m, y = idx - lr * m;
+        const int k = k0 + (lr >> 1);
+        const int x = (lr & 1) ? m - 1 - k : k;
+        float v = 0.0f;
+        if (x < s && y < s) v = (float)(0.5 * (M[x + (size_t)y * ldm] + M[y + (size_t)x * ldm]));
+        rows[(size_t)lr * m + y] = v;
+    }
+    cl.sync();  // every CTA of the cluster runs before any remote access
+    int cur = 0, round = 0, sweep = 0, converged = 0;
+    for (sweep = 0; sweep < kMaxSweeps && round + m1 <= max_rounds; ++sweep) {
+        // off-diagonal mass at the start of the sweep (P = identity again)
+        {
+            const float *R = rows + cur * bufsz;
+            float off = 0.0f, tot = 0.0f;
+            for (int idx = t; idx < 2 * nloc * m; idx += blockDim.x) {
+                const int lr = idx / m, y = idx - lr * m;
+                const int k = k0 + (lr >> 1);
+                const int x = (lr & 1) ? m - 1 - k : k;
+                const float v = R[(size_t)lr * m + y];
+                tot += v * v;
+                if (x != y) off += v * v;
+            }
+            for (int o = 16; o > 0; o >>= 1) {
+                off += __shfl_xor_sync(0xffffffffu, off, o);
+                tot += __shfl_xor_sync(0xffffffffu, tot, o);
+            }
+            if (lane == 0) {
+                wsum[warp][0] = off;
+                wsum[warp][1] = tot;
+            }
+            __syncthreads();
+            if (t == 0) {
+                float a = 0.0f, b = 0.0f;
+                for (int w = 0; w < nwarps; ++w) {
+                    a += wsum[w][0];
+                    b += wsum[w][1];
+                }
+                float *slot = red + ((sweep & 1) * kJC + rank) * 2;
+                for (int c = 0; c < kJC; ++c) {
+                    float *dst = cl.map_shared_rank(slot, c);
+                    dst[0] = a;
+                    dst[1] = b;
+                }
+            }
+            cl.sync();
+            if (t == 0) {
+                float a = 0.0f, b = 0.0f;
+                for (int c = 0; c < kJC; ++c) {
+                    a += red[((sweep & 1) * kJC + c) * 2];
+                    b += red[((sweep & 1) * kJC + c) * 2 + 1];
+                }
+                stop = (a <= kOffTol * kOffTol * b) ? 1 : 0;
+            }
+            __syncthreads();
+            if (stop) {
+                converged = 1;
+                break;
+            }
+        }
+        for (int r = 0; r < m1; ++r) {
+            const float *R = rows + cur * bufsz;
+            float4 *tab = table + (round & 1) * np;
+            // (a) rotations of the local slots, into every CTA's round table
+            for (int ls = t; ls < nloc; ls += blockDim.x) {
+                const int k = k0 + ls;
+                const int p = circle_index(k, r, m1), q = circle_index(m - 1 - k, r, m1);
+                float c = 1.0f, sv = 0.0f;
+                if (p < s && q < s) {
+                    const float app = R[(size_t)(2 * ls) * m + p];
+                    const float aqq = R[(size_t)(2 * ls + 1) * m + q];
+                    const float apq = R[(size_t)(2 * ls) * m + q];
+                    const float thr = kRotTol * sqrtf(fabsf(app) * fabsf(aqq));
+                    if (fabsf(apq) > thr && fabsf(apq) > 1e-30f) {
+                        const float tau = (aqq - app) / (2.0f * apq);
+                        const float tt =
+                            (tau >= 0.0f ? 1.0f : -1.0f) / (fabsf(tau) + hypotf(1.0f, tau));
+                        c = rsqrtf(1.0f + tt * tt);
+                        sv = tt * c;
+                    }
+                }
+                const float4 e = make_float4(c, sv, __int_as_float(p), __int_as_float(q));
+                for (int cc = 0; cc < kJC; ++cc) *cl.map_shared_rank(tab + k, cc) = e;
+                log[(size_t)round * np + k] = e;
+            }
+            cl.sync();
+            // (b) the 2x2 blocks of the local rows, written to the next buffers
+            const size_t nxt = (size_t)(cur ^ 1) * bufsz;
+            for (int b = t; b < nloc * np; b += blockDim.x) {
+                const int li = b / np, j = b - li * np;
+                const int ki = k0 + li;
+                const float4 ei = tab[ki], ej = tab[j];
+                const float ci = ei.x, si = ei.y, cj = ej.x, sj = ej.y;
+                const int pj = __float_as_int(ej.z), qj = __float_as_int(ej.w);
+                const float *Tp = R + (size_t)(2 * li) * m, *Tq = Tp + m;
+                float o11, o12, o21, o22;
+                if (ki == j) {
+                    const float app = Tp[pj], aqq = Tq[qj], apq = Tp[qj], aqp = Tq[pj];
+                    if (si != 0.0f) {
+                        const float t11 = ci * app - si * apq, t12 = ci * apq - si * aqq;
+                        const float t21 = si * app + ci * apq, t22 = si * apq + ci * aqq;
+                        o11 = t11 * ci - t12 * si;
+                        o22 = t21 * si + t22 * ci;
+                        o12 = o21 = 0.0f;
+                    } else {
+                        o11 = app;
+                        o12 = apq;
+                        o21 = aqp;
+                        o22 = aqq;
+                    }
+                } else {
+                    const float a11 = Tp[pj], a12 = Tp[qj], a21 = Tq[pj], a22 = Tq[qj];
+                    const float t11 = ci * a11 - si * a21, t12 = ci * a12 - si * a22;
+                    const float t21 = si * a11 + ci * a21, t22 = si * a12 + ci * a22;
+                    o11 = t11 * cj - t12 * sj;
+                    o12 = t11 * sj + t12 * cj;
+                    o21 = t21 * cj - t22 * sj;
+                    o22 = t21 * sj + t22 * cj;
+                }
+                // next-round positions of the two rows (circle method)
+                int kt, st_, kb, sb;
+                if (np == 1) {
+                    kt = 0, st_ = 0, kb = 0, sb = 1;
+                } else {
+                    if (ki == 0) kt = 0, st_ = 0;
+                    else if (ki <= np - 2) kt = ki + 1, st_ = 0;
+                    else kt = np - 1, st_ = 1;
+                    if (ki == 0) kb = 1, sb = 0;
+                    else kb = ki - 1, sb = 1;
+                }
+                const int ot = slot_owner(kt, np), ob = slot_owner(kb, np);
+                float *dt = rows + nxt + (size_t)(2 * (kt - (ot * np) / kJC) + st_) * m;
+                float *db = rows + nxt + (size_t)(2 * (kb - (ob * np) / kJC) + sb) * m;
+                if (ot != rank) dt = cl.map_shared_rank(dt, ot);
+                if (ob != rank) db = cl.map_shared_rank(db, ob);
+                dt[pj] = o11;
+                dt[qj] = o12;
+                db[pj] = o21;
+                db[qj] = o22;
+            }
+            cl.sync();
+            cur ^= 1;
+            ++round;
+        }
+    }
+    if (rank == 0 && t == 0) {
+        info[0] = round;
+        info[1] = sweep;
+        info[2] = converged;
+    }
+    cl.sync();  // no CTA leaves while another may still address its memory
 }
 
 // Largest dynamic shared memory the Jacobi kernel may request: the device's
@@ -224,64 +443,51 @@ static size_t jacobi_dyn_limit() {
 }
 
 // V = J_1 J_2 ... J_T, one warp per row of V: row r starts as e_r and every
-// logged rotation (p, q, c, s) maps (v_p, v_q) -> (c v_p - s v_q, s v_p + c v_q).
+// logged rotation (c, s, p, q) maps (v_p, v_q) -> (c v_p - s v_q, s v_p + c v_q).
 // Lane l applies the rotations of pairs l, l + 32, ... (NS slots); the log of
 // the next kRotGroup rounds is loaded while the current ones are applied, so
 // the row's updates do not wait on the log's L2 latency.
-constexpr int kRotGroup = 4;
+constexpr int kRotGroup = 2;
 template <int NS>
 __global__ void __launch_bounds__(256)
-k_apply_rotations(int s, const float2 *__restrict__ log, const int *__restrict__ info,
+k_apply_rotations(int s, const float4 *__restrict__ log, const int *__restrict__ info,
                   double *__restrict__ V, int ldv) {
     extern __shared__ float rows[];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int r = blockIdx.x * 8 + warp;
     if (r >= s) return;  // warp-uniform; the kernel has no block-wide barrier
     float *v = rows + (size_t)warp * s;
-    const int m = jac_m(s), np = m / 2, m1 = m - 1;
+    const int np = jac_m(s) / 2;
     const int rounds = info[0];
     for (int j = lane; j < s; j += 32) v[j] = (j == r) ? 1.0f : 0.0f;
     __syncwarp();
-    auto load = [&](float2 (&dst)[kRotGroup][NS], int t0) {
+    auto load = [&](float4 (&dst)[kRotGroup][NS], int t0) {
 #pragma unroll
         for (int g = 0; g < kRotGroup; ++g)
 #pragma unroll
             for (int k = 0; k < NS; ++k) {
                 const int i = lane + 32 * k;
                 dst[g][k] = (t0 + g < rounds && i < np) ? log[(size_t)(t0 + g) * np + i]
-                                                        : make_float2(1.0f, 0.0f);
+                                                        : make_float4(1.0f, 0.0f, 0.0f, 0.0f);
             }
     };
-    float2 cur[kRotGroup][NS], nxt[kRotGroup][NS];
+    float4 cur[kRotGroup][NS], nxt[kRotGroup][NS];
     load(cur, 0);
-    int rr = 0;  // round within the sweep
     for (int t0 = 0; t0 < rounds; t0 += kRotGroup) {
         load(nxt, t0 + kRotGroup);
 #pragma unroll
         for (int g = 0; g < kRotGroup; ++g) {
 #pragma unroll
             for (int k = 0; k < NS; ++k) {
-                const int i = lane + 32 * k;
-                const float2 cs = cur[g][k];
-                if (cs.y == 0.0f) continue;  // also every slot past np or past the last round
-                int a, b;
-                if (i == 0) {
-                    a = m1;
-                    b = rr;
-                } else {
-                    a = rr + i;
-                    if (a >= m1) a -= m1;
-                    b = rr - i;
-                    if (b < 0) b += m1;
-                }
-                const int p = min(a, b), q = max(a, b);
-                if (q >= s) continue;
+                const float4 e = cur[g][k];
+                if (e.y == 0.0f) continue;  // also every slot past np or past the last round
+                const int p = __float_as_int(e.z), q = __float_as_int(e.w);
+                if (p >= s || q >= s) continue;
                 const float vp = v[p], vq = v[q];
-                v[p] = cs.x * vp - cs.y * vq;
-                v[q] = cs.y * vp + cs.x * vq;
+                v[p] = e.x * vp - e.y * vq;
+                v[q] = e.y * vp + e.x * vq;
             }
             __syncwarp();
-            if (++rr == m1) rr = 0;
         }
 #pragma unroll
         for (int g = 0; g < kRotGroup; ++g)
@@ -292,10 +498,50 @@ k_apply_rotations(int s, const float2 *__restrict__ log, const int *__restrict__
 }
 
 template <int NS>
-static void launch_rotations(int s, const float2 *log, const int *info, double *V, int ldv,
+static void launch_rotations(int s, const float4 *log, const int *info, double *V, int ldv,
                              cudaStream_t st) {
     k_apply_rotations<NS><<<(s + 7) / 8, 256, (size_t)8 * s * sizeof(float), st>>>(s, log, info,
                                                                                   V, ldv);
+}
+
+// Whether a cluster of kJC CTAs with the largest shared memory the cluster
+// kernel may use can be resident on this device (checked once).
+static bool jacobi_cluster_usable() {
+    static std::once_flag once;
+    static bool ok = false;
+    std::call_once(once, [] {
+        const size_t lim = jacobi_dyn_limit();
+        if (cudaFuncSetAttribute(k_jacobi32_cluster, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)lim) != cudaSuccess) {
+            cudaGetLastError();
+            return;
+        }
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3(kJC);
+        cfg.blockDim = dim3(kJacobiThreads);
+        cfg.dynamicSmemBytes = lim;
+        cudaLaunchAttribute at[1];
+        at[0].id = cudaLaunchAttributeClusterDimension;
+        at[0].val.clusterDim.x = kJC;
+        at[0].val.clusterDim.y = 1;
+        at[0].val.clusterDim.z = 1;
+        cfg.attrs = at;
+        cfg.numAttrs = 1;
+        int n = 0;
+        if (cudaOccupancyMaxActiveClusters(&n, k_jacobi32_cluster, &cfg) != cudaSuccess) {
+            cudaGetLastError();
+            return;
+        }
+        ok = n > 0;
+    });
+    return ok;
+}
+
+static int jacobi_cluster_max_dim() {
+    const size_t lim = jacobi_dyn_limit();
+    int s = kJacClusterMin;
+    while (jacobi_cluster_smem_bytes(s + 1) <= lim) ++s;
+    return s;
 }
 
 void EigWork::reserve(int smax) {
@@ -311,7 +557,7 @@ void EigWork::reserve(int smax) {
     info.alloc(4);
     const int m = jac_m(smax);
     max_rounds = kMaxSweeps * (m - 1);
-    log.alloc((size_t)max_rounds * (m / 2) + 1);
+    log.alloc((size_t)max_rounds * (m / 2) + 1);  // (c, s, p, q) per pair and round
     gscr.alloc(gram_scratch_elems(smax, smax, smax));
     h_S.alloc(s2);
     h_C.alloc(2 * s2);
@@ -398,13 +644,34 @@ int sym_eig(EigWork &wk, int s, const double *M, int ld, double *eval_host, doub
     GCGE_REQUIRE(s >= 1 && s <= wk.cap, GCGE_ERR_ARG, "sym_eig: size");
     GCGE_REQUIRE(s <= jacobi_max_dim(), GCGE_ERR_TOO_LARGE,
                  "sym_eig: projected dimension exceeds the shared-memory Jacobi capacity");
-    const size_t smem = jacobi_smem_bytes(s);
     static std::once_flag once;  // allow the largest size once, for every caller thread
     std::call_once(once, [] {
         GCGE_CUDA(cudaFuncSetAttribute(k_jacobi32, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        (int)jacobi_dyn_limit()));
     });
-    k_jacobi32<<<1, kJacobiThreads, smem, st>>>(s, M, ld, wk.log.p, wk.max_rounds, wk.info.p);
+    const bool cluster = s >= kJacClusterMin && jacobi_cluster_usable() &&
+                         jacobi_cluster_smem_bytes(s) <= jacobi_dyn_limit();
+    if (cluster) {
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3(kJC);
+        cfg.blockDim = dim3(kJacobiThreads);
+        cfg.dynamicSmemBytes = jacobi_cluster_smem_bytes(s);
+        cfg.stream = st;
+        cudaLaunchAttribute at[1];
+        at[0].id = cudaLaunchAttributeClusterDimension;
+        at[0].val.clusterDim.x = kJC;
+        at[0].val.clusterDim.y = 1;
+        at[0].val.clusterDim.z = 1;
+        cfg.attrs = at;
+        cfg.numAttrs = 1;
+        GCGE_CUDA(cudaLaunchKernelEx(&cfg, k_jacobi32_cluster, s, M, ld, wk.log.p, wk.max_rounds,
+                                     wk.info.p));
+    } else {
+        GCGE_REQUIRE(jacobi_smem_bytes(s) <= jacobi_dyn_limit(), GCGE_ERR_TOO_LARGE,
+                     "sym_eig: projected dimension exceeds the one-CTA Jacobi capacity");
+        k_jacobi32<<<1, kJacobiThreads, jacobi_smem_bytes(s), st>>>(s, M, ld, wk.log.p,
+                                                                    wk.max_rounds, wk.info.p);
+    }
     GCGE_CHECK_LAUNCH();
     switch ((jac_m(s) / 2 + 31) / 32) {
         case 1: launch_rotations<1>(s, wk.log.p, wk.info.p, wk.X.p, s, st); break;
@@ -412,7 +679,9 @@ int sym_eig(EigWork &wk, int s, const double *M, int ld, double *eval_host, doub
         case 3: launch_rotations<3>(s, wk.log.p, wk.info.p, wk.X.p, s, st); break;
         case 4: launch_rotations<4>(s, wk.log.p, wk.info.p, wk.X.p, s, st); break;
         case 5: launch_rotations<5>(s, wk.log.p, wk.info.p, wk.X.p, s, st); break;
-        default: launch_rotations<6>(s, wk.log.p, wk.info.p, wk.X.p, s, st); break;
+        case 6: launch_rotations<6>(s, wk.log.p, wk.info.p, wk.X.p, s, st); break;
+        case 7: launch_rotations<7>(s, wk.log.p, wk.info.p, wk.X.p, s, st); break;
+        default: launch_rotations<8>(s, wk.log.p, wk.info.p, wk.X.p, s, st); break;
     }
     GCGE_CHECK_LAUNCH();
     count_launch(2);
@@ -481,12 +750,35 @@ int sym_eig(EigWork &wk, int s, const double *M, int ld, double *eval_host, doub
             while (e < s && comp[ord[e]] == comp[ord[k]]) ++e;
             const int c = e - k;
             if (c > 1) {
+                // the cluster block of (I + E)^T S (I + E): its in-cluster part
+                // T = I + E_c (first-order G_c^{-1/2}) carries the off-diagonal
+                // Gram entries, so the block's eigenvalues are accurate to
+                // second order in them; the cross terms through entries of E
+                // outside the cluster are second order too
+                std::vector<double> Sc((size_t)c * c), Tc((size_t)c * c), ST((size_t)c * c);
                 std::vector<double> blk((size_t)c * c), vec;
                 for (int a = 0; a < c; ++a)
                     for (int b = 0; b < c; ++b) {
                         const int ia = ord[k + a], ib = ord[k + b];
-                        blk[(size_t)a * c + b] = 0.5 * (hS[ia + (size_t)ib * s] + hS[ib + (size_t)ia * s]) /
-                                                 std::sqrt(hG[ia + (size_t)ia * s] * hG[ib + (size_t)ib * s]);
+                        Sc[(size_t)a * c + b] = 0.5 * (hS[ia + (size_t)ib * s] + hS[ib + (size_t)ia * s]);
+                        Tc[(size_t)a * c + b] = hC[ia + (size_t)ib * s];  // row a, column b
+                    }
+                for (int a = 0; a < c; ++a)  // ST = Sc Tc
+                    for (int b = 0; b < c; ++b) {
+                        double v = 0.0;
+                        for (int u = 0; u < c; ++u) v += Sc[(size_t)a * c + u] * Tc[(size_t)u * c + b];
+                        ST[(size_t)a * c + b] = v;
+                    }
+                for (int a = 0; a < c; ++a)  // blk = Tc^T ST
+                    for (int b = 0; b < c; ++b) {
+                        double v = 0.0;
+                        for (int u = 0; u < c; ++u) v += Tc[(size_t)u * c + a] * ST[(size_t)u * c + b];
+                        blk[(size_t)a * c + b] = v;
+                    }
+                for (int a = 0; a < c; ++a)
+                    for (int b = 0; b < a; ++b) {
+                        const double v = 0.5 * (blk[(size_t)a * c + b] + blk[(size_t)b * c + a]);
+                        blk[(size_t)a * c + b] = blk[(size_t)b * c + a] = v;
                     }
                 host_jacobi(c, blk, vec);
                 std::vector<double> tmp((size_t)s * c, 0.0);

@@ -8,7 +8,7 @@ struct EigWork {
     int cap = 0;
     int max_rounds = 0;
     DevBuf<double> G, W, S, C, X, X2, lam, delta, gscr;
-    DevBuf<float2> log;
+    DevBuf<float4> log;  // rotation log: (c, s, p, q as int bits) per pair and round
     DevBuf<int> info;
     PinnedBuf<double> h_S, h_C, h_lam, h_info;
     double last_delta = 0, last_orth = 0;
