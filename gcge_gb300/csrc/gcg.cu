@@ -17,6 +17,7 @@
 //   * the dense eigensolve (dsyevx) is the FP32 Jacobi + FP64 Ogita-Aishima
 //     refinement of eig.cu.
 #include <algorithm>
+#include <array>
 #include <chrono>
 #include <cmath>
 #include <cstring>
@@ -672,6 +673,7 @@ struct GcgRun {
     bool restart_active() {
         const int k = sizeX - sizeC;
         if (k <= 0) return false;
+        chk_n = 0;  // the Ritz vectors change: CheckConvergence's products no longer apply
         double *Xa = colp(ritz, sizeC);
         const int e = borth(c, B, ritz->data, ritz->ld, n, sizeC, sizeX, B != nullptr,
                             g.compW_orth_zero_tol, g.compW_orth_max_reorth, &spmm_calls);
@@ -773,29 +775,64 @@ struct GcgRun {
         startW = endP;
         int bsz = 0;
         double *hscale = c.hbuf.p;
-        bool stored = true;  // every column's A x and B x kept by CheckConvergence
+        // B x of each column: CheckConvergence's product where it checked the
+        // column, else a product here (the last run of unconverged columns may
+        // extend past the checked ones, :285-300); `fresh` lists the latter
+        // (W position, Ritz column, count) for S x0 below
+        std::vector<std::array<int, 3>> fresh;
+        const int chk_hi = chk_lo + chk_n;
         for (int i = 0; i < offset[0]; ++i) {
             const int o1 = offset[2 * i + 1], o2 = offset[2 * i + 2], len = o2 - o1;
             copy_cols(n, len, colp(ritz, o1), ritz->ld, colp(V, startW + bsz), ld, st);
-            if (have_products(o1, o2))
-                copy_cols(n, len, c.chkB.p + (size_t)(o1 - chk_lo) * ld, ld,
+            const int cov = (c.chkB.p != nullptr && o1 >= chk_lo && o1 < chk_hi)
+                                ? std::min(o2, chk_hi) - o1
+                                : 0;
+            if (cov > 0)
+                copy_cols(n, cov, c.chkB.p + (size_t)(o1 - chk_lo) * ld, ld,
                           c.bbuf.p + (size_t)bsz * ld, ld, st);
-            else {
-                applyB(colp(V, o1), ld, c.bbuf.p + (size_t)bsz * ld, ld, len);
-                stored = false;
+            if (len > cov) {
+                applyB(colp(V, o1 + cov), ld, c.bbuf.p + (size_t)(bsz + cov) * ld, ld, len - cov);
+                fresh.push_back({bsz + cov, o1 + cov, len - cov});
             }
             for (int j = 0; j < len; ++j) hscale[bsz + j] = ss_eval[o1 + j] + sigma;
             bsz += len;
         }
         endW = startW + bsz;
+        const bool mixed = c.precision == GCGE_PREC_MIXED && !c.escalated;
+        const int ud = g.user_defined_multi_linear_solver;
+        // S x0 = A x0 + sigma B x0 for the mixed inner solve, from the stored
+        // products and, for the other columns, A x0 here and the B x0 above
+        // (before bbuf is scaled)
+        const bool have_sx = mixed && ud == 0;
+        if (have_sx) {
+            int off = 0;
+            for (int i = 0; i < offset[0]; ++i) {
+                const int o1 = offset[2 * i + 1], o2 = offset[2 * i + 2], len = o2 - o1;
+                const int cov = (c.chkB.p != nullptr && o1 >= chk_lo && o1 < chk_hi)
+                                    ? std::min(o2, chk_hi) - o1
+                                    : 0;
+                if (cov > 0) {
+                    copy_cols(n, cov, c.chkA.p + (size_t)(o1 - chk_lo) * ld, ld,
+                              c.r64.p + (size_t)off * ld, ld, st);
+                    axpby(n, cov, sigma, c.chkB.p + (size_t)(o1 - chk_lo) * ld, ld, 1.0,
+                          c.r64.p + (size_t)off * ld, ld, st);
+                }
+                off += len;
+            }
+            for (const auto &f : fresh) {
+                spmm<double>(A->pat, A->val.p, colp(V, f[1]), ld, c.r64.p + (size_t)f[0] * ld, ld,
+                             f[2], st);
+                spmm_calls++;
+                axpby(n, f[2], sigma, c.bbuf.p + (size_t)f[0] * ld, ld, 1.0,
+                      c.r64.p + (size_t)f[0] * ld, ld, st);
+            }
+        }
         GCGE_CUDA(cudaMemcpyAsync(c.dvec.p, hscale, sizeof(double) * bsz, cudaMemcpyHostToDevice, st));
         scale_columns(n, bsz, c.bbuf.p, ld, c.dvec.p, st);
         // shifted operator S = A + sigma B on the union pattern
-        const bool mixed = c.precision == GCGE_PREC_MIXED && !c.escalated;
         shift_values(c.upat.padded, c.ua.p, c.ub.p, sigma, c.us64.p, mixed ? c.us32.p : nullptr,
                      st);
         timer.mark(PH_LINSOL);
-        const int ud = g.user_defined_multi_linear_solver;
         if (ud == 1 || ud == 2) {
             // the caller's solver (:590-592) on b = (lambda + sigma) B x, which
             // the reference keeps in the Ritz-vector columns [offset[1], +bsz)
@@ -813,23 +850,7 @@ struct GcgRun {
             // BlockPCG after it (ud == 2) starts from its x with its b
             copy_cols(n, bsz, colp(ritz, offset[1]), ritz->ld, c.bbuf.p, ld, st);
         }
-        if (ud != 1) {
-            bool have_sx = false;  // r64 holds S x0
-            if (mixed && stored && ud == 0) {
-                // S x0 = A x0 + sigma B x0 from the stored products
-                int off = 0;
-                for (int i = 0; i < offset[0]; ++i) {
-                    const int o1 = offset[2 * i + 1], len = offset[2 * i + 2] - o1;
-                    copy_cols(n, len, c.chkA.p + (size_t)(o1 - chk_lo) * ld, ld,
-                              c.r64.p + (size_t)off * ld, ld, st);
-                    axpby(n, len, sigma, c.chkB.p + (size_t)(o1 - chk_lo) * ld, ld, 1.0,
-                          c.r64.p + (size_t)off * ld, ld, st);
-                    off += len;
-                }
-                have_sx = true;
-            }
-            w_solve(colp(V, startW), bsz, mixed, have_sx);
-        }
+        if (ud != 1) w_solve(colp(V, startW), bsz, mixed, have_sx);
         timer.mark(PH_W);
         endW = orth(colp(V, 0), ld, n, startW, endW, B != nullptr, g.compW_orth_zero_tol,
                     g.compW_orth_max_reorth, g.compW_orth_method, g.compW_orth_block_size);
