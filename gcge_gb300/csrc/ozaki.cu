@@ -8,22 +8,25 @@
 // Method (error-free digit splitting, the Ozaki scheme): within each chunk of
 // kBK = 64 consecutive k, every row of the left operand and every column of
 // the right operand gets an exponent e with |x| < 2^e over the chunk, and each
-// x is written as 2^e * sum_i d_i 2^(-7(i+1)), i = 0..7, with signed 7-bit
-// digits d_i (56-bit fixed point, truncated).  Digits are exact in bf16.  A
-// chunk's product sum_k x_k y_k is 2^(ea+eb) * sum_l L_l 2^(-7(l+2)) with level
-// sums L_l = sum_{i+j=l} sum_k d_i(x_k) d_j(y_k), l = 0..7 (the 36 digit pairs
-// with i + j <= 7).  |L_l| <= (l+1) * 64 * 127^2 < 2^24, so the level sums of
-// bf16 products accumulated in FP32 by mma.sync are exact integers.  After the
-// chunk they are folded into two exact int64 words, converted exactly to FP64
-// and added, with the chunk scale, into FP64 accumulators.  The truncation
-// error is below 2^-56 of the chunk's largest |x| |y| per product, the same
-// order as FP64 rounding; non-finite inputs give NaN outputs.
+// |x| becomes a 56-bit fixed-point integer X = |x| 2^(56 - e) (truncated)
+// written with 7 digits of 8 bits, X = sum_i d_i 2^(8(6-i)): the leading digit
+// d_0 in [0, 256] and balanced digits d_1..d_6 in [-128, 127] (the bytes of
+// X + 0x808080808080, less 128), each carrying x's sign.  Digits are exact in
+// bf16.  A chunk's product sum_k x_k y_k is 2^(ea+eb-112) * sum_l L_l
+// 2^(8(12-l)) with level sums L_l = sum_{i+j=l} sum_k d_i(x_k) d_j(y_k),
+// l = 0..6 (the 28 digit pairs with i + j <= 6).  |L_l| <= 64 (2 * 256 * 128
+// + 5 * 128^2) < 2^24, so the level sums of bf16 products accumulated in FP32
+// by mma.sync are exact integers.  After the chunk they are folded into two
+// exact int64 words, converted exactly to FP64 and added, with the chunk
+// scale, into FP64 accumulators.  The truncation error is below 2^-55 of the
+// chunk's largest |x| |y| per product, the same order as FP64 rounding;
+// non-finite inputs give NaN outputs.
 //
 // Tiles: a CTA computes a 64 x BN block of the result for a range of k; the
-// operands' digit planes for one chunk sit in shared memory (8 planes each,
+// operands' digit planes for one chunk sit in shared memory (7 planes each,
 // rows padded to 72 bf16 so ldmatrix is conflict-free) and each warp owns a
-// 16 x 8 tile: per 16-wide k step it loads 8 A and 8 B digit fragments and
-// issues 36 MMAs into 8 level accumulators.  Gram products split k over CTAs
+// 16 x 8 tile: per 16-wide k step it loads 7 A and 7 B digit fragments and
+// issues 28 MMAs into 7 level accumulators.  Gram products split k over CTAs
 // (partials summed in a fixed order); linear combinations tile the long row
 // dimension and keep k whole.
 #include <cstdint>
@@ -34,8 +37,7 @@
 namespace gcge {
 namespace {
 
-constexpr int kDigits = 8;
-constexpr int kDigitBits = 7;
+constexpr int kDigits = 7;
 constexpr int kBK = 64;
 constexpr int kBKP = kBK + 8;
 constexpr int kBM = 64;
@@ -58,8 +60,9 @@ __device__ __forceinline__ int exp_field(double x) {
     return max((int)((__double_as_longlong(x) >> 52) & 0x7FF), 1);
 }
 
-// x as a 56-bit fixed-point magnitude relative to 2^(emax - 1022) (emax >=
-// exp_field(x)), split into 32-bit words, and the bias word of its digits:
+// x as a 56-bit fixed-point magnitude X relative to 2^(emax - 1022) (emax >=
+// exp_field(x)), plus 128 in each of its six low bytes (so that byte - 128 is
+// a balanced digit), split into 32-bit words, and the bias word of its digits:
 // +2^23 or -2^23 as an FP32 bit pattern, carrying x's sign.
 struct Fixed56 {
     uint32_t hi, lo;
@@ -72,25 +75,32 @@ __device__ __forceinline__ Fixed56 fixed56(double x, int emax) {
     if (ef != 0) mant |= 0x0010000000000000ull;
     const int sh = max(ef, 1) - emax + 3;  // <= 3: the value < 2^56 in fixed point
     const unsigned long long X = sh >= 0 ? (mant << sh) : (sh > -64 ? (mant >> (-sh)) : 0ull);
+    const unsigned long long Y = X + 0x0000808080808080ull;  // < 2^57
     Fixed56 f;
-    f.hi = (uint32_t)(X >> 32);
-    f.lo = (uint32_t)X;
+    f.hi = (uint32_t)(Y >> 32);
+    f.lo = (uint32_t)Y;
     f.magic = 0x4B000000u | ((uint32_t)(b >> 32) & 0x80000000u);
     return f;
 }
 
-// Digit i (bits 49-7i .. 55-7i of the fixed-point value) as an FP32 number
-// +-d, d in [0, 127]: (bias | d) read as FP32 is +-(2^23 + d), and subtracting
-// the bias +-2^23 leaves +-d exactly.  Its upper 16 bits are its bf16 pattern.
+// Digit i as an FP32 number: (bias | t) read as FP32 is +-(2^23 + t) for the
+// field t (bits 48.. of the biased value for i = 0, else its byte 6 - i), and
+// subtracting +-2^23 (i = 0) or +-(2^23 + 128) leaves +-d_i exactly.  Its
+// upper 16 bits are its bf16 pattern.
 template <int I>
 __device__ __forceinline__ uint32_t digit_f32(const Fixed56 &f) {
-    constexpr int s = 49 - 7 * I;
-    uint32_t t;
-    if constexpr (s >= 32)
-        t = f.hi >> (s - 32);
-    else
-        t = __funnelshift_r(f.lo, f.hi, s);
-    const float v = __uint_as_float((t & 127u) | f.magic) - __uint_as_float(f.magic);
+    float v;
+    if constexpr (I == 0) {
+        v = __uint_as_float((f.hi >> 16) | f.magic) - __uint_as_float(f.magic);
+    } else {
+        constexpr int s = 48 - 8 * I;
+        uint32_t t;
+        if constexpr (s >= 32)
+            t = f.hi >> (s - 32);
+        else
+            t = __funnelshift_r(f.lo, f.hi, s);
+        v = __uint_as_float((t & 255u) | f.magic) - __uint_as_float(f.magic | 128u);
+    }
     return __float_as_uint(v);
 }
 
@@ -369,21 +379,21 @@ __global__ void __launch_bounds__(oz_threads<BN>(), 2) k_oz_gemm(OzArgs a) {
                     for (int j = 0; j < kDigits - i; ++j) mma_bf16(lv[i + j], af, bf[j]);
                 }
             }
-            // the exact level sums as two int64 words (|hi| < 2^42.1, |lo| < 2^44.3
-            // per chunk)
+            // the exact level sums as two int64 words, hi = levels 0..3 in units
+            // of level 3 and lo = levels 4..6 in units of level 6 (|hi| < 2^47.3,
+            // |lo| < 2^39.3 per chunk)
 #pragma unroll
             for (int q = 0; q < 4; ++q) {
                 int L[kDigits];
 #pragma unroll
                 for (int l = 0; l < kDigits; ++l) L[l] = __float2int_rn(lv[l][q]);
-                thi[q] += ((long long)L[0] << 21) + ((long long)L[1] << 14) +
-                          ((long long)L[2] << 7) + (long long)L[3];
-                tlo[q] += ((long long)L[4] << 21) + ((long long)L[5] << 14) +
-                          ((long long)L[6] << 7) + (long long)L[7];
+                thi[q] += ((long long)L[0] << 24) + ((long long)L[1] << 16) +
+                          ((long long)L[2] << 8) + (long long)L[3];
+                tlo[q] += ((long long)L[4] << 16) + ((long long)L[5] << 8) + (long long)L[6];
             }
             __syncthreads();
         }
-        // fold into the FP64 accumulators: value = 2^(ea-1022 + eb-1022 - 63) (hi 2^28 + lo)
+        // fold into the FP64 accumulators: value = 2^(ea-1022 + eb-1022 - 64) (hi 2^24 + lo)
 #pragma unroll
         for (int q = 0; q < 4; ++q) {
             const int rl = m0 + g + ((q >> 1) << 3);
@@ -392,11 +402,11 @@ __global__ void __launch_bounds__(oz_threads<BN>(), 2) k_oz_gemm(OzArgs a) {
             if (ea == 0x7FF || eb == 0x7FF) {
                 acc[q] = __longlong_as_double(0x7FF8000000000000LL);
             } else {
-                const int fld = ea + eb - 1084;  // exponent field of the scale
+                const int fld = ea + eb - 1085;  // exponent field of the scale
                 if (fld > 0) {
                     const double s = fld >= 2047 ? __longlong_as_double(0x7FF0000000000000LL)
                                                  : __longlong_as_double((long long)fld << 52);
-                    const double v = fma(i64_to_f64(thi[q]), 268435456.0, i64_to_f64(tlo[q]));
+                    const double v = fma(i64_to_f64(thi[q]), 16777216.0, i64_to_f64(tlo[q]));
                     acc[q] = fma(v, s, acc[q]);
                 }
             }
