@@ -6,6 +6,7 @@ columns, blocks of bs = 20).
     python -m gcge_gb300.profile_cases lincomb   # X C, X n x 180, C 180 x 20
     python -m gcge_gb300.profile_cases both
     python -m gcge_gb300.profile_cases pcg       # FP32 block PCG, 20 columns, 30 steps
+    python -m gcge_gb300.profile_cases eig       # dense eigensolver, s = 200
 
 Each case runs the FP64-accurate digit-plane product once after one warm-up
 call, through the same C-ABI entry points the parity tests use
@@ -16,6 +17,12 @@ The pcg case runs the persistent FP32 block PCG of the W step (30 CG steps,
 no early stop) on the shifted generalized 64^3 operator A + sigma B through
 GCGE_BlockPCG, once after one warm-up call, and checks that the residual
 dropped; select it with -k regex:k_block_pcg.
+
+The eig case runs the dense eigensolver of the Rayleigh-Ritz step
+(GCGE_DenseEig) on a 200 x 200 matrix shaped like a late GCG projection (a
+diagonal block of 160 Ritz values with double eigenvalues, coupled weakly to a
+dense 40 x 40 block) and checks it against numpy; the FP32 Jacobi kernel is
+k_jacobi32_cluster.
 """
 from __future__ import annotations
 
@@ -69,6 +76,26 @@ def pcg():
     return it == 30 and red < 0.5
 
 
+def eig():
+    rng = np.random.default_rng(5)
+    d = np.sort(rng.uniform(1.0, 100.0, 160))
+    d[10:13] = d[10]
+    M = np.zeros((200, 200))
+    M[:160, :160] = np.diag(d)
+    Cw = 1e-3 * rng.standard_normal((160, 40))
+    M[:160, 160:] = Cw
+    M[160:, :160] = Cw.T
+    Wm = rng.standard_normal((40, 40))
+    M[160:, 160:] = 150.0 + 10.0 * (Wm + Wm.T)
+    G.dense_eig(M)
+    ev, Z = G.dense_eig(M)
+    ref = np.linalg.eigvalsh(M)
+    err = float(np.max(np.abs(ev - ref)) / np.abs(ref).max())
+    res = float(np.abs(M @ Z - Z * ev).max() / np.abs(ref).max())
+    print(f"eig s=200: eigenvalue error {err:.1e}, residual {res:.1e}")
+    return err < 1e-13 and res < 1e-12
+
+
 def main(argv):
     what = argv[1] if len(argv) > 1 else "both"
     ok = True
@@ -78,6 +105,8 @@ def main(argv):
         ok &= lincomb()
     if what == "pcg":
         ok &= pcg()
+    if what == "eig":
+        ok &= eig()
     return 0 if ok else 1
 
 
