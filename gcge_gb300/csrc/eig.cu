@@ -236,6 +236,7 @@ k_jacobi32(int s, const double *__restrict__ M, int ldm, float4 *__restrict__ lo
 // per-CTA off-diagonal masses in the same order, so all take the same decision.
 constexpr int kJC = 8;
 constexpr int kJacClusterMin = 64;  // smaller matrices use the one-CTA kernel
+constexpr int kJacMaxLocal = 32;    // slots per CTA (np <= 256: s <= 512)
 
 __host__ __device__ inline int jc_slots(int np) { return (np + kJC - 1) / kJC; }
 
@@ -269,6 +270,7 @@ k_jacobi32_cluster(int s, const double *__restrict__ M, int ldm, float4 *__restr
     float *red = rows + (size_t)2 * 2 * ks * m;                 // [2][kJC][2]
     __shared__ float wsum[kJacobiThreads / 32][2];
     __shared__ int stop;
+    __shared__ float *s_dst[2 * kJacMaxLocal];  // next-round rows of each local slot
     const size_t bufsz = (size_t)2 * ks * m;
     const int k0 = (rank * np) / kJC, k1 = ((rank + 1) * np) / kJC, nloc = k1 - k0;
     const int t = threadIdx.x, lane = t & 31, warp = t >> 5, nwarps = blockDim.x >> 5;
@@ -357,12 +359,30 @@ k_jacobi32_cluster(int s, const double *__restrict__ M, int ldm, float4 *__restr
                 const float4 e = make_float4(c, sv, __int_as_float(p), __int_as_float(q));
                 for (int cc = 0; cc < kJC; ++cc) *cl.map_shared_rank(tab + k, cc) = e;
                 log[(size_t)round * np + k] = e;
+                // next-round positions of the slot's two rows (circle method)
+                int kt, st_, kb, sb;
+                if (np == 1) {
+                    kt = 0, st_ = 0, kb = 0, sb = 1;
+                } else {
+                    if (k == 0) kt = 0, st_ = 0;
+                    else if (k <= np - 2) kt = k + 1, st_ = 0;
+                    else kt = np - 1, st_ = 1;
+                    if (k == 0) kb = 1, sb = 0;
+                    else kb = k - 1, sb = 1;
+                }
+                const int ot = slot_owner(kt, np), ob = slot_owner(kb, np);
+                const size_t nb = (size_t)(cur ^ 1) * bufsz;
+                float *dt = rows + nb + (size_t)(2 * (kt - (ot * np) / kJC) + st_) * m;
+                float *db = rows + nb + (size_t)(2 * (kb - (ob * np) / kJC) + sb) * m;
+                s_dst[2 * ls] = ot == rank ? dt : cl.map_shared_rank(dt, ot);
+                s_dst[2 * ls + 1] = ob == rank ? db : cl.map_shared_rank(db, ob);
             }
             cl.sync();
             // (b) the 2x2 blocks of the local rows, written to the next buffers
-            const size_t nxt = (size_t)(cur ^ 1) * bufsz;
-            for (int b = t; b < nloc * np; b += blockDim.x) {
-                const int li = b / np, j = b - li * np;
+            const float inv_np = 1.0f / (float)np;  // b / np exactly: the quotient's
+            for (int b = t; b < nloc * np; b += blockDim.x) {  // fraction is >= 0.5 / np away
+                const int li = (int)(((float)b + 0.5f) * inv_np);
+                const int j = b - li * np;
                 const int ki = k0 + li;
                 const float4 ei = tab[ki], ej = tab[j];
                 const float ci = ei.x, si = ei.y, cj = ej.x, sj = ej.y;
@@ -392,22 +412,7 @@ k_jacobi32_cluster(int s, const double *__restrict__ M, int ldm, float4 *__restr
                     o21 = t21 * cj - t22 * sj;
                     o22 = t21 * sj + t22 * cj;
                 }
-                // next-round positions of the two rows (circle method)
-                int kt, st_, kb, sb;
-                if (np == 1) {
-                    kt = 0, st_ = 0, kb = 0, sb = 1;
-                } else {
-                    if (ki == 0) kt = 0, st_ = 0;
-                    else if (ki <= np - 2) kt = ki + 1, st_ = 0;
-                    else kt = np - 1, st_ = 1;
-                    if (ki == 0) kb = 1, sb = 0;
-                    else kb = ki - 1, sb = 1;
-                }
-                const int ot = slot_owner(kt, np), ob = slot_owner(kb, np);
-                float *dt = rows + nxt + (size_t)(2 * (kt - (ot * np) / kJC) + st_) * m;
-                float *db = rows + nxt + (size_t)(2 * (kb - (ob * np) / kJC) + sb) * m;
-                if (ot != rank) dt = cl.map_shared_rank(dt, ot);
-                if (ob != rank) db = cl.map_shared_rank(db, ob);
+                float *dt = s_dst[2 * li], *db = s_dst[2 * li + 1];
                 dt[pj] = o11;
                 dt[qj] = o12;
                 db[pj] = o21;
@@ -437,6 +442,20 @@ static size_t jacobi_dyn_limit() {
         cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
         cudaFuncAttributes fa{};
         cudaFuncGetAttributes(&fa, k_jacobi32);
+        lim = optin > 0 ? (size_t)optin - fa.sharedSizeBytes : 48 * 1024;
+    });
+    return lim;
+}
+// the same for the cluster kernel (its static shared memory differs)
+static size_t jacobi_cluster_dyn_limit() {
+    static std::once_flag once;
+    static size_t lim = 0;
+    std::call_once(once, [] {
+        int dev = 0, optin = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+        cudaFuncAttributes fa{};
+        cudaFuncGetAttributes(&fa, k_jacobi32_cluster);
         lim = optin > 0 ? (size_t)optin - fa.sharedSizeBytes : 48 * 1024;
     });
     return lim;
@@ -510,7 +529,7 @@ static bool jacobi_cluster_usable() {
     static std::once_flag once;
     static bool ok = false;
     std::call_once(once, [] {
-        const size_t lim = jacobi_dyn_limit();
+        const size_t lim = jacobi_cluster_dyn_limit();
         if (cudaFuncSetAttribute(k_jacobi32_cluster, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)lim) != cudaSuccess) {
             cudaGetLastError();
@@ -538,9 +557,10 @@ static bool jacobi_cluster_usable() {
 }
 
 static int jacobi_cluster_max_dim() {
-    const size_t lim = jacobi_dyn_limit();
+    const size_t lim = jacobi_cluster_dyn_limit();
     int s = kJacClusterMin;
-    while (jacobi_cluster_smem_bytes(s + 1) <= lim) ++s;
+    while (jacobi_cluster_smem_bytes(s + 1) <= lim && jc_slots(jac_m(s + 1) / 2) <= kJacMaxLocal)
+        ++s;
     return s;
 }
 
@@ -650,7 +670,8 @@ int sym_eig(EigWork &wk, int s, const double *M, int ld, double *eval_host, doub
                                        (int)jacobi_dyn_limit()));
     });
     const bool cluster = s >= kJacClusterMin && jacobi_cluster_usable() &&
-                         jacobi_cluster_smem_bytes(s) <= jacobi_dyn_limit();
+                         jacobi_cluster_smem_bytes(s) <= jacobi_cluster_dyn_limit() &&
+                         jc_slots(jac_m(s) / 2) <= kJacMaxLocal;
     if (cluster) {
         cudaLaunchConfig_t cfg = {};
         cfg.gridDim = dim3(kJC);
