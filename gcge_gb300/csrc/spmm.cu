@@ -66,10 +66,12 @@ k_residual(const long long *__restrict__ sa, const int *__restrict__ ca,
     __syncthreads();
     // A x and B x, each on its own matrix's SELL pattern (as the reference's
     // two SpMMs and axpby, src/ops_eig_sol_gcg.c:220-238); padding entries
-    // carry a zero value and the row's own column
-    double acc[K], bcc[K];
+    // carry a zero value and the row's own column.  A x is stored before B x
+    // is formed in the same registers (half the registers of keeping both, so
+    // twice the resident warps), and read back for the residual.
+    double acc[K];
 #pragma unroll
-    for (int c = 0; c < K; ++c) acc[c] = bcc[c] = 0.0;
+    for (int c = 0; c < K; ++c) acc[c] = 0.0;
     const int row = slice * 32 + lane;
     if (slice < nslices) {
         for (long long e = sa[slice] + lane, end = sa[slice + 1]; e < end; e += 32) {
@@ -79,32 +81,41 @@ k_residual(const long long *__restrict__ sa, const int *__restrict__ ca,
             for (int c = 0; c < K; ++c)
                 if (c < k) acc[c] = fma(v, __ldg(xj + (size_t)c * ldx), acc[c]);
         }
+    }
+    if (row < n) {
+#pragma unroll
+        for (int c = 0; c < K; ++c)
+            if (c < k) ax[row + (size_t)c * ldo] = acc[c];
+    }
+#pragma unroll
+    for (int c = 0; c < K; ++c) acc[c] = 0.0;
+    if (slice < nslices) {
         if (sb != nullptr) {
             for (long long e = sb[slice] + lane, end = sb[slice + 1]; e < end; e += 32) {
                 const double v = __ldg(vb + e);
                 const double *xj = X + __ldg(cb + e);
 #pragma unroll
                 for (int c = 0; c < K; ++c)
-                    if (c < k) bcc[c] = fma(v, __ldg(xj + (size_t)c * ldx), bcc[c]);
+                    if (c < k) acc[c] = fma(v, __ldg(xj + (size_t)c * ldx), acc[c]);
             }
         } else if (row < n) {  // B = I
 #pragma unroll
             for (int c = 0; c < K; ++c)
-                if (c < k) bcc[c] = X[row + (size_t)c * ldx];
+                if (c < k) acc[c] = X[row + (size_t)c * ldx];
         }
     }
-    if (ax != nullptr && row < n) {  // keep A x and B x for the W step
+    if (row < n) {
 #pragma unroll
         for (int c = 0; c < K; ++c)
-            if (c < k) {
-                ax[row + (size_t)c * ldo] = acc[c];
-                bx[row + (size_t)c * ldo] = bcc[c];
-            }
+            if (c < k) bx[row + (size_t)c * ldo] = acc[c];
     }
 #pragma unroll
     for (int c = 0; c < K; ++c) {
-        const double r = fma(-slam[c], bcc[c], acc[c]);
-        double v = (row < n && c < k) ? r * r : 0.0;
+        double v = 0.0;
+        if (row < n && c < k) {
+            const double r = fma(-slam[c], acc[c], ax[row + (size_t)c * ldo]);
+            v = r * r;
+        }
         for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
         if (lane == 0) red[warp][c] = v;
     }
@@ -149,6 +160,7 @@ int residual_norms(const SellPattern &pa, const double *va, const SellPattern *p
                    const double *vb, const double *X, int ldx, const double *lam, int k,
                    double *partial, int kmax, cudaStream_t st, double *ax, double *bx, int ldo) {
     GCGE_REQUIRE(k <= kMaxChunk && k <= kmax, GCGE_ERR_ARG, "residual_norms: too many columns");
+    GCGE_REQUIRE(ax != nullptr && bx != nullptr, GCGE_ERR_ARG, "residual_norms: no product buffers");
     GCGE_REQUIRE(!pb || (pb->n == pa.n && pb->nslices == pa.nslices), GCGE_ERR_ARG,
                  "residual_norms: patterns differ in size");
     const int blocks = spmm_blocks(pa);
