@@ -123,3 +123,32 @@ def test_mixed_escalates_to_fp64_inner_solve_when_fp32_stalls(gpu_lib):
                           return_eigenvectors=False))
     np.testing.assert_allclose(mixed.eval[:nev], w, rtol=1e-9, atol=0)
     np.testing.assert_allclose(mixed.eval[:nev], fp64.eval[:nev], rtol=1e-10, atol=0)
+
+
+def test_nev200_projected_dimension_400(gpu_lib):
+    """The block rule of the 128^3 variable-coefficient workload (nev 200:
+    bs 40, nevInit 120, nevMax 320) at 16^3: projected dimensions up to 400,
+    the cluster Jacobi's range beyond the one-CTA kernel's.  Mixed and FP64
+    solves agree with each other and with the dense generalized eigenvalues,
+    and every returned pair meets the relative residual tolerance."""
+    import scipy.linalg as sl
+    c = P.config3(16)
+    A, B, nev = c["A"], c["B"], c["nev"]
+    kw = dict(nev=nev, block_size=c["block_size"], nev_init=c["nev_init"], nev_max=c["nev_max"],
+              max_iter=2000)
+    assert (c["block_size"], c["nev_init"], c["nev_max"]) == (40, 120, 320)
+    r64 = gpu_lib.solve(A, B, precision=gpu_lib.PREC_FP64, **kw)
+    rmx = gpu_lib.solve(A, B, precision=gpu_lib.PREC_MIXED, **kw)
+    for r in (r64, rmx):
+        assert r.status == gpu_lib.GCGE_OK and r.nconv >= nev
+    d = B.diagonal()
+    s = 1.0 / np.sqrt(d)
+    H = (A.to_scipy().toarray() * s[:, None]) * s[None, :]
+    ref = sl.eigh(H, eigvals_only=True, subset_by_index=[0, nev - 1])
+    for r in (r64, rmx):
+        assert np.max(np.abs(r.eval[:nev] - ref) / np.abs(ref)) < 1e-10
+        X = r.evec[:, :nev]
+        R = A.to_scipy() @ X - (d[:, None] * X) * r.eval[:nev]
+        rel = np.linalg.norm(R, axis=0) / np.abs(r.eval[:nev])
+        assert rel.max() < 1e-8 * 1.05
+    assert np.max(np.abs(rmx.eval[:nev] - r64.eval[:nev]) / np.abs(r64.eval[:nev])) < 1e-10
