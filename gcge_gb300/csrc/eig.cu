@@ -5,7 +5,7 @@
 // GB300 issues FP64 at ~1/58 of its FP32 rate, so an FP64 Jacobi on one SM
 // would take tens of milliseconds for s = 200.  The solver therefore
 //   1. runs a parallel-order (round-robin) two-sided cyclic Jacobi in FP32,
-//      logging each round's rotations: for s >= 64 in a cluster of 8 CTAs
+//      logging each round's rotations: for s >= 88 in a cluster of 8 CTAs
 //      whose shared memories hold the matrix rows of the pairs each CTA owns
 //      (distributed shared memory; rows move between neighbouring CTAs as the
 //      round-robin order advances), else in one 1024-thread CTA with the
@@ -235,7 +235,10 @@ k_jacobi32(int s, const double *__restrict__ M, int ldm, float4 *__restrict__ lo
 // Rotations and the stopping test are those of k_jacobi32; every CTA sums the
 // per-CTA off-diagonal masses in the same order, so all take the same decision.
 constexpr int kJC = 8;
-constexpr int kJacClusterMin = 64;  // smaller matrices use the one-CTA kernel
+// Smaller matrices use the one-CTA kernel.  Measured on GB300 (RR-shaped
+// matrices, kernel time): s = 64, 80: one CTA 480, 609 us, cluster 510, 652 us;
+// s = 96, 128, 200: one CTA 1152, 2321, 8161 us, cluster 956, 1290, 2403 us.
+constexpr int kJacClusterMin = 88;
 constexpr int kJacMaxLocal = 32;    // slots per CTA (np <= 256: s <= 512)
 
 __host__ __device__ inline int jc_slots(int np) { return (np + kJC - 1) / kJC; }
