@@ -7,6 +7,7 @@ columns, blocks of bs = 20).
     python -m gcge_gb300.profile_cases both
     python -m gcge_gb300.profile_cases pcg       # FP32 block PCG, 20 columns, 30 steps
     python -m gcge_gb300.profile_cases eig       # dense eigensolver, s = 200
+    python -m gcge_gb300.profile_cases pcgsmall  # FP32 block PCG, 2D n = 4160 (cluster form)
 
 Each case runs the FP64-accurate digit-plane product once after one warm-up
 call, through the same C-ABI entry points the parity tests use
@@ -17,6 +18,10 @@ The pcg case runs the persistent FP32 block PCG of the W step (30 CG steps,
 no early stop) on the shifted generalized 64^3 operator A + sigma B through
 GCGE_BlockPCG, once after one warm-up call, and checks that the residual
 dropped; select it with -k regex:k_block_pcg.
+
+The pcgsmall case runs the same solve on a batch-sized operator (anisotropic
+2D 64 x 65, diagonal B, n = 4160, 130 slices), which the library runs in the
+kernel's cluster form (one thread-block cluster, hardware barrier).
 
 The eig case runs the dense eigensolver of the Rayleigh-Ritz step
 (GCGE_DenseEig) on a 200 x 200 matrix shaped like a late GCG projection (a
@@ -76,6 +81,21 @@ def pcg():
     return it == 30 and red < 0.5
 
 
+def pcgsmall():
+    from gcge_gb300 import problems as Pr
+    A = Pr.aniso2d(64, 65, 2.31)
+    B = Pr.diag_matrix(0.5 + 1.5 * Pr.splitmix_uniform(7, A.n, 0))
+    b = np.random.default_rng(4).standard_normal((A.n, W))
+    x0 = np.zeros_like(b)
+    sigma = 0.01
+    G.block_pcg(A, B, sigma, b, x0, max_iter=30, rate=1e-30, tol=1e-30, fp32=True)
+    x, it = G.block_pcg(A, B, sigma, b, x0, max_iter=30, rate=1e-30, tol=1e-30, fp32=True)
+    S = A.to_scipy() + sigma * B.to_scipy()
+    red = float(np.max(np.linalg.norm(b - S @ x, axis=0) / np.linalg.norm(b, axis=0)))
+    print(f"pcg n={A.n} k={W} steps={it}: max relative residual {red:.2e}")
+    return it == 30 and red < 0.5
+
+
 def eig():
     rng = np.random.default_rng(5)
     d = np.sort(rng.uniform(1.0, 100.0, 160))
@@ -107,6 +127,8 @@ def main(argv):
         ok &= pcg()
     if what == "eig":
         ok &= eig()
+    if what == "pcgsmall":
+        ok &= pcgsmall()
     return 0 if ok else 1
 
 
