@@ -586,6 +586,7 @@ void EigWork::reserve(int smax) {
     h_C.alloc(2 * s2);
     h_lam.alloc(smax);
     h_info.alloc(8);
+    std::fill(h_info.p, h_info.p + 8, 0.0);
     cap = smax;
 }
 
@@ -665,6 +666,12 @@ void host_eigh(int n, const double *G, double *w, double *V) {
 int sym_eig(EigWork &wk, int s, const double *M, int ld, double *eval_host, double *Z, int ldz,
             int refine_steps, cudaStream_t st) {
     GCGE_REQUIRE(s >= 1 && s <= wk.cap, GCGE_ERR_ARG, "sym_eig: size");
+    {  // counts of the previous call (its copy has completed by now: every
+       // caller synchronises the stream between two eigensolves)
+        const int *hi = reinterpret_cast<const int *>(wk.h_info.p);
+        wk.last_rounds = hi[0];
+        wk.last_sweeps = hi[1];
+    }
     GCGE_REQUIRE(s <= jacobi_max_dim(), GCGE_ERR_TOO_LARGE,
                  "sym_eig: projected dimension exceeds the shared-memory Jacobi capacity");
     static std::once_flag once;  // allow the largest size once, for every caller thread
@@ -848,11 +855,10 @@ int sym_eig(EigWork &wk, int s, const double *M, int ld, double *eval_host, doub
         wk.last_delta = emax;
         break;
     }
-    int hinfo[3] = {0, 0, 0};
-    GCGE_CUDA(cudaMemcpyAsync(hinfo, wk.info.p, sizeof(int) * 3, cudaMemcpyDeviceToHost, st));
-    GCGE_CUDA(cudaStreamSynchronize(st));
-    wk.last_rounds = hinfo[0];
-    wk.last_sweeps = hinfo[1];
+    // the Jacobi's round and sweep counts reach the host with the caller's
+    // next synchronisation (no wait here); the next call reads them
+    GCGE_CUDA(cudaMemcpyAsync(wk.h_info.p, wk.info.p, sizeof(int) * 3, cudaMemcpyDeviceToHost,
+                              st));
     return GCGE_OK;
 }
 

@@ -87,6 +87,7 @@ void SolverCtx::reserve(int n_, int nev_max, int nev_init, int bs, int spmm_nblo
         dmask.alloc(std::max(smax, 64));
         didx.alloc(std::max(smax, 64));
         hbuf.alloc(s2 + (size_t)cols * cols + 4096);
+        hup.alloc((size_t)4 * smax + 256);
         eig.reserve(smax);
         cap_s = smax;
     }
@@ -180,6 +181,7 @@ int borth(SolverCtx &c, SparseMat *B, double *x, int ldx, int nrows, int start, 
     if (end <= start) return end;
     int k = end - start;
     double *X1 = x + (size_t)start * ldx;
+    bool upload_pending = false;  // a Cholesky-QR coefficient upload from hbuf in flight
     const double reorth_tol = 50.0 * 2.220446049250313e-16;  // src/ops_orth.c:404
     // Two rounds at most.  Cholesky-QR multiplies the block by R^-1, which
     // scales the rounding-level remainder of the prefix components by up to
@@ -225,6 +227,7 @@ int borth(SolverCtx &c, SparseMat *B, double *x, int ldx, int nrows, int start, 
             GCGE_CUDA(cudaMemcpyAsync(c.hbuf.p, c.dC.p, sizeof(double) * k * k,
                                       cudaMemcpyDeviceToHost, st));
             GCGE_CUDA(cudaStreamSynchronize(st));
+            upload_pending = false;
             const double *G = c.hbuf.p;
             double offmax = 0.0;
             for (int a = 0; a < k; ++a)
@@ -277,8 +280,11 @@ int borth(SolverCtx &c, SparseMat *B, double *x, int ldx, int nrows, int start, 
                 copy_cols(nrows, kk, c.T1.p, ld, X1, ldx, st);
             }
             k = kk;
-            // the host buffer is reused next pass: wait for the upload
-            GCGE_CUDA(cudaStreamSynchronize(st));
+            // the next pass downloads its Gram matrix into hbuf[0, k^2), apart
+            // from this upload's source, and waits for that download (so for
+            // this upload) before writing hbuf again; the caller may reuse
+            // hbuf at once, so the last upload is waited for on return
+            upload_pending = kk > 0;
             // two factorisations of a block with kappa < 1e5 leave it orthonormal
             // to rounding (Cholesky-QR2 is stable for kappa^2 eps < 1): its
             // Gram matrix need not be formed again to check
@@ -286,6 +292,7 @@ int borth(SolverCtx &c, SparseMat *B, double *x, int ldx, int nrows, int start, 
         }
         if (start == 0 || kappa < 1e3) break;
     }
+    if (upload_pending) GCGE_CUDA(cudaStreamSynchronize(st));
     return start + k;
 }
 
@@ -736,14 +743,15 @@ struct GcgRun {
         // work = [evec(:, 0:base) | evec(:, cols) with the unconverged X rows zeroed]
         double *wk = c.work.p;
         copy_cols(s, base, c.evec.p, s, wk, s, st);
-        int *hidx = reinterpret_cast<int *>(c.hbuf.p);
+        // c.hup is next written in the next iteration, after several stream
+        // synchronisations: the copies need no wait here
+        int *hidx = reinterpret_cast<int *>(c.hup.p);
         for (int a = 0; a < np; ++a) hidx[a] = cols[a];
         for (int a = 0; a < s; ++a) hidx[np + a] = mask[a];
         GCGE_CUDA(cudaMemcpyAsync(c.didx.p, hidx, sizeof(int) * np, cudaMemcpyHostToDevice, st));
         GCGE_CUDA(cudaMemcpyAsync(c.dmask.p, hidx + np, sizeof(int) * s, cudaMemcpyHostToDevice, st));
         gather_columns(s, np, c.evec.p, s, c.didx.p, wk + (size_t)base * s, s, st);
         zero_rows(s, np, wk + (size_t)base * s, s, c.dmask.p, st);
-        GCGE_CUDA(cudaStreamSynchronize(st));  // hbuf reuse
         // small-space orthonormalisation against the X coefficients (B = I)
         const int endP_local = orth(wk, s, s, base, base + np, false, g.compP_orth_zero_tol,
                                     g.compP_orth_max_reorth, g.compP_orth_method,
@@ -994,14 +1002,15 @@ struct GcgRun {
             for (int j = 0; j < xp; ++j)
                 GCGE_CUDA(cudaMemsetAsync(M + (size_t)j * s, 0, sizeof(double) * xp, st));
             const int nx = sizeX - sizeC;
-            double *hd = c.hbuf.p;
+            // second half of c.hup (ComputeP uses the first): rewritten next
+            // iteration, after the stream has passed this copy
+            double *hd = c.hup.p + 2 * (size_t)c.cap_s;
             for (int i = 0; i < nx; ++i) hd[i] = ss_eval[sizeC + i];
             GCGE_CUDA(cudaMemcpyAsync(c.dvec.p, hd, sizeof(double) * nx, cudaMemcpyHostToDevice, st));
             GCGE_CUDA(cudaMemcpy2DAsync(M, sizeof(double) * (s + 1), c.dvec.p, sizeof(double),
                                         sizeof(double), nx, cudaMemcpyDeviceToDevice, st));
             if (sizeP > 0)
                 copy_cols(sizeP, sizeP, c.ptap.p, sizeP, M + nx + (size_t)nx * s, s, st);
-            GCGE_CUDA(cudaStreamSynchronize(st));  // hbuf reuse
         }
         timer.mark(PH_EIG);
         std::vector<double> w(s);

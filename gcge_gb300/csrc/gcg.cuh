@@ -38,6 +38,10 @@ struct SolverCtx {
     DevBuf<unsigned char> ozb;
     DevBuf<int> dmask, didx;
     PinnedBuf<double> hbuf, hmax;
+    // host staging of small uploads that no later host write touches before
+    // the stream has passed them (ComputeP's column lists, the Ritz values of
+    // the projected matrix), so their copies need no wait
+    PinnedBuf<double> hup;
     EigWork eig;
     PcgWork pcg;
 

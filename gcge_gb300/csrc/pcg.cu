@@ -286,6 +286,25 @@ template <int KP, int NT>
 __device__ __forceinline__ void grid_cols_sum(const double *part, double *out, double *stripe) {
     constexpr int S = NT / KP;
     const int t = threadIdx.x;
+    if (gridDim.x <= 32) {
+        // few blocks (the cluster form): one thread per column, four chains
+        // in a fixed order, no tree and its barriers
+        if (t < KP) {
+            const int nb = gridDim.x;
+            double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0;
+            int b = 0;
+            for (; b + 3 < nb; b += 4) {
+                s0 += __ldcg(part + (size_t)b * KP + t);
+                s1 += __ldcg(part + (size_t)(b + 1) * KP + t);
+                s2 += __ldcg(part + (size_t)(b + 2) * KP + t);
+                s3 += __ldcg(part + (size_t)(b + 3) * KP + t);
+            }
+            for (; b < nb; ++b) s0 += __ldcg(part + (size_t)b * KP + t);
+            out[t] = (s0 + s1) + (s2 + s3);
+        }
+        __syncthreads();
+        return;
+    }
     double s = 0.0;
     if (t < S * KP) {
         const int c = t % KP;
