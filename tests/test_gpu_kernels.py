@@ -65,8 +65,11 @@ def test_dense_eig_rr_structure(gpu_lib):
 
 
 @pytest.mark.parametrize("fp32", [False, True])
-def test_block_pcg_matches_oracle(gpu_lib, fp32):
-    A = P.laplace2d(30, 30)
+@pytest.mark.parametrize("grid", [30, 170])
+def test_block_pcg_matches_oracle(gpu_lib, fp32, grid):
+    """n = 900 runs the kernel's cluster form, n = 28900 (904 slices) its
+    grid form with the cooperative launch."""
+    A = P.laplace2d(grid, grid)
     B = P.diag_matrix(0.5 + 1.5 * P.splitmix_uniform(3, A.n, 0))
     rng = np.random.default_rng(4)
     b = rng.standard_normal((A.n, 5))
