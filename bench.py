@@ -250,6 +250,8 @@ def run_ours(args, d: Dist):
     prep_mixed = G.Prepared(A, B, precision=G.PREC_MIXED, **kw)
     prep_fp64 = G.Prepared(A, B, precision=G.PREC_FP64, **kw)
 
+    last_eval = {}
+
     def timed(prep, steps):
         infos, pairs = [], 0
         d.barrier()
@@ -258,6 +260,7 @@ def run_ours(args, d: Dist):
                 r = prep.solve()  # returns after the solve's last device work
                 infos.append(r.info)
                 pairs += min(r.nconv, nev) if r.status == G.GCGE_OK else 0
+        last_eval[id(prep)] = r.eval[:nev].copy()
         return tm.ms / 1000.0, pairs, infos
 
     def percentile(xs, q):
@@ -298,6 +301,15 @@ def run_ours(args, d: Dist):
         r = G.solve(pA, pB, precision=G.PREC_MIXED, evec_out=evec_out, eval_out=ev_out, **kw_e2e)
         e2e_pairs += min(r.nconv, nev) if r.status == G.GCGE_OK else 0
     t_e2e = d.max(time.perf_counter() - t0)
+    # accuracy of the mixed solve: eigenvalues against the FP64 solve, and the
+    # relative residuals ||A x - lambda B x|| / |lambda| of the returned pairs
+    # (host sparse products on the e2e solve's eigenvectors, outside the timing)
+    ev_m, ev_f = last_eval[id(prep_mixed)], last_eval[id(prep_fp64)]
+    eig_err = float(np.max(np.abs(ev_m - ev_f) / np.abs(ev_f)))
+    Xe = np.asarray(evec_out)[:, :nev]
+    lam = np.asarray(ev_out)[:nev]
+    Rr = A.to_scipy() @ Xe - (B.to_scipy() @ Xe) * lam
+    max_res = float(np.max(np.linalg.norm(Rr, axis=0) / np.abs(lam)))
     # per-solve latency of the mixed solve (host clock around each solve,
     # which returns after its device work)
     lat = [1000.0 * i["seconds"] for i in infos]
@@ -327,6 +339,8 @@ def run_ours(args, d: Dist):
         "config": dict(WORKLOAD, precision="mixed", parallelism=f"replicas x{d.world}"),
         "fp64_value": fp64_value, "mixed_over_fp64": value / fp64_value if fp64_value else None,
         "fp64_ms_per_step": t_fp64 / max(1, args.steps // 2) * 1000.0,
+        "eigenvalue_rel_error_vs_fp64": eig_err,
+        "max_rel_residual": max_res,
         "niter": [i["niter"] for i in infos], "nconv": [i["nconv"] for i in infos],
         "phase_ms_last_step": infos[-1]["phase_ms"], "phase_ms_fp64": infos64[-1]["phase_ms"],
         "gpu_launches": sum(i["kernel_launches"] for i in infos),
@@ -490,6 +504,10 @@ def run_vardiff(args, d: Dist):
     re = G.solve(pA, pB, precision=G.PREC_MIXED, evec_out=evec_out, eval_out=ev_out, **kw)
     t_e2e = d.max(time.perf_counter() - t0)
     e2e_pairs = min(re.nconv, nev) if re.status == G.GCGE_OK else 0
+    Xe = np.asarray(evec_out)[:, :nev]
+    lam = np.asarray(ev_out)[:nev]
+    Rr = A.to_scipy() @ Xe - (B.to_scipy() @ Xe) * lam
+    max_res = float(np.max(np.linalg.norm(Rr, axis=0) / np.abs(lam)))
     pcg_ms = sum(i["pcg_kernel_ms"] for i in infos)
     pcg_bytes = sum(i["pcg_kernel_bytes"] for i in infos)
     pcg_launches = sum(i["pcg_kernel_launches"] for i in infos)
@@ -510,6 +528,7 @@ def run_vardiff(args, d: Dist):
         "fp64_value": fp64_value, "mixed_over_fp64": value / fp64_value if fp64_value else None,
         "fp64_ms_per_step": t_fp64 * 1000.0,
         "eigenvalue_rel_error_vs_fp64": err,
+        "max_rel_residual": max_res,
         "niter": [i["niter"] for i in infos], "nconv": [i["nconv"] for i in infos],
         "fp64_niter": r64.niter, "fp64_nconv": r64.nconv,
         "phase_ms_last_step": infos[-1]["phase_ms"], "phase_ms_fp64": r64.info["phase_ms"],
