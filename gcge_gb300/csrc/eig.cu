@@ -582,6 +582,7 @@ void EigWork::reserve(int smax) {
     max_rounds = kMaxSweeps * (m - 1);
     log.alloc((size_t)max_rounds * (m / 2) + 1);  // (c, s, p, q) per pair and round
     gscr.alloc(gram_scratch_elems(smax, smax, smax));
+    ozb.alloc(oz_lincomb_scratch_bytes(smax, smax));
     h_S.alloc(s2);
     h_C.alloc(2 * s2);
     h_lam.alloc(smax);
@@ -664,7 +665,7 @@ void host_eigh(int n, const double *G, double *w, double *V) {
 // is of the order max|E|^2 / gap); that step folds the ascending sort into the
 // update and writes Z.
 int sym_eig(EigWork &wk, int s, const double *M, int ld, double *eval_host, double *Z, int ldz,
-            int refine_steps, cudaStream_t st) {
+            int refine_steps, cudaStream_t st, bool emulated) {
     GCGE_REQUIRE(s >= 1 && s <= wk.cap, GCGE_ERR_ARG, "sym_eig: size");
     {  // counts of the previous call (its copy has completed by now: every
        // caller synchronises the stream between two eigensolves)
@@ -718,7 +719,19 @@ int sym_eig(EigWork &wk, int s, const double *M, int ld, double *eval_host, doub
     count_launch(2);
     const int lds = s;
     double *X = wk.X.p, *Xn = wk.X2.p;
-    const size_t gs = wk.gscr.n;
+    // s x s products of the refinement: X^T P (ld s) and A B (ld of A given)
+    auto sgram = [&](const double *P, double *C) {
+        if (emulated)
+            oz_gram(s, s, s, X, lds, P, lds, C, lds, wk.gscr.p, wk.gscr.n, st);
+        else
+            gram(s, s, s, X, lds, P, lds, C, lds, wk.gscr.p, wk.gscr.n, st);
+    };
+    auto slincomb = [&](const double *A, int lda, const double *B, double *Y, int ldy) {
+        if (emulated)
+            oz_lincomb(s, s, s, A, lda, B, lds, Y, ldy, nullptr, 0, st, 1.0, wk.ozb.p, wk.ozb.n);
+        else
+            lincomb(s, s, s, A, lda, B, lds, Y, ldy, nullptr, 0, st);
+    };
     const size_t s2 = (size_t)s * s;
     double *hS = wk.h_S.p, *hG = wk.h_C.p + s2, *hC = wk.h_C.p;
     std::vector<double> lam(s);
@@ -732,9 +745,9 @@ int sym_eig(EigWork &wk, int s, const double *M, int ld, double *eval_host, doub
     };
     const int steps = std::max(2, refine_steps);
     for (int step = 0; step < steps; ++step) {
-        gram(s, s, s, X, lds, X, lds, wk.G.p, lds, wk.gscr.p, gs, st);
-        lincomb(s, s, s, M, ld, X, lds, wk.W.p, lds, nullptr, 0, st);
-        gram(s, s, s, X, lds, wk.W.p, lds, wk.S.p, lds, wk.gscr.p, gs, st);
+        sgram(X, wk.G.p);
+        slincomb(M, ld, X, wk.W.p, lds);
+        sgram(wk.W.p, wk.S.p);
         GCGE_CUDA(cudaMemcpyAsync(hS, wk.S.p, sizeof(double) * s2, cudaMemcpyDeviceToHost, st));
         GCGE_CUDA(cudaMemcpyAsync(hG, wk.G.p, sizeof(double) * s2, cudaMemcpyDeviceToHost, st));
         GCGE_CUDA(cudaStreamSynchronize(st));
@@ -836,7 +849,7 @@ int sym_eig(EigWork &wk, int s, const double *M, int ld, double *eval_host, doub
         wk.last_steps = step + 1;
         if (!last) {
             GCGE_CUDA(cudaMemcpyAsync(wk.C.p, hC, sizeof(double) * s2, cudaMemcpyHostToDevice, st));
-            lincomb(s, s, s, X, lds, wk.C.p, lds, Xn, lds, nullptr, 0, st);
+            slincomb(X, lds, wk.C.p, Xn, lds);
             std::swap(X, Xn);
             // hC is rewritten only after the next step's synchronisation, which
             // follows this copy on the stream
@@ -851,7 +864,7 @@ int sym_eig(EigWork &wk, int s, const double *M, int ld, double *eval_host, doub
             eval_host[j] = lam[ord[j]];
         }
         GCGE_CUDA(cudaMemcpyAsync(wk.C.p, hP, sizeof(double) * s2, cudaMemcpyHostToDevice, st));
-        lincomb(s, s, s, X, lds, wk.C.p, lds, Z, ldz, nullptr, 0, st);
+        slincomb(X, lds, wk.C.p, Z, ldz);
         wk.last_delta = emax;
         break;
     }

@@ -9,6 +9,7 @@ struct EigWork {
     int max_rounds = 0;
     DevBuf<double> G, W, S, C, X, X2, lam, delta, gscr;
     DevBuf<float4> log;  // rotation log: (c, s, p, q as int bits) per pair and round
+    DevBuf<unsigned char> ozb;  // right-operand digit planes of the emulated products
     DevBuf<int> info;
     PinnedBuf<double> h_S, h_C, h_lam, h_info;
     double last_delta = 0, last_orth = 0;
@@ -27,8 +28,10 @@ void host_eigh(int n, const double *G, double *w, double *V);
 
 // Eigenpairs of the symmetric s x s matrix M (device, leading dim ld):
 // ascending eigenvalues to eval_host, orthonormal eigenvectors to Z
-// (device, ldz).  refine_steps Ogita-Aishima steps follow the FP32 Jacobi.
+// (device, ldz).  refine_steps Ogita-Aishima steps follow the FP32 Jacobi;
+// with `emulated` their s x s products run on the FP64-accurate digit-plane
+// tensor-core kernels instead of the FP64 units.
 int sym_eig(EigWork &wk, int s, const double *M, int ld, double *eval_host, double *Z, int ldz,
-            int refine_steps, cudaStream_t st);
+            int refine_steps, cudaStream_t st, bool emulated = false);
 
 }  // namespace gcge

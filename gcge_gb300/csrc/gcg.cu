@@ -1014,7 +1014,8 @@ struct GcgRun {
         }
         timer.mark(PH_EIG);
         std::vector<double> w(s);
-        sym_eig(c.eig, s, M, s, w.data(), c.evec.p, s, c.refine_steps, st);
+        sym_eig(c.eig, s, M, s, w.data(), c.evec.p, s, c.refine_steps, st,
+                c.precision == GCGE_PREC_MIXED && !c.escalated);
         for (int i = 0; i < s; ++i) ss_eval[sizeC + i] = w[i] - 0.0;
         timer.mark(PH_RR);
     }
