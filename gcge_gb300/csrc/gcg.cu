@@ -964,10 +964,10 @@ struct GcgRun {
         const int s_prev = sizeV - sizeC;
         if (sizeP > 0) {
             // PtAP = coefP^T Mold coefP in the previous projected space (:942-955)
-            lincomb(s_prev, s_prev, sizeP, M, s_prev, c.coefP.p, s_prev, c.dtmp.p, s_prev, nullptr,
-                    0, st);
-            gram(s_prev, sizeP, sizeP, c.coefP.p, s_prev, c.dtmp.p, s_prev, c.ptap.p, sizeP,
-                 c.gscr.p, c.gscr.n, st);
+            dlincomb(c, s_prev, s_prev, sizeP, M, s_prev, c.coefP.p, s_prev, c.dtmp.p, s_prev,
+                     nullptr, 0, st);
+            dgram(c, s_prev, sizeP, sizeP, c.coefP.p, s_prev, c.dtmp.p, s_prev, c.ptap.p, sizeP,
+                  c.gscr.p, c.gscr.n, st);
         }
         sizeV = sizeX + sizeP + sizeW;
         startN += nevConv - sizeC;
