@@ -55,3 +55,17 @@ def test_bench_single_rank_needs_no_process_group():
     d = bench.Dist()
     assert d.pg is None and d.max(3.5) == 3.5 and d.sum(2.0) == 2.0
     d.barrier()
+
+
+def test_reference_arm_reports_large_workload_unavailable():
+    """The CPU reference arm is not sampled on the 128^3 workload: one JSON
+    line with impl "reference" and the reason, exit status 0."""
+    import json
+    import subprocess
+    out = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference",
+                          "--workload", "vardiff3d"], capture_output=True, text=True, timeout=120)
+    assert out.returncode == 0
+    lines = [ln for ln in out.stdout.splitlines() if ln.startswith("{")]
+    assert len(lines) == 1
+    rec = json.loads(lines[0])
+    assert rec["impl"] == "reference" and "unavailable" in rec
