@@ -700,7 +700,7 @@ struct GcgRun {
     // Precision escalation of the mixed solve.  The FP32 inner solve sees the
     // shifted operator with entry errors of about eps32 |S|, which the
     // near-singular shift (0.01 of a gap from the target eigenvalue) amplifies,
-    // and the digit products are exact only to 2^-56 of each chunk's largest
+    // and the digit products are exact only to 2^-55 of each chunk's largest
     // entries; for tolerances tight against |A| (small eigenvalues, tol ~1e-10)
     // the residuals then stop falling just above the tolerance.  When the
     // first unconverged residual is within 100x of the tolerance and shrinks

@@ -1,7 +1,8 @@
 // Block conjugate gradient on (A + sigma B) x = b for all columns of a block
 // at once (reference BlockPCG, src/ops_lin_sol.c:140-437).
 //
-// The whole solve is ONE cooperative (persistent) kernel launch.  Each block
+// The whole solve is ONE persistent kernel launch (cooperative grid, or one
+// thread-block cluster for small operators, below).  Each block
 // owns a contiguous range of SELL slices (balanced by stored entries) and the
 // rows they cover; the iteration runs in three phases separated by grid-wide
 // barriers:

@@ -59,7 +59,7 @@ struct PcgWork {
 // Solve S x = b column-wise (S on the SELL pattern `pat` with values sval)
 // starting from x (or from 0 when x_zero, in which case x need not be
 // initialised).  B, X, R, P, W are slice-blocked n x kp blocks
-// (pcg_block_elems; padding rows and columns of B and X zero).  One cooperative launch runs the
+// (pcg_block_elems; padding rows and columns of B and X zero).  One persistent launch runs the
 // whole iteration; the iteration count and any error stay on the device
 // (PcgWork::collect, or pcg_last_iters after a synchronisation).
 template <typename T>
