@@ -6,6 +6,7 @@ stores eigenvalues, converged counts and iteration counts (golden.json) plus
 the leading eigenvectors of the small cases (golden_vectors.npz).
 
     make -C oracle/ref && OPENBLAS_NUM_THREADS=1 python tests/golden/make_golden.py
+    OPENBLAS_NUM_THREADS=1 python tests/golden/make_golden.py vardiff3d_12_nev200   # one case
 
 The reference tree must be present; the fixtures it writes are what the
 tests use everywhere else (including on machines without the reference).
@@ -46,6 +47,10 @@ def cases():
     out["laplace3d_mass_24"] = (lambda: (P.laplace3d(24), P.mass3d(24)), 100, bs, ni, nm, {}, False)
     bs, ni, nm = rule(20)
     out["vardiff3d_12"] = (lambda: P.vardiff3d(12, seed=3), 20, bs, ni, nm, {}, True)
+    # the block rule of the 128^3 variable-coefficient workload (nev 200: bs 40,
+    # nevInit 120, nevMax 320; projected dimensions up to 400)
+    bs, ni, nm = rule(200)
+    out["vardiff3d_12_nev200"] = (lambda: P.vardiff3d(12, seed=3), 200, bs, ni, nm, {}, False)
     bs, ni, nm = rule(16)
     out["aniso2d_40x30_eps10_diagB"] = (
         lambda: (P.aniso2d(40, 30, 10.0), P.diag_matrix(0.5 + 1.5 * P.splitmix_uniform(11, 1200, 0))),
@@ -56,11 +61,19 @@ def cases():
     return out
 
 
-def main():
+def main(only=None):
+    """All cases, or only the named ones (merged into the existing fixtures)."""
     if not ref_lib.available():
         raise SystemExit("oracle/_ref/libgcge_ref.so missing: run make -C oracle/ref")
     out, vecs = {}, {}
+    if only:
+        with open(os.path.join(HERE, "golden.json")) as f:
+            out = json.load(f)
+        with np.load(os.path.join(HERE, "golden_vectors.npz")) as z:
+            vecs = {k: z[k] for k in z.files}
     for name, (builder, nev, bs, ni, nm, opt, keep) in cases().items():
+        if only and name not in only:
+            continue
         A, B = builder()
         X0 = P.initial_block(A.n, ni, seed=1)
         tol = opt.get("tol", (1e300, 1e-8))
@@ -81,4 +94,4 @@ def main():
 
 
 if __name__ == "__main__":
-    main()
+    main(sys.argv[1:] or None)

@@ -10,7 +10,8 @@ from oracle import ref_lib
 from oracle.gcg_oracle import GCGOracle, GCGParams, gcg_solve, residuals
 
 FAST_CASES = ["laplace2d_24x24_nev8", "laplace2d_24x24_noshift", "laplace2d_20x20_abstol",
-              "vardiff3d_12", "aniso2d_40x30_eps10_diagB", "rgg_2000_deg10"]
+              "vardiff3d_12", "vardiff3d_12_nev200", "aniso2d_40x30_eps10_diagB",
+              "rgg_2000_deg10"]
 
 
 def run_oracle(case, g):
