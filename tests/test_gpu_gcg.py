@@ -13,7 +13,8 @@ pytestmark = pytest.mark.gpu
 
 CASES = ["laplace2d_24x24_nev8", "laplace2d_24x24_noshift", "laplace2d_20x20_abstol",
          "laplace2d_128x128_nev20_bs20", "laplace2d_128x128_nev20_rule", "laplace3d_mass_16",
-         "laplace3d_mass_24", "vardiff3d_12", "aniso2d_40x30_eps10_diagB", "rgg_2000_deg10"]
+         "laplace3d_mass_24", "vardiff3d_12", "vardiff3d_12_nev200", "aniso2d_40x30_eps10_diagB",
+         "rgg_2000_deg10"]
 
 
 def run_gpu(G, case, g, precision=0):
