@@ -59,51 +59,81 @@ const char *status_string(int s) {
 }
 
 namespace {
-struct ThreadStream {
+// Per-device facts, queried once per device: SM count, and the stream-ordered
+// pool told to keep freed blocks cached for reuse.
+struct DeviceInfo {
+    std::once_flag once;
+    int sms = 0;
+};
+DeviceInfo g_dev[kMaxDevices];
+std::once_flag g_count_once;
+int g_ndev = 0;
+
+// The calling thread's stream and OPS-slot staging buffers on each device it
+// has used.  Destroyed at thread exit: buffers freed on their own stream, then
+// the stream synchronised and destroyed.
+struct ThreadDevice {
     cudaStream_t s = nullptr;
-    ~ThreadStream() {
-        if (s) {
-            cudaStreamSynchronize(s);
-            cudaStreamDestroy(s);
+    SlotStage stage;
+};
+struct ThreadCtx {
+    ThreadDevice dev[kMaxDevices];
+    ~ThreadCtx() {
+        for (int d = 0; d < kMaxDevices; ++d) {
+            ThreadDevice &t = dev[d];
+            if (!t.s) continue;
+            if (cudaSetDevice(d) != cudaSuccess) continue;
+            t.stage.release_on(t.s);
+            cudaStreamSynchronize(t.s);
+            cudaStreamDestroy(t.s);
+            t.s = nullptr;
         }
     }
 };
-thread_local ThreadStream t_stream;
-std::once_flag g_device_once;
-bool g_have_device = false;
-int g_sms = 0;
+thread_local ThreadCtx t_ctx;
+}  // namespace
 
-void device_init() {
-    std::call_once(g_device_once, [] {
-        int ndev = 0;
-        if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return;
-        int dev = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&g_sms, cudaDevAttrMultiProcessorCount, dev);
-        if (g_sms <= 0) g_sms = 148;
-        // keep freed pool blocks cached for reuse instead of returning them
+void SlotStage::release_on(cudaStream_t st) {
+    dcoef.release_on(st);
+    dbeta.release_on(st);
+    dres.release_on(st);
+    scr.release_on(st);
+}
+
+int current_device() {
+    std::call_once(g_count_once, [] {
+        if (cudaGetDeviceCount(&g_ndev) != cudaSuccess) {
+            cudaGetLastError();
+            g_ndev = 0;
+        }
+    });
+    if (g_ndev <= 0) throw CudaError{GCGE_ERR_NO_DEVICE, "no CUDA device visible"};
+    int dev = 0;
+    GCGE_CUDA(cudaGetDevice(&dev));
+    GCGE_REQUIRE(dev >= 0 && dev < kMaxDevices, GCGE_ERR_NO_DEVICE, "device index out of range");
+    DeviceInfo &d = g_dev[dev];
+    std::call_once(d.once, [&d, dev] {
+        if (cudaDeviceGetAttribute(&d.sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+            d.sms <= 0) {
+            cudaGetLastError();
+            d.sms = 148;
+        }
         cudaMemPool_t pool;
         if (cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
             unsigned long long keep = ~0ULL;
             cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
         }
-        g_have_device = true;
     });
-    if (!g_have_device) throw CudaError{GCGE_ERR_NO_DEVICE, "no CUDA device visible"};
+    return dev;
 }
-}  // namespace
 
 cudaStream_t lib_stream() {
-    if (t_stream.s == nullptr) {
-        device_init();
-        GCGE_CUDA(cudaStreamCreateWithFlags(&t_stream.s, cudaStreamNonBlocking));
-    }
-    return t_stream.s;
+    ThreadDevice &t = t_ctx.dev[current_device()];
+    if (t.s == nullptr) GCGE_CUDA(cudaStreamCreateWithFlags(&t.s, cudaStreamNonBlocking));
+    return t.s;
 }
-int device_sms() {
-    device_init();
-    return g_sms;
-}
+int device_sms() { return g_dev[current_device()].sms; }
+SlotStage &slot_stage() { return t_ctx.dev[current_device()].stage; }
 
 MultiVec *as_mv(void *h) {
     MultiVec *m = reinterpret_cast<MultiVec *>(h);
@@ -342,8 +372,9 @@ static void CUDA_MultiVecLinearComb(void **x, void **y, int is_vec, int *start, 
         if (k == 0 || m == 0 || Y->nrows == 0) return;
         check_range(Y, start[1], end[1], "MultiVecLinearComb y");
         cudaStream_t st = lib_stream();
-        static DevBuf<double> dcoef, dbeta;
-        static PinnedBuf<double> hstage;
+        SlotStage &sg = slot_stage();
+        DevBuf<double> &dcoef = sg.dcoef, &dbeta = sg.dbeta;
+        PinnedBuf<double> &hstage = sg.hstage;
         double *Yp = Y->data + (size_t)start[1] * Y->ld;
         const double *dB = nullptr;
         if (beta) {
@@ -385,8 +416,9 @@ static void inner_prod_impl(char nsd, MultiVec *X, MultiVec *Y, int *start, int 
     check_range(Y, start[1], end[1], "MultiVecInnerProd y");
     GCGE_REQUIRE(X->nrows == Y->nrows, GCGE_ERR_ARG, "MultiVecInnerProd: rows differ");
     cudaStream_t st = lib_stream();
-    static DevBuf<double> dres, scr;
-    static PinnedBuf<double> hres;
+    SlotStage &sg = slot_stage();
+    DevBuf<double> &dres = sg.dres, &scr = sg.scr;
+    PinnedBuf<double> &hres = sg.hres;
     const int n = X->nrows;
     const double *Xp = X->data + (size_t)start[0] * X->ld;
     const double *Yp = Y->data + (size_t)start[1] * Y->ld;
@@ -657,6 +689,7 @@ void OPS_Destroy(OPS **ops) {
     if (!ops || !*ops) return;
     orth_release(*ops);
     ctx_release(*ops);
+    linsol_release(*ops);
     if ((*ops)->lapack_ops) OPS_Destroy(&(*ops)->lapack_ops);
     free(*ops);
     *ops = nullptr;

@@ -6,6 +6,7 @@
 
 #include <cstdint>
 #include <cstdio>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -44,12 +45,30 @@ struct CudaError {
 extern thread_local unsigned long long t_kernel_launches;
 inline void count_launch(int k = 1) { t_kernel_launches += (unsigned long long)k; }
 
-// The calling thread's stream (created on first use, destroyed at thread
-// exit): every kernel and copy of a solve runs on it, so solves driven from
-// different host threads overlap on the device.
+// Devices a process may drive (indices of per-device caches).
+constexpr int kMaxDevices = 64;
+// The current device's index, validated; the first call on a device queries
+// its attributes.  Throws GCGE_ERR_NO_DEVICE without a device.
+int current_device();
+// The calling thread's stream on the current device (created on first use,
+// destroyed at thread exit): every kernel and copy of a solve runs on it, so
+// solves driven from different host threads overlap on the device.
 cudaStream_t lib_stream();
-// Streaming multiprocessors of the current device (queried once).
+// Streaming multiprocessors of the current device (queried once per device).
 int device_sms();
+// A value computed once per device, on first use with that device current
+// (kernel attributes, occupancy and cluster limits are per device).
+template <typename T>
+struct PerDevice {
+    std::once_flag once[kMaxDevices];
+    T value[kMaxDevices]{};
+    template <typename F>
+    T &get(F &&f) {
+        const int d = current_device();
+        std::call_once(once[d], [&] { value[d] = f(); });
+        return value[d];
+    }
+};
 // Number of solves sharing the device with the calling thread's solves (0 or
 // 1: the whole device); the persistent block-PCG kernel then takes that share
 // of the co-resident grid, so the cooperative kernels of concurrent solves
@@ -77,6 +96,12 @@ struct DevBuf {
             if (st) cudaFreeAsync(p, st);
             else cudaFree(p);
         }
+        p = nullptr;
+        n = 0;
+    }
+    // free on a given stream (teardown of a thread's per-device state)
+    void release_on(cudaStream_t st) {
+        if (p) cudaFreeAsync(p, st);
         p = nullptr;
         n = 0;
     }
@@ -114,6 +139,17 @@ struct PinnedBuf {
         n = count;
     }
 };
+
+// Staging buffers of the OPS slots that move coefficients and inner products
+// across the host boundary (MultiVecLinearComb, MultiVecInnerProd).  One set
+// per host thread and device (slot_stage()), so slots called concurrently from
+// several threads, or on several devices, never share a buffer.
+struct SlotStage {
+    DevBuf<double> dcoef, dbeta, dres, scr;
+    PinnedBuf<double> hstage, hres;
+    void release_on(cudaStream_t st);
+};
+SlotStage &slot_stage();
 
 // ---------------------------------------------------------------- objects
 constexpr uint32_t kMultiVecMagic = 0x4D564755u;  // multivector

@@ -437,31 +437,25 @@ k_jacobi32_cluster(int s, const double *__restrict__ M, int ldm, float4 *__restr
 // Largest dynamic shared memory the Jacobi kernel may request: the device's
 // opt-in per-block limit minus the kernel's static shared memory.
 static size_t jacobi_dyn_limit() {
-    static std::once_flag once;
-    static size_t lim = 0;
-    std::call_once(once, [] {
-        int dev = 0, optin = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    static PerDevice<size_t> cache;
+    return cache.get([] {
+        int optin = 0;
+        cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, current_device());
         cudaFuncAttributes fa{};
         cudaFuncGetAttributes(&fa, k_jacobi32);
-        lim = optin > 0 ? (size_t)optin - fa.sharedSizeBytes : 48 * 1024;
+        return optin > 0 ? (size_t)optin - fa.sharedSizeBytes : (size_t)48 * 1024;
     });
-    return lim;
 }
 // the same for the cluster kernel (its static shared memory differs)
 static size_t jacobi_cluster_dyn_limit() {
-    static std::once_flag once;
-    static size_t lim = 0;
-    std::call_once(once, [] {
-        int dev = 0, optin = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    static PerDevice<size_t> cache;
+    return cache.get([] {
+        int optin = 0;
+        cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, current_device());
         cudaFuncAttributes fa{};
         cudaFuncGetAttributes(&fa, k_jacobi32_cluster);
-        lim = optin > 0 ? (size_t)optin - fa.sharedSizeBytes : 48 * 1024;
+        return optin > 0 ? (size_t)optin - fa.sharedSizeBytes : (size_t)48 * 1024;
     });
-    return lim;
 }
 
 // V = J_1 J_2 ... J_T, one warp per row of V: row r starts as e_r and every
@@ -529,14 +523,13 @@ static void launch_rotations(int s, const float4 *log, const int *info, double *
 // Whether a cluster of kJC CTAs with the largest shared memory the cluster
 // kernel may use can be resident on this device (checked once).
 static bool jacobi_cluster_usable() {
-    static std::once_flag once;
-    static bool ok = false;
-    std::call_once(once, [] {
+    static PerDevice<bool> cache;
+    return cache.get([] {
         const size_t lim = jacobi_cluster_dyn_limit();
         if (cudaFuncSetAttribute(k_jacobi32_cluster, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)lim) != cudaSuccess) {
             cudaGetLastError();
-            return;
+            return false;
         }
         cudaLaunchConfig_t cfg = {};
         cfg.gridDim = dim3(kJC);
@@ -552,11 +545,10 @@ static bool jacobi_cluster_usable() {
         int n = 0;
         if (cudaOccupancyMaxActiveClusters(&n, k_jacobi32_cluster, &cfg) != cudaSuccess) {
             cudaGetLastError();
-            return;
+            return false;
         }
-        ok = n > 0;
+        return n > 0;
     });
-    return ok;
 }
 
 static int jacobi_cluster_max_dim() {
@@ -675,10 +667,11 @@ int sym_eig(EigWork &wk, int s, const double *M, int ld, double *eval_host, doub
     }
     GCGE_REQUIRE(s <= jacobi_max_dim(), GCGE_ERR_TOO_LARGE,
                  "sym_eig: projected dimension exceeds the shared-memory Jacobi capacity");
-    static std::once_flag once;  // allow the largest size once, for every caller thread
-    std::call_once(once, [] {
+    static PerDevice<bool> smem_set;  // allow the largest size once per device
+    smem_set.get([] {
         GCGE_CUDA(cudaFuncSetAttribute(k_jacobi32, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        (int)jacobi_dyn_limit()));
+        return true;
     });
     const bool cluster = s >= kJacClusterMin && jacobi_cluster_usable() &&
                          jacobi_cluster_smem_bytes(s) <= jacobi_cluster_dyn_limit() &&

@@ -39,17 +39,18 @@ __global__ void k_reduce_chunks(const double *__restrict__ part, int chunks, int
 namespace {
 
 constexpr size_t kScratchDoubles = GCGE_NOALLOC_SCRATCH_BYTES / sizeof(double);
-constexpr int kMaxDevices = 64;
+constexpr int kMaxDevices = gcge::kMaxDevices;
 constexpr int kTile = 32;
 
 static __device__ __align__(256) double g_noalloc_scratch[kScratchDoubles];
 
 std::mutex g_mu;
 double *g_scratch_ptr[kMaxDevices] = {};
+int g_sms[kMaxDevices] = {};
 
-// Device address of the scratch array for the current device (set up once per
-// device, on its first call).
-int scratch_for_current_device(double **out) {
+// Device address of the scratch array and the SM count of the current device
+// (both set up once per device, on its first call).
+int scratch_for_current_device(double **out, int *sms) {
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) {
@@ -68,9 +69,17 @@ int scratch_for_current_device(double **out) {
             gcge::set_error(GCGE_ERR_CUDA, "GCGE_GramNoAlloc: cudaGetSymbolAddress failed");
             return GCGE_ERR_CUDA;
         }
+        int count = 0;
+        e = cudaDeviceGetAttribute(&count, cudaDevAttrMultiProcessorCount, dev);
+        if (e != cudaSuccess || count <= 0) {
+            gcge::set_error(GCGE_ERR_CUDA, "GCGE_GramNoAlloc: SM count query failed");
+            return GCGE_ERR_CUDA;
+        }
+        g_sms[dev] = count;
         g_scratch_ptr[dev] = p;
     }
     *out = g_scratch_ptr[dev];
+    *sms = g_sms[dev];
     return GCGE_OK;
 }
 
@@ -89,7 +98,8 @@ extern "C" int GCGE_GramNoAlloc(int n, int m, int w, const double *Q, int ldq, c
         return GCGE_ERR_TOO_LARGE;
     }
     double *scratch = nullptr;
-    int st = scratch_for_current_device(&scratch);
+    int sms = 0;
+    int st = scratch_for_current_device(&scratch, &sms);
     if (st != GCGE_OK) return st;
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     if (n == 0) {
@@ -100,9 +110,6 @@ extern "C" int GCGE_GramNoAlloc(int n, int m, int w, const double *Q, int ldq, c
         }
         return GCGE_OK;
     }
-    int dev = 0, sms = 148;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     const int tiles = ((m + kTile - 1) / kTile) * ((w + kTile - 1) / kTile);
     long long chunks = std::max(1, (3 * sms + tiles - 1) / tiles);
     chunks = std::min<long long>(chunks, std::max(1, (n + 127) / 128));

@@ -465,11 +465,12 @@ int oz_num_sms() { return device_sms(); }
 
 template <int BN, bool GRAM>
 void launch_oz(const OzArgs &a, dim3 grid, cudaStream_t st) {
-    static std::once_flag once;
+    static PerDevice<bool> smem_set;
     const int smem = (int)sizeof(OzSmem<BN>);
-    std::call_once(once, [smem] {
+    smem_set.get([smem] {
         GCGE_CUDA(cudaFuncSetAttribute(k_oz_gemm<BN, GRAM>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+        return true;
     });
     k_oz_gemm<BN, GRAM><<<grid, oz_threads<BN>(), smem, st>>>(a);
     GCGE_CHECK_LAUNCH();

@@ -149,7 +149,8 @@ __device__ __forceinline__ unsigned long long global_ns() {
 // cross-block reductions are done once.  Returns false when the wait ran out
 // (or another block's did); the caller then returns.
 template <typename F>
-__device__ __forceinline__ bool grid_sync(PcgSync *gs, int *error, unsigned long long epoch,
+__device__ __forceinline__ bool grid_sync(PcgSync *gs, int *error, unsigned long long timeout_ns,
+                                          long long max_polls, unsigned long long epoch,
                                           F &&last) {
     __shared__ int s_last, s_ok;
     __syncthreads();
@@ -173,8 +174,8 @@ __device__ __forceinline__ bool grid_sync(PcgSync *gs, int *error, unsigned long
         const unsigned long long t0 = global_ns();
         for (long long poll = 0; ld_acquire(&gs->release) < epoch; ++poll) {
             if ((poll & 31) == 31 &&
-                (*(volatile int *)error != 0 || poll > kBarrierMaxPolls ||
-                 global_ns() - t0 > kBarrierTimeoutNs)) {
+                (*(volatile int *)error != 0 || poll > max_polls ||
+                 global_ns() - t0 > timeout_ns)) {
                 atomicExch(error, 1);
                 s_ok = 0;
                 break;
@@ -192,7 +193,8 @@ __device__ __forceinline__ bool grid_sync(PcgSync *gs, int *error, unsigned long
 // the same order, so the copies agree).  No wait can run out: the barrier is
 // the hardware's.
 template <bool CL, typename F>
-__device__ __forceinline__ bool pcg_sync(PcgSync *gs, int *error, unsigned long long epoch,
+__device__ __forceinline__ bool pcg_sync(PcgSync *gs, int *error, unsigned long long timeout_ns,
+                                         long long max_polls, unsigned long long epoch,
                                          F &&last) {
     if constexpr (CL) {
         cooperative_groups::this_cluster().sync();
@@ -200,7 +202,7 @@ __device__ __forceinline__ bool pcg_sync(PcgSync *gs, int *error, unsigned long 
         __syncthreads();
         return true;
     } else {
-        return grid_sync(gs, error, epoch, last);
+        return grid_sync(gs, error, timeout_ns, max_polls, epoch, last);
     }
 }
 
@@ -219,6 +221,12 @@ struct PcgArgs {
     PcgSync *sync;
     PcgStats *stats;
     double *part;  // 2 x gridDim.x x KP
+    // bound of every grid-barrier wait (device clock and poll count)
+    unsigned long long timeout_ns;
+    long long max_polls;
+    // failure-detection test only: the grid's last block returns before its
+    // first barrier, so the others' waits run out (never set otherwise)
+    int withhold_last;
 };
 
 // Compiler-only ordering point between the 16-byte groups of a row in the
@@ -373,6 +381,7 @@ k_block_pcg(PcgArgs<T> a) {
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int k = a.k, n = a.n;
     const double vb = (double)sizeof(T);
+    if (!CL && a.withhold_last && gridDim.x > 1 && blockIdx.x == gridDim.x - 1) return;
 
     // per-warp accumulators: clear, and flush (fixed-order sum over warps)
     auto wred_zero = [&]() {
@@ -506,7 +515,7 @@ k_block_pcg(PcgArgs<T> a) {
         wred_flush(part2);
     }
     // initial residual norms (src/ops_lin_sol.c:171-233)
-    if (!pcg_sync<CL>(gs, error, ++epoch, [&]() {
+    if (!pcg_sync<CL>(gs, error, a.timeout_ns, a.max_polls, ++epoch, [&]() {
             grid_cols_sum<KP, kPcgThreads>(part_base(epoch), sum1, stripe);
             if (a.rel_tol)
                 grid_cols_sum<KP, kPcgThreads>(part_base(epoch) + (size_t)gridDim.x * KP, sum2,
@@ -573,7 +582,7 @@ k_block_pcg(PcgArgs<T> a) {
             }
         }
         wred_zero();
-        if (!pcg_sync<CL>(gs, error, ++epoch, [&]() {
+        if (!pcg_sync<CL>(gs, error, a.timeout_ns, a.max_polls, ++epoch, [&]() {
                 if (tid == 0 && stats_block) a.sync->t_spmm = global_ns();
             })) {
             finish(false);
@@ -621,7 +630,7 @@ k_block_pcg(PcgArgs<T> a) {
             wred_flush(part_base(epoch + 1) + (size_t)blockIdx.x * KP);
         }
         // alpha = rho / p^T w (src/ops_lin_sol.c:300-330)
-        if (!pcg_sync<CL>(gs, error, ++epoch, [&]() {
+        if (!pcg_sync<CL>(gs, error, a.timeout_ns, a.max_polls, ++epoch, [&]() {
                 grid_cols_sum<KP, kPcgThreads>(part_base(epoch), sum1, stripe);
                 if (tid < k) {
                     const int c = tid;
@@ -681,7 +690,7 @@ k_block_pcg(PcgArgs<T> a) {
             wred_flush(part_base(epoch + 1) + (size_t)blockIdx.x * KP);
         }
         // convergence test of src/ops_lin_sol.c:383-394 and beta for the next step
-        if (!pcg_sync<CL>(gs, error, ++epoch, [&]() {
+        if (!pcg_sync<CL>(gs, error, a.timeout_ns, a.max_polls, ++epoch, [&]() {
                 grid_cols_sum<KP, kPcgThreads>(part_base(epoch), sum1, stripe);
                 if (tid < k && sc->active[tid]) {
                     const int c = tid;
@@ -716,9 +725,9 @@ constexpr int kMaxBlocksPerSm = 4;
 // a cluster of this kernel, else 8), or 0 when neither can run.
 template <typename T, int KP>
 int pcg_cluster_size() {
-    static std::once_flag once;
-    static int csize = 0;
-    std::call_once(once, [] {
+    static PerDevice<int> cache;
+    return cache.get([] {
+        int csize = 0;
         for (int c : {16, 8}) {
             if (c > 8 && cudaFuncSetAttribute(k_block_pcg<T, KP, true>,
                                               cudaFuncAttributeNonPortableClusterSizeAllowed,
@@ -747,8 +756,8 @@ int pcg_cluster_size() {
                 break;
             }
         }
+        return csize;
     });
-    return csize;
 }
 
 template <typename T, int KP>
@@ -777,13 +786,12 @@ void launch_block_pcg(PcgArgs<T> a, cudaStream_t st) {
         count_launch();
         return;
     }
-    static std::once_flag once;
-    static int bpsm = 0;
-    std::call_once(once, [] {
+    static PerDevice<int> occupancy;
+    const int bpsm = occupancy.get([] {
         int b = 0;
         GCGE_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_block_pcg<T, KP, false>,
                                                                 pcg_threads<T, KP>(), 0));
-        bpsm = std::min(b, kMaxBlocksPerSm);
+        return std::min(b, kMaxBlocksPerSm);
     });
     GCGE_REQUIRE(bpsm >= 1, GCGE_ERR_CUDA, "block PCG: kernel does not fit on an SM");
     int nb = std::max(1, std::min(bpsm * num_sms_pcg(), a.nslices));
@@ -880,8 +888,13 @@ void PcgWork::collect(cudaStream_t st) {
     kernel_bytes = h_stats.p->kernel_bytes;
     spmm_bytes = h_stats.p->spmm_bytes;
     total_iters = (long long)h_stats.p->iters;
-    GCGE_REQUIRE(h_stats.p->error == 0, GCGE_ERR_CUDA,
-                 "block PCG: a grid barrier wait timed out");
+    if (h_stats.p->error != 0) {
+        // the launch that timed out has ended; clear the flag so the next
+        // solve on this work area starts clean, then report
+        GCGE_CUDA(cudaMemsetAsync(&stats.p->error, 0, sizeof(int), st));
+        GCGE_CUDA(cudaStreamSynchronize(st));
+        throw CudaError{GCGE_ERR_CUDA, "block PCG: a grid barrier wait timed out"};
+    }
 }
 PcgWork::~PcgWork() {
     for (auto e : ev) cudaEventDestroy(e);
@@ -906,10 +919,15 @@ int pcg_last_iters(PcgWork &wk, cudaStream_t st) {
     GCGE_CUDA(cudaMemcpyAsync(wk.h_stats.p, wk.stats.p, sizeof(PcgStats), cudaMemcpyDeviceToHost,
                               st));
     GCGE_CUDA(cudaStreamSynchronize(st));
-    GCGE_REQUIRE(wk.h_stats.p->error == 0, GCGE_ERR_CUDA,
-                 "block PCG: a grid barrier wait timed out");
+    if (wk.h_stats.p->error != 0) {
+        GCGE_CUDA(cudaMemsetAsync(&wk.stats.p->error, 0, sizeof(int), st));
+        GCGE_CUDA(cudaStreamSynchronize(st));
+        throw CudaError{GCGE_ERR_CUDA, "block PCG: a grid barrier wait timed out"};
+    }
     return wk.h_sc.p->niter;
 }
+
+thread_local PcgBarrierTest t_pcg_barrier_test;
 
 template <typename T>
 void block_pcg_rows(PcgWork &wk, const SellPattern &pat, const T *sval, const T *Bv, T *X, T *R,
@@ -941,6 +959,13 @@ void block_pcg_rows(PcgWork &wk, const SellPattern &pat, const T *sval, const T 
     a.sync = wk.sync.p;
     a.stats = wk.stats.p;
     a.part = wk.part.p;
+    a.timeout_ns = kBarrierTimeoutNs;
+    a.max_polls = kBarrierMaxPolls;
+    a.withhold_last = 0;
+    if (t_pcg_barrier_test.active) {
+        a.timeout_ns = t_pcg_barrier_test.timeout_ns;
+        a.withhold_last = t_pcg_barrier_test.withhold_last;
+    }
     GCGE_CUDA(cudaMemsetAsync(wk.sync.p, 0, sizeof(PcgSync), st));
     const bool timed = wk.ev_used + 2 <= 65536;
     if (timed) {
