@@ -45,6 +45,7 @@ EXPORTED_SYMBOLS = [
     "GCGE_ServerSubmit", "GCGE_ServerWait", "GCGE_ServerDestroy", "GCGE_SolveBatch",
     "MultiVecOrthSetup_ModifiedGramSchmidt", "MultiVecOrthSetup_BinaryGramSchmidt",
     "EigenSolverSetParametersFromCommandLine_GCG", "CUDA_MatAxpby",
+    "MultiLinearSolverSetup_BlockPCG", "GCGE_TestBlockPCGBarrierTimeout",
 ]
 
 _lib = None

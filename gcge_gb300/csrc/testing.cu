@@ -81,6 +81,20 @@ int GCGE_BlockPCG(void *A, void *B, double sigma, void **b, void **x, int k, int
     }
 }
 
+int GCGE_TestBlockPCGBarrierTimeout(void *A, void **b, void **x, int k, double timeout_ms) {
+    if (!(timeout_ms > 0.0)) return GCGE_ERR_ARG;
+    struct Hook {
+        explicit Hook(double ms) {
+            t_pcg_barrier_test.active = true;
+            t_pcg_barrier_test.timeout_ns = (unsigned long long)(ms * 1e6);
+            t_pcg_barrier_test.withhold_last = 1;
+        }
+        ~Hook() { t_pcg_barrier_test = PcgBarrierTest{}; }
+    } hook(timeout_ms);
+    int it = 0;
+    return GCGE_BlockPCG(A, nullptr, 0.0, b, x, k, 30, 1e-2, 1e-14, 0, &it);
+}
+
 int GCGE_BOrth(void *B, void **x, int start, int *end, double zero_tol, int max_reorth) {
     try {
         SparseMat *Bm = B ? as_mat(B) : nullptr;

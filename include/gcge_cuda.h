@@ -208,6 +208,14 @@ int GCGE_DenseEig(int s, const double *M, int ldm, double *eval, double *Z, int 
  * precision path. */
 int GCGE_BlockPCG(void *A, void *B, double sigma, void **b, void **x, int k, int max_iter,
                   double rate, double tol, int fp32, int *iters);
+/* Failure-detection test of the persistent block-PCG kernel's grid barrier:
+ * GCGE_BlockPCG (FP64, sigma 0, 30 steps) with every barrier wait bounded by
+ * timeout_ms and the grid's last block leaving before its first barrier, so
+ * the other blocks' waits run out.  Expected result: GCGE_ERR_CUDA, with the
+ * device context intact (the next solve succeeds).  Needs an operator large
+ * enough for the grid form (FP64: more slices than a 16-CTA cluster has
+ * warps, n > 4096 or so).  No counterpart in the reference. */
+int GCGE_TestBlockPCGBarrierTimeout(void *A, void **b, void **x, int k, double timeout_ms);
 /* B-orthonormalise columns [start, *end) of x against [0, start) (B NULL =
  * identity), as MultiVecOrth does (src/ops_orth.c:203-394); *end shrinks by
  * the number of dependent columns dropped. */

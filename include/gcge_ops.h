@@ -127,6 +127,20 @@ typedef struct GCGSolver_ {
     double compRR_tol;
 } GCGSolver;
 
+/* src/ops_lin_sol.h:29-40: the block-PCG parameters that
+ * MultiLinearSolverSetup_BlockPCG stores; ops->multi_linear_solver_workspace
+ * points at one, whose niter / residual the solve fills in. */
+typedef struct BlockPCGSolver_ {
+    int max_iter; double rate; double tol; char tol_type[8];
+    void **mv_ws[3];  /* r p w */
+    double *dbl_ws;
+    int *int_ws;
+    void *pc;
+    void (*MatDotMultiVec)(void **x, void **y, int *start, int *end, void **z, int s,
+                           struct OPS_ *ops);
+    int niter; double residual;
+} BlockPCGSolver;
+
 /* OPS lifetime: src/ops.c:26-149.  OPS_Setup fills Printf/GetWtime/
  * GetOptionFromCommandLine defaults; the GPU GCG needs no lapack_ops. */
 void OPS_Create(OPS **ops);
@@ -150,6 +164,29 @@ void MultiVecOrthSetup_ModifiedGramSchmidt(int block_size, int max_reorth, doubl
                                            void **mv_ws, double *dbl_ws, struct OPS_ *ops);
 void MultiVecOrthSetup_BinaryGramSchmidt(int block_size, int max_reorth, double orth_zero_tol,
                                          void **mv_ws, double *dbl_ws, struct OPS_ *ops);
+
+/* Linear-solver setup: src/ops_lin_sol.h:41-45, src/ops_lin_sol.c:439-465.
+ * Installs the GPU block conjugate gradient (src/ops_lin_sol.c:140-437) as
+ * ops->MultiLinearSolver(mat, b, x, start, end, ops), solving mat x = b for
+ * columns [start[0], end[0]) of b into [start[1], end[1]) of x (x holds the
+ * initial guess) with the reference's per-column stopping rule: stop when the
+ * residual norm is <= rate x the initial one or <= tol x norm_b (norm_b = 1
+ * for "abs", ||b_i|| for "rel", |dbl_ws[i]| for "user"), or after max_iter
+ * steps.  With MatDotMultiVec NULL and an "abs"/"rel" tolerance the solve is
+ * one persistent kernel launch per 40 columns on the CUDA matrix `mat`; with
+ * an operator callback (e.g. the shifted product of GCG's ComputeW) or
+ * "user" norms, the reference's loop runs step for step on the device
+ * multivectors, calling the callback on the same column ranges with the same
+ * workspace arguments; mv_ws[0..2] (r, p, w: CUDA multivectors at least as
+ * wide as the block) are then required.  pc and int_ws are stored and unused,
+ * as in the reference.  Each ops keeps its own setting (the reference keeps
+ * one static setting per process).  Failures go to ops_cuda_last_error(). */
+void MultiLinearSolverSetup_BlockPCG(int max_iter, double rate, double tol, const char *tol_type,
+                                     void **mv_ws[3], double *dbl_ws, int *int_ws, void *pc,
+                                     void (*MatDotMultiVec)(void **x, void **y, int *start,
+                                                            int *end, void **z, int s,
+                                                            struct OPS_ *ops),
+                                     struct OPS_ *ops);
 
 /* GCG entry points: src/ops_eig_sol_gcg.c:1565-1628 (Setup), :1684-1741
  * (SetParameters), :1865-1877 (GCGE_Create), :1878-1918 (GCGE_Setparameters),

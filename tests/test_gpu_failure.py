@@ -1,6 +1,10 @@
 """Failure reporting without faulting the GPU: bad inputs and non-convergence
 come back as status codes; a poisoned (NaN) matrix is detected on the host
-from the residual norms and the solve stops with GCGE_ERR_NUMERIC."""
+from the residual norms and the solve stops with GCGE_ERR_NUMERIC; a grid
+barrier of the persistent block-PCG kernel whose wait runs out returns an
+error status and leaves the device usable."""
+import ctypes
+
 import numpy as np
 import pytest
 
@@ -46,3 +50,32 @@ def test_library_recovers_after_errors(gpu_lib):
         gpu_lib.solve(A, None, 8, 4, 30, 20)
     r = gpu_lib.solve(A, None, 8, 4, 12, 20, X0=X0)
     assert r.status == gpu_lib.GCGE_OK and r.nconv >= 8
+
+
+def test_block_pcg_barrier_timeout_returns_status_and_device_stays_usable(gpu_lib):
+    """One block of the persistent kernel leaves before its first grid
+    barrier, so the others' bounded waits (100 ms here) run out: the call
+    returns GCGE_ERR_CUDA; then the same solve without the fault, and a whole
+    GCG solve, succeed."""
+    G = gpu_lib
+    A = P.laplace2d(200, 200)            # 1250 slices: the grid form in FP64
+    rng = np.random.default_rng(3)
+    b = rng.standard_normal((A.n, 8))
+    ops = G.CudaOps()
+    try:
+        hA = ops.mat(A)
+        hb = ops.multivec(hA, 8, b)
+        hx = ops.multivec(hA, 8)
+        st = ops.lib.GCGE_TestBlockPCGBarrierTimeout(hA, hb, hx, ctypes.c_int(8),
+                                                     ctypes.c_double(100.0))
+        assert st == G.GCGE_ERR_CUDA
+        it = ctypes.c_int()
+        st = ops.lib.GCGE_BlockPCG(hA, None, ctypes.c_double(0.0), hb, hx, ctypes.c_int(8),
+                                   ctypes.c_int(30), ctypes.c_double(1e-2),
+                                   ctypes.c_double(1e-14), ctypes.c_int(0), ctypes.byref(it))
+        assert st == G.GCGE_OK and it.value > 0
+    finally:
+        ops.close()
+    X0 = P.initial_block(576, 12, seed=1)
+    r = G.solve(P.laplace2d(24, 24), None, 8, 4, 12, 20, X0=X0)
+    assert r.status == G.GCGE_OK and r.nconv >= 8
