@@ -138,11 +138,20 @@ enum { PH_CHECK = 0, PH_P, PH_RR, PH_RRW, PH_EIG, PH_RV, PH_W, PH_LINSOL, PH_X, 
 
 // Products over the long (vector-length) dimension: FP64 FMA kernels in the
 // FP64 solve, FP64-accurate digit products on the tensor cores in the mixed
-// solve (same results to FP64 accuracy).
+// solve (same results to FP64 accuracy).  The digit products' error bound is
+// relative to the largest |x| |y| of each 64-row chunk: FP64-level for the
+// n-row blocks, but not for the coefficient vectors of the projected space
+// (ComputeP's orthogonalisation and its P^T A P, contractions over s rows),
+// whose entries mix O(1) and ~1e-8 values in one chunk.  Products over fewer
+// than kDigitMinRows rows - every projected-space product, since s stays
+// below it for nev up to ~300 - therefore stay FP64; they cost next to
+// nothing.
+constexpr int kDigitMinRows = 1024;
+
 static void dgram(const SolverCtx &c, int n, int m, int w, const double *Q, int ldq,
                   const double *P, int ldp, double *C, int ldc, double *scratch, size_t elems,
                   cudaStream_t st) {
-    if (c.precision == GCGE_PREC_MIXED && !c.escalated)
+    if (c.precision == GCGE_PREC_MIXED && !c.escalated && n >= kDigitMinRows)
         oz_gram(n, m, w, Q, ldq, P, ldp, C, ldc, scratch, elems, st);
     else
         gram(n, m, w, Q, ldq, P, ldp, C, ldc, scratch, elems, st);
@@ -150,7 +159,7 @@ static void dgram(const SolverCtx &c, int n, int m, int w, const double *Q, int 
 static void dlincomb(const SolverCtx &c, int n, int k, int m, const double *X, int ldx,
                      const double *C, int ldc, double *Y, int ldy, const double *beta, int incb,
                      cudaStream_t st, double alpha = 1.0) {
-    if (c.precision == GCGE_PREC_MIXED && !c.escalated)
+    if (c.precision == GCGE_PREC_MIXED && !c.escalated && n >= kDigitMinRows)
         oz_lincomb(n, k, m, X, ldx, C, ldc, Y, ldy, beta, incb, st, alpha, c.ozb.p, c.ozb.n);
     else
         lincomb(n, k, m, X, ldx, C, ldc, Y, ldy, beta, incb, st, alpha);
