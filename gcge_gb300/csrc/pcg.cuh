@@ -66,8 +66,20 @@ template <typename T>
 void block_pcg_rows(PcgWork &wk, const SellPattern &pat, const T *sval, const T *B, T *X, T *R,
                     T *P, T *W, int kp, int k, int max_iter, double rate, double tol, bool rel_tol,
                     bool x_zero, cudaStream_t st);
-// Iterations of the last solve (synchronises the stream).
+// Iterations of the last solve (synchronises the stream).  A barrier wait
+// that ran out in that solve throws GCGE_ERR_CUDA (and is cleared, so the
+// work area's next solve starts clean).
 int pcg_last_iters(PcgWork &wk, cudaStream_t st);
+
+// Failure-detection test of the grid barrier (this thread's launches only):
+// a short wait bound, and the grid's last block leaving before its first
+// barrier so that the others' waits run out.  Inactive by default.
+struct PcgBarrierTest {
+    bool active = false;
+    unsigned long long timeout_ns = 0;
+    int withhold_last = 0;
+};
+extern thread_local PcgBarrierTest t_pcg_barrier_test;
 
 // Elements of a slice-blocked n x kp block (rows padded to a multiple of 32).
 inline size_t pcg_block_elems(int n, int kp) { return (size_t)((n + 31) / 32) * 32 * kp; }

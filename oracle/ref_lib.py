@@ -13,6 +13,19 @@ import time
 import numpy as np
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
+
+
+def reference_dir():
+    """The reference source tree (GCGE_REFERENCE_DIR, else the recipe's
+    default in oracle/ref/Makefile), or None where it is absent."""
+    d = os.environ.get("GCGE_REFERENCE_DIR")
+    if d is None:
+        with open(os.path.join(_HERE, "ref", "Makefile")) as f:
+            for line in f:
+                if line.startswith("GCGE_REFERENCE_DIR"):
+                    d = line.split("=", 1)[1].strip()
+                    break
+    return d if d and os.path.isdir(os.path.join(d, "src")) else None
 LIB_PATH = os.path.join(_HERE, "_ref", "libgcge_ref.so")
 _lib = None
 

@@ -28,6 +28,12 @@ def golden_vectors():
 
 
 @pytest.fixture(scope="session")
+def golden_vectors_large():
+    """Leading eigenvectors (FP32) of the fixtures at the benchmarked sizes."""
+    return dict(np.load(os.path.join(GOLDEN_DIR, "golden_vectors_large.npz")))
+
+
+@pytest.fixture(scope="session")
 def golden_orth():
     with open(os.path.join(GOLDEN_DIR, "golden_orth.json")) as f:
         meta = json.load(f)
@@ -89,5 +95,34 @@ def cluster_subspace_angle(evals, V1, V2, B=None, rel_gap=1e-6):
         C = V1[:, i:j].T @ BV2[:, i:j]
         s = np.linalg.svd(C, compute_uv=False)
         worst = max(worst, float(np.arccos(np.clip(s.min(), -1.0, 1.0))))
+        i = j
+    return worst
+
+
+def cluster_subspace_sine(evals, V1, V2, B=None, rel_gap=1e-6):
+    """Largest sine of the principal angles between span(V1) and span(V2) over
+    clusters of nearly equal eigenvalues, in the B inner product.  V1 is
+    B-orthonormal; each cluster block of V2 is B-orthonormalised first (V2 may
+    be stored in FP32), and the sine is the norm of the part of that block
+    outside span(V1) - stable for small angles, where arccos of a cosine near 1
+    is not."""
+    k = V1.shape[1]
+    V2 = np.asarray(V2, dtype=np.float64)
+    worst = 0.0
+    i = 0
+    while i < k:
+        j = i + 1
+        while j < k and abs(evals[j] - evals[j - 1]) <= rel_gap * abs(evals[j]):
+            j += 1
+        Q = V2[:, i:j]
+        BQ = Q if B is None else B @ Q
+        L = np.linalg.cholesky(Q.T @ BQ)
+        Q = np.linalg.solve(L, Q.T).T
+        BQ = np.linalg.solve(L, BQ.T).T
+        V = V1[:, i:j]
+        R = Q - V @ (V.T @ BQ)
+        BR = R if B is None else B @ R
+        s = float(np.sqrt(max(0.0, np.linalg.eigvalsh(R.T @ BR).max())))
+        worst = max(worst, s)
         i = j
     return worst

@@ -3,7 +3,10 @@
 Runs the reference's own C sources (compiled by oracle/ref/Makefile into
 oracle/_ref/libgcge_ref.so) on seeded problems from gcge_gb300.problems and
 stores eigenvalues, converged counts and iteration counts (golden.json) plus
-the leading eigenvectors of the small cases (golden_vectors.npz).
+the leading eigenvectors of the small cases (golden_vectors.npz, FP64) and of
+the cases at the benchmarked sizes (golden_vectors_large.npz: the leading
+columns up to a cluster boundary, stored in FP32, which resolves subspace
+angles far below the 1e-6 rad the tests ask for).
 
     make -C oracle/ref && OPENBLAS_NUM_THREADS=1 python tests/golden/make_golden.py
     OPENBLAS_NUM_THREADS=1 python tests/golden/make_golden.py vardiff3d_12_nev200   # one case
@@ -29,7 +32,10 @@ from oracle import ref_lib  # noqa: E402
 
 
 def cases():
-    """name -> (builder, nev, bs, nev_init, nev_max, options, keep_vectors)."""
+    """name -> (builder, nev, bs, nev_init, nev_max, options, keep_vectors).
+
+    keep_vectors: True stores all nev eigenvectors in FP64; an integer m stores
+    the leading columns (at most m, ending at a cluster boundary) in FP32."""
     rule = P.gcge_block_rule
     out = {}
     out["laplace2d_24x24_nev8"] = (lambda: (P.laplace2d(24, 24), None), 8, 4, 12, 20, {}, True)
@@ -58,19 +64,40 @@ def cases():
     bs, ni, nm = rule(12)
     out["rgg_2000_deg10"] = (lambda: (P.rgg_laplacian(2000, 10.0, seed=5), None), 12, bs, ni, nm, {},
                              True)
+    # the benchmarked workloads at full size (64^3 stiffness + Kronecker mass,
+    # nev 100) and reduced (32^3), and the 128^3 variable-coefficient operator's
+    # generator with the nev-200 block rule at 32^3
+    bs, ni, nm = rule(100)
+    out["laplace3d_mass_32"] = (lambda: (P.laplace3d(32), P.mass3d(32)), 100, bs, ni, nm, {}, 40)
+    out["laplace3d_mass_64"] = (lambda: (P.laplace3d(64), P.mass3d(64)), 100, bs, ni, nm, {},
+                                False)
+    bs, ni, nm = rule(200)
+    out["vardiff3d_32_nev200"] = (lambda: P.vardiff3d(32, seed=3), 200, bs, ni, nm, {}, 48)
     return out
+
+
+def leading_cluster_cut(ev, m, rel_gap=1e-6):
+    """The largest j <= m such that eigenvalues j-1 and j are not in one cluster."""
+    j = m
+    while j > 1 and abs(ev[j] - ev[j - 1]) <= rel_gap * abs(ev[j]):
+        j -= 1
+    return j
 
 
 def main(only=None):
     """All cases, or only the named ones (merged into the existing fixtures)."""
     if not ref_lib.available():
         raise SystemExit("oracle/_ref/libgcge_ref.so missing: run make -C oracle/ref")
-    out, vecs = {}, {}
+    out, vecs, large = {}, {}, {}
     if only:
         with open(os.path.join(HERE, "golden.json")) as f:
             out = json.load(f)
         with np.load(os.path.join(HERE, "golden_vectors.npz")) as z:
             vecs = {k: z[k] for k in z.files}
+    large_path = os.path.join(HERE, "golden_vectors_large.npz")
+    if os.path.exists(large_path):
+        with np.load(large_path) as z:
+            large = {k: z[k] for k in z.files}
     for name, (builder, nev, bs, ni, nm, opt, keep) in cases().items():
         if only and name not in only:
             continue
@@ -86,11 +113,15 @@ def main(only=None):
                          block_size=bs, nev_init=ni, nev_max=nm, tol=list(tol), auto_shift=shift,
                          gap_min=1e-5, max_iter=500, x0_seed=1, nconv=nc, niter=it,
                          eval=[float(v) for v in ev], ref_seconds=sec)
-        if keep:
+        if keep is True:
             vecs[name] = evec[:, :nev].copy()
-    with open(os.path.join(HERE, "golden.json"), "w") as f:
-        json.dump(out, f, indent=1)
-    np.savez_compressed(os.path.join(HERE, "golden_vectors.npz"), **vecs)
+        elif keep:
+            m = leading_cluster_cut(ev, int(keep))
+            large[name] = evec[:, :m].astype(np.float32)
+        with open(os.path.join(HERE, "golden.json"), "w") as f:
+            json.dump(out, f, indent=1)
+        np.savez_compressed(os.path.join(HERE, "golden_vectors.npz"), **vecs)
+        np.savez_compressed(large_path, **large)
 
 
 if __name__ == "__main__":

@@ -2,12 +2,12 @@
 (n = 262144 rows, the 64^3 generalized problem: nev_max + 2 bs = 200 basis
 columns, blocks of bs = 20).
 
-    python -m gcge_gb300.profile_cases gram      # Q^T P, Q n x 180, P n x 20
-    python -m gcge_gb300.profile_cases lincomb   # X C, X n x 180, C 180 x 20
-    python -m gcge_gb300.profile_cases both
-    python -m gcge_gb300.profile_cases pcg       # FP32 block PCG, 20 columns, 30 steps
-    python -m gcge_gb300.profile_cases eig       # dense eigensolver, s = 200
-    python -m gcge_gb300.profile_cases pcgsmall  # FP32 block PCG, 2D n = 4160 (cluster form)
+    python tests/profile_cases.py gram      # Q^T P, Q n x 180, P n x 20
+    python tests/profile_cases.py lincomb   # X C, X n x 180, C 180 x 20
+    python tests/profile_cases.py both
+    python tests/profile_cases.py pcg       # FP32 block PCG, 20 columns, 30 steps
+    python tests/profile_cases.py eig       # dense eigensolver, s = 200
+    python tests/profile_cases.py pcgsmall  # FP32 block PCG, 2D n = 4160 (cluster form)
 
 Each case runs the FP64-accurate digit-plane product once after one warm-up
 call, through the same C-ABI entry points the parity tests use
@@ -31,11 +31,13 @@ k_jacobi32_cluster.
 """
 from __future__ import annotations
 
+import os
 import sys
 
 import numpy as np
 
-import gcge_gb300 as G
+sys.path.insert(0, os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+import gcge_gb300 as G  # noqa: E402
 
 N, M, W = 262144, 180, 20
 

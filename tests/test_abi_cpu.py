@@ -122,11 +122,13 @@ def _probe(tmp_path, header, incs):
 def test_layout_matches_reference_headers(tmp_path):
     ours = _probe(tmp_path, '"gcge_ops.h"', [INC])
     assert int(ours[0]) == 46 * 8 and int(ours[3]) == 45 * 8
-    ref_src = "/root/reference/src"
-    if not os.path.isdir(ref_src):
-        pytest.skip("reference headers not mounted here")
+    from oracle.ref_lib import reference_dir
+    ref_dir = reference_dir()
+    if ref_dir is None:
+        pytest.skip("reference headers not present here")
     ref = _probe(tmp_path, '"ops_eig_sol_gcg.h"',
-                 [os.path.join(ROOT, "oracle", "ref"), ref_src, "/root/reference/app"])
+                 [os.path.join(ROOT, "oracle", "ref"), os.path.join(ref_dir, "src"),
+                  os.path.join(ref_dir, "app")])
     assert ours == ref
 
 
