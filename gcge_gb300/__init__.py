@@ -46,6 +46,7 @@ EXPORTED_SYMBOLS = [
     "MultiVecOrthSetup_ModifiedGramSchmidt", "MultiVecOrthSetup_BinaryGramSchmidt",
     "EigenSolverSetParametersFromCommandLine_GCG", "CUDA_MatAxpby",
     "MultiLinearSolverSetup_BlockPCG", "GCGE_TestBlockPCGBarrierTimeout",
+    "GCGE_BenchDenseProduct",
 ]
 
 _lib = None
@@ -658,6 +659,20 @@ def block_pcg(A, B, sigma, b, x0, max_iter=30, rate=1e-2, tol=1e-14, fp32=False)
         return ops.download(hx, 0, k), it.value
     finally:
         ops.close()
+
+
+def bench_dense_product(kind, n, m, w, emulated=True, reps=5):
+    """Average ms of one long-dimension product on generated device data:
+    kind "gram" (Q^T P, Q n x m, P n x w) or "lincomb" (X C, X n x m, C m x w)."""
+    lib = load()
+    ms = ctypes.c_double()
+    st = lib.GCGE_BenchDenseProduct(ctypes.c_int(0 if kind == "gram" else 1), ctypes.c_int(n),
+                                    ctypes.c_int(m), ctypes.c_int(w),
+                                    ctypes.c_int(1 if emulated else 0), ctypes.c_int(reps),
+                                    ctypes.byref(ms))
+    if st != GCGE_OK:
+        raise GCGEError(st, "GCGE_BenchDenseProduct")
+    return ms.value
 
 
 def dense_gram(Q, P, emulated=False):

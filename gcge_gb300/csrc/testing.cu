@@ -148,6 +148,63 @@ int GCGE_DenseGram(int n, int m, int w, const double *Q, int ldq, const double *
     }
 }
 
+int GCGE_BenchDenseProduct(int kind, int n, int m, int w, int emulated, int reps,
+                           double *ms_per_call) {
+    try {
+        GCGE_REQUIRE((kind == 0 || kind == 1) && n >= 1 && m >= 1 && w >= 1 && reps >= 1 &&
+                         ms_per_call,
+                     GCGE_ERR_ARG, "GCGE_BenchDenseProduct: arguments");
+        cudaStream_t st = lib_stream();
+        const int ld = (n + 31) / 32 * 32;
+        DevBuf<double> dA, dB, dC, scr;
+        DevBuf<unsigned char> ozb;
+        dA.alloc((size_t)ld * m);
+        fill_uniform(n, m, dA.p, ld, 11, st);
+        if (kind == 0) {
+            dB.alloc((size_t)ld * w);
+            fill_uniform(n, w, dB.p, ld, 12, st);
+            dC.alloc((size_t)m * w);
+        } else {
+            dB.alloc((size_t)m * w);
+            fill_uniform(m, w, dB.p, m, 12, st);
+            dC.alloc((size_t)ld * w);
+            fill_uniform(n, w, dC.p, ld, 13, st);
+            ozb.alloc(oz_lincomb_scratch_bytes(m, w));
+        }
+        const size_t elems = std::max<size_t>(gram_scratch_elems(n, m, w), (size_t)1 << 22);
+        scr.alloc(elems);
+        auto call = [&]() {
+            if (kind == 0) {
+                if (emulated) oz_gram(n, m, w, dA.p, ld, dB.p, ld, dC.p, m, scr.p, elems, st);
+                else gram(n, m, w, dA.p, ld, dB.p, ld, dC.p, m, scr.p, elems, st);
+            } else {
+                if (emulated)
+                    oz_lincomb(n, m, w, dA.p, ld, dB.p, m, dC.p, ld, nullptr, 0, st, 1.0, ozb.p,
+                               ozb.n);
+                else lincomb(n, m, w, dA.p, ld, dB.p, m, dC.p, ld, nullptr, 0, st, 1.0);
+            }
+        };
+        call();
+        cudaEvent_t e0, e1;
+        GCGE_CUDA(cudaEventCreate(&e0));
+        GCGE_CUDA(cudaEventCreate(&e1));
+        GCGE_CUDA(cudaEventRecord(e0, st));
+        for (int r = 0; r < reps; ++r) call();
+        GCGE_CUDA(cudaEventRecord(e1, st));
+        GCGE_CUDA(cudaEventSynchronize(e1));
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        *ms_per_call = ms / reps;
+        return GCGE_OK;
+    } catch (const CudaError &e) {
+        set_error(e.status, e.where.c_str());
+        take_error();
+        return e.status;
+    }
+}
+
 int GCGE_DenseLinComb(int n, int k, int m, const double *X, int ldx, const double *Cf, int ldc,
                       double *Y, int ldy, const double *beta, double alpha, int emulated) {
     try {

@@ -191,6 +191,15 @@ void GCGE_PreparedDestroy(gcge_prepared **prep);
 int GCGE_BenchSpMM(void *mat, int k, int fp32, int reps, double *ms_per_launch,
                    double *bytes_per_launch);
 
+/* One long-dimension dense product on device data the call generates
+ * (seeded uniform values), timed with CUDA events on the library stream
+ * after one untimed call: kind 0 = Gram C (m x w) = Q^T P with Q n x m and
+ * P n x w; kind 1 = linear combination Y (n x w) = X C with X n x m and
+ * C m x w; emulated selects the tensor-core digit kernels of the mixed solve
+ * instead of the FP64 ones.  Returns the average ms per call. */
+int GCGE_BenchDenseProduct(int kind, int n, int m, int w, int emulated, int reps,
+                           double *ms_per_call);
+
 /* CUDA-event timer on the library stream: GCGE_TimerStart records the start
  * event; GCGE_TimerStop records the stop event, waits for it and returns the
  * elapsed milliseconds (negative on error). */

@@ -118,9 +118,37 @@ def eig():
     return err < 1e-13 and res < 1e-12
 
 
+# long-dimension product shapes of the mixed solves: (kind, n, m, w)
+PROD_SHAPES = [("gram", 262144, 180, 20), ("lincomb", 262144, 180, 20),
+               ("gram", 2097152, 360, 40), ("lincomb", 2097152, 360, 40),
+               ("gram", 2097152, 400, 40), ("lincomb", 2097152, 400, 320)]
+
+
+def prodbench():
+    """CUDA-event time of each product shape, digit kernels and FP64 kernels,
+    with its algorithmic bytes (8 n (m + w) for a Gram, 8 n (m + 2 w) for a
+    linear combination) over the measured HBM peak."""
+    import json
+    try:
+        with open(os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))),
+                               "MEASURED_PEAKS.json")) as f:
+            peak = float(json.load(f)["hbm_gbs"])
+    except Exception:
+        peak = 6800.0
+    for kind, n, m, w in PROD_SHAPES:
+        emu = G.bench_dense_product(kind, n, m, w, emulated=True, reps=5)
+        f64 = G.bench_dense_product(kind, n, m, w, emulated=False, reps=2)
+        byts = 8.0 * n * (m + w) if kind == "gram" else 8.0 * n * (m + 2 * w)
+        print(f"{kind} n={n} m={m} w={w}: digits {emu:.3f} ms ({byts / emu / 1e6:.0f} GB/s, "
+              f"{byts / emu / 1e6 / peak:.3f} of HBM), fp64 {f64:.3f} ms", flush=True)
+    return True
+
+
 def main(argv):
     what = argv[1] if len(argv) > 1 else "both"
     ok = True
+    if what == "prodbench":
+        ok &= prodbench()
     if what in ("gram", "both"):
         ok &= gram()
     if what in ("lincomb", "both"):
