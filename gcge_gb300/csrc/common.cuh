@@ -249,6 +249,19 @@ void oz_lincomb(int n, int k, int m, const double *X, int ldx, const double *C, 
                 void *scratch, size_t scratch_bytes);
 // Scratch bytes oz_lincomb needs for k terms and m columns.
 size_t oz_lincomb_scratch_bytes(int k, int m);
+// The same products on the 5th-generation tensor cores (ozaki_tc.cu:
+// tcgen05.mma with accumulators in tensor memory), same arguments and
+// results; oz_gram / oz_lincomb use them where tc_digits_available().
+bool tc_digits_available();
+void tc_gram(int n, int m, int w, const double *Q, int ldq, const double *P, int ldp, double *C,
+             int ldc, double *scratch, size_t scratch_elems, cudaStream_t st);
+void tc_lincomb(int n, int k, int m, const double *X, int ldx, const double *C, int ldc,
+                double *Y, int ldy, const double *beta_dev, int incb, cudaStream_t st,
+                double alpha, void *scratch, size_t scratch_bytes);
+size_t tc_lincomb_scratch_bytes(int k, int m);
+// Throws GCGE_ERR_CUDA (and clears the flag) if a tensor-core product's
+// bounded wait ran out since the last check (synchronises the stream).
+void tc_check_error(cudaStream_t st);
 // per-column dots out[c] = X(:,c) . Y(:,c)
 void coldot(int n, int k, const double *X, int ldx, const double *Y, int ldy, double *out,
             double *scratch, size_t scratch_elems, cudaStream_t st);

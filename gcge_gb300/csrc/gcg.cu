@@ -1218,6 +1218,7 @@ void gcg_eigensolver(void *Ah, void *Bh, double *eval, void **evec, int nevGiven
         c->pcg.timing_reset(st);
         const int status = run.run(eval, nevGiven, nevConv);
         c->pcg.collect(st);
+        if (c->precision == GCGE_PREC_MIXED && tc_digits_available()) tc_check_error(st);
         c->info.pcg_spmm_ms = c->pcg.spmm_ms;
         c->info.pcg_spmm_launches = (int)c->pcg.total_iters;
         c->info.pcg_spmm_bytes = c->pcg.spmm_bytes;

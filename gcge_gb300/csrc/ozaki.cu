@@ -521,6 +521,10 @@ void launch_oz_bn(const OzArgs &a, int bn, dim3 grid, cudaStream_t st) {
 void oz_gram(int n, int m, int w, const double *Q, int ldq, const double *P, int ldp, double *C,
              int ldc, double *scratch, size_t scratch_elems, cudaStream_t st) {
     if (m <= 0 || w <= 0) return;
+    if (tc_digits_available()) {
+        tc_gram(n, m, w, Q, ldq, P, ldp, C, ldc, scratch, scratch_elems, st);
+        return;
+    }
     if (n <= 0) {
         GCGE_CUDA(cudaMemset2DAsync(C, sizeof(double) * ldc, 0, sizeof(double) * m, w, st));
         return;
@@ -554,7 +558,9 @@ void oz_gram(int n, int m, int w, const double *Q, int ldq, const double *P, int
 
 // Y (n x m, ldy) = alpha X C + Y diag(beta) for X n x k (ldx), C k x m (ldc);
 // beta == nullptr overwrites Y; incb == 0 broadcasts beta[0].
-size_t oz_lincomb_scratch_bytes(int k, int m) { return bprep_bytes(k, m, oz_tile_n(m)); }
+size_t oz_lincomb_scratch_bytes(int k, int m) {
+    return std::max(bprep_bytes(k, m, oz_tile_n(m)), tc_lincomb_scratch_bytes(k, m));
+}
 
 void oz_lincomb(int n, int k, int m, const double *X, int ldx, const double *C, int ldc,
                 double *Y, int ldy, const double *beta_dev, int incb, cudaStream_t st,
@@ -562,6 +568,11 @@ void oz_lincomb(int n, int k, int m, const double *X, int ldx, const double *C, 
     if (n <= 0 || m <= 0) return;
     if (k <= 0) {
         lincomb(n, k, m, X, ldx, C, ldc, Y, ldy, beta_dev, incb, st, alpha);
+        return;
+    }
+    if (tc_digits_available()) {
+        tc_lincomb(n, k, m, X, ldx, C, ldc, Y, ldy, beta_dev, incb, st, alpha, scratch,
+                   scratch_bytes);
         return;
     }
     const int bn = oz_tile_n(m);

@@ -138,6 +138,7 @@ int GCGE_DenseGram(int n, int m, int w, const double *Q, int ldq, const double *
             oz_gram(n, m, w, dQ.p, std::max(n, 1), dP.p, std::max(n, 1), dC.p, m, scr.p, elems, st);
         else
             gram(n, m, w, dQ.p, std::max(n, 1), dP.p, std::max(n, 1), dC.p, m, scr.p, elems, st);
+        if (emulated && tc_digits_available()) tc_check_error(st);
         GCGE_CUDA(cudaMemcpyAsync(C, dC.p, sizeof(double) * m * w, cudaMemcpyDeviceToHost, st));
         GCGE_CUDA(cudaStreamSynchronize(st));
         return GCGE_OK;
@@ -196,6 +197,7 @@ int GCGE_BenchDenseProduct(int kind, int n, int m, int w, int emulated, int reps
         cudaEventElapsedTime(&ms, e0, e1);
         cudaEventDestroy(e0);
         cudaEventDestroy(e1);
+        if (emulated && tc_digits_available()) tc_check_error(st);
         *ms_per_call = ms / reps;
         return GCGE_OK;
     } catch (const CudaError &e) {
@@ -235,6 +237,7 @@ int GCGE_DenseLinComb(int n, int k, int m, const double *X, int ldx, const doubl
             ozb.alloc(oz_lincomb_scratch_bytes(k, m));
             oz_lincomb(n, k, m, dX.p, n, dC.p, std::max(k, 1), dY.p, n, bp, 1, st, alpha, ozb.p,
                        ozb.n);
+            if (tc_digits_available()) tc_check_error(st);
         } else
             lincomb(n, k, m, dX.p, n, dC.p, std::max(k, 1), dY.p, n, bp, 1, st, alpha);
         GCGE_CUDA(cudaMemcpy2DAsync(Y, sizeof(double) * ldy, dY.p, sizeof(double) * n,
