@@ -51,6 +51,10 @@ constexpr int kTcProdThreads = kTcProdWarps * 32;
 constexpr int kTcDrainThreads = kTcDrainWarps * 32;
 constexpr uint32_t kTcTmemCols = 512;
 constexpr long long kTcWaitPolls = 1LL << 26;  // bounded mbarrier waits (~seconds)
+// Exponent-field slots: the producers fill super-chunk j + 1's while they
+// write super-chunk j's digits and the drain folds super-chunk j - 1 with its
+// own, so three slots keep the producers from waiting on the drain.
+constexpr int kTcExpSlots = 3;
 
 // Byte layout of one operand tile of R rows in a stage: plane i (digit),
 // k-group g (8 consecutive k), row r: i * plane + g * lbo + (r / 8) * 128 +
@@ -69,10 +73,11 @@ struct TcLayout {
     static constexpr uint32_t stage_bytes = a_bytes + b_bytes;
     static constexpr uint32_t stages_off = 0;
     static constexpr uint32_t acc_off = 2 * stage_bytes;  // double acc[BN][kTcM]
-    static constexpr uint32_t ea_off = acc_off + (uint32_t)BN * kTcM * 8;  // int ea[2][kTcM]
-    static constexpr uint32_t eb_off = ea_off + 2 * kTcM * 4;               // int eb[2][BN]
-    static constexpr uint32_t bar_off = (eb_off + 2 * BN * 4 + 15) / 16 * 16;
-    static constexpr int nbars = 11;  // full[2] empty[2] accf tfree exfull[2] exfree[2] final
+    static constexpr uint32_t ea_off = acc_off + (uint32_t)BN * kTcM * 8;  // int ea[3][kTcM]
+    static constexpr uint32_t eb_off = ea_off + kTcExpSlots * kTcM * 4;     // int eb[3][BN]
+    static constexpr uint32_t bar_off = (eb_off + kTcExpSlots * BN * 4 + 15) / 16 * 16;
+    // full[2] empty[2] accf tfree exfull[3] exfree[3] final
+    static constexpr int nbars = 7 + 2 * kTcExpSlots;
     static constexpr uint32_t misc_off = bar_off + nbars * 8;  // tmem slot, abort flag
     static constexpr uint32_t bytes = misc_off + 16;
 };
@@ -275,11 +280,11 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_tc_digits(TcArgs a) {
     using L = TcLayout<BN>;
     extern __shared__ __align__(1024) uint8_t sm[];
     double *acc = reinterpret_cast<double *>(sm + L::acc_off);  // [BN][kTcM]
-    int *ea = reinterpret_cast<int *>(sm + L::ea_off);           // [2][kTcM]
-    int *eb = reinterpret_cast<int *>(sm + L::eb_off);           // [2][BN]
+    int *ea = reinterpret_cast<int *>(sm + L::ea_off);           // [3][kTcM]
+    int *eb = reinterpret_cast<int *>(sm + L::eb_off);           // [3][BN]
     uint64_t *bars = reinterpret_cast<uint64_t *>(sm + L::bar_off);
     uint64_t *full = bars, *empty = bars + 2, *accf = bars + 4, *tfree = bars + 5;
-    uint64_t *exfull = bars + 6, *exfree = bars + 8, *fin = bars + 10;
+    uint64_t *exfull = bars + 6, *exfree = bars + 6 + kTcExpSlots, *fin = bars + 6 + 2 * kTcExpSlots;
     uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(sm + L::misc_off);
     volatile int *abort_flag = reinterpret_cast<volatile int *>(sm + L::misc_off + 4);
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -289,6 +294,8 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_tc_digits(TcArgs a) {
         for (int s = 0; s < 2; ++s) {
             mbar_init(&full[s], kTcProdThreads);
             mbar_init(&empty[s], 1);
+        }
+        for (int s = 0; s < kTcExpSlots; ++s) {
             mbar_init(&exfull[s], kTcProdThreads);
             mbar_init(&exfree[s], kTcDrainThreads);
         }
@@ -414,8 +421,8 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_tc_digits(TcArgs a) {
                 }
                 if (!ok) break;
                 // fold the super-chunk into the FP64 accumulators
-                const uint32_t b = sc & 1;
-                if (!mbar_wait_warp(&exfull[b], (sc >> 1) & 1, abort_flag, a.error)) {
+                const uint32_t b = sc % kTcExpSlots;
+                if (!mbar_wait_warp(&exfull[b], (sc / kTcExpSlots) & 1, abort_flag, a.error)) {
                     ok = false;
                     break;
                 }
@@ -474,133 +481,226 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_tc_digits(TcArgs a) {
         }
     } else {
         // ------------------------------------------------------------ producers
+        // The super-chunks of this CTA's work items form one sequence j = 0, 1,
+        // ...; while the producers write the digit planes of super-chunk j,
+        // each stage also takes a slice of the exponent pass of super-chunk
+        // j + 1 (its first reads of those data from HBM), so the exponent pass
+        // overlaps the digit work instead of stalling it, and the digit pass
+        // reads data the exponent pass brought into L2.
         const int pw = warp < 4 ? warp - 1 : warp - (4 + kTcDrainWarps) + 3;  // 0..6
         const int p = pw * 32 + lane;                                          // 0..223
-        uint32_t t = 0, sc = 0;
-        bool ok = true;
         auto prod_sync = [] { asm volatile("bar.sync 1, %0;" ::"n"(kTcProdThreads) : "memory"); };
-        for (int it = blockIdx.x; it < a.items && ok; it += gridDim.x) {
-            const TcItem w = tc_item<GRAM>(a, it);
-            for (int sk = w.kb; sk < w.ke && ok; sk += super_k, ++sc) {
-                const int ske = min(w.ke, sk + super_k);
-                const uint32_t b = sc & 1;
-                // every producer wait is followed by a producer barrier and a
-                // check of the abort flag, so that all producer warps leave
-                // together (none is left waiting at a barrier the others skip)
-                if (sc >= 2) mbar_wait_warp(&exfree[b], ((sc - 2) >> 1) & 1, abort_flag, a.error);
+        constexpr int RX = GRAM ? kTcM + BN : kTcM;  // rows of the exponent pass
+        // exponent items [e0, e1) of super-chunk (w, sk, ske) into slot buffers
+        auto exp_items = [&](const TcItem &w, int sk, int ske, int e0, int e1, int *ebuf_a,
+                             int *ebuf_b) {
+            for (int e = e0 + p; e < e1; e += 2 * kTcProdThreads) {
+                int em2[2] = {1, 1};
+                int rr2[2] = {-1, -1};
+                double v[2][8];
+#pragma unroll
+                for (int h = 0; h < 2; ++h) {
+                    const int ee = e + h * kTcProdThreads;
+#pragma unroll
+                    for (int q = 0; q < 8; ++q) v[h][q] = 0.0;
+                    if (ee >= e1) continue;
+                    const int r = ee % RX, g = ee / RX;
+                    const int k = sk + g * 8;
+                    rr2[h] = r;
+                    if (GRAM) {
+                        const bool isb = r >= kTcM;
+                        const int gr = isb ? w.nt * BN + (r - kTcM) : w.mt0 + r;
+                        if (gr >= (isb ? a.N : a.M)) continue;
+                        const double *src =
+                            isb ? a.B + (size_t)gr * a.ldb : a.A + (size_t)gr * a.lda;
+                        if (k + 8 <= ske && (reinterpret_cast<uintptr_t>(src + k) & 15) == 0) {
+                            const double2 *s2 = reinterpret_cast<const double2 *>(src + k);
+#pragma unroll
+                            for (int q = 0; q < 4; ++q) {
+                                const double2 u = __ldg(s2 + q);
+                                v[h][2 * q] = u.x;
+                                v[h][2 * q + 1] = u.y;
+                            }
+                        } else {
+#pragma unroll
+                            for (int q = 0; q < 8; ++q)
+                                if (k + q < ske) v[h][q] = __ldg(src + k + q);
+                        }
+                    } else {
+                        const int gr = w.mt0 + r;
+                        if (gr >= a.M) continue;
+#pragma unroll
+                        for (int q = 0; q < 8; ++q)
+                            if (k + q < ske) v[h][q] = __ldg(a.A + gr + (size_t)(k + q) * a.lda);
+                    }
+                }
+#pragma unroll
+                for (int h = 0; h < 2; ++h) {
+                    if (rr2[h] < 0) continue;
+#pragma unroll
+                    for (int q = 0; q < 8; ++q) em2[h] = max(em2[h], tc_exp_field(v[h][q]));
+                    const int r = rr2[h];
+                    if (GRAM && r >= kTcM) atomicMax(&ebuf_b[r - kTcM], em2[h]);
+                    else atomicMax(&ebuf_a[r], em2[h]);
+                }
+            }
+        };
+        // slot buffers of super-chunk (w, sk): set to 1 (the minimum field),
+        // or, for the right operand of a linear combination, its prepared fields
+        auto exp_init = [&](const TcItem &w, int sk, int *ebuf_a, int *ebuf_b) {
+            for (int r = p; r < kTcM; r += kTcProdThreads) ebuf_a[r] = 1;
+            if (GRAM) {
+                for (int c = p; c < BN; c += kTcProdThreads) ebuf_b[c] = 1;
+            } else {
+                const int sidx = (sk - w.kb) / super_k;
+                for (int c = p; c < BN; c += kTcProdThreads)
+                    ebuf_b[c] = a.bexps[((size_t)w.nt * a.nsup + sidx) * BN + c];
+            }
+        };
+        auto n_exp_items = [&](int sk, int ske) { return RX * ((ske - sk + 7) / 8); };
+
+        uint32_t t = 0, j = 0;
+        bool ok = true;
+        int it = blockIdx.x;
+        TcItem w = tc_item<GRAM>(a, it);
+        int sk = w.kb;
+        // prologue: the exponent pass of the first super-chunk on its own
+        {
+            const int ske = min(w.ke, sk + super_k);
+            exp_init(w, sk, ea, eb);
+            prod_sync();
+            exp_items(w, sk, ske, 0, n_exp_items(sk, ske), ea, eb);
+            prod_sync();
+            mbar_arrive(&exfull[0]);
+        }
+        while (ok) {
+            const int ske = min(w.ke, sk + super_k);
+            const uint32_t b = j % kTcExpSlots;
+            // the next super-chunk of the sequence (same work item, or the
+            // CTA's next one)
+            int it1 = it, sk1 = ske;
+            if (sk1 >= w.ke) {
+                it1 = it + gridDim.x;
+                sk1 = -1;
+            }
+            const bool has_next = it1 < a.items;
+            TcItem w1 = w;
+            if (has_next && sk1 < 0) {
+                w1 = tc_item<GRAM>(a, it1);
+                sk1 = w1.kb;
+            }
+            const int ske1 = has_next ? min(w1.ke, sk1 + super_k) : 0;
+            const uint32_t b1 = (j + 1) % kTcExpSlots;
+            int *ea1 = ea + b1 * kTcM, *eb1 = eb + b1 * BN;
+            // every producer wait is followed by a producer barrier and a check
+            // of the abort flag, so that all producer warps leave together
+            // (none is left waiting at a barrier the others skip)
+            if (has_next && j + 1 >= kTcExpSlots)
+                mbar_wait_warp(&exfree[b1], ((j + 1 - kTcExpSlots) / kTcExpSlots) & 1, abort_flag,
+                               a.error);
+            prod_sync();
+            if (*abort_flag) break;
+            if (has_next) exp_init(w1, sk1, ea1, eb1);
+            const int nst = (ske - sk + kTcStageK - 1) / kTcStageK;
+            const int ne1 = has_next ? n_exp_items(sk1, ske1) : 0;
+            const int per = (ne1 + nst - 1) / nst;
+            const int *ebuf_a = ea + b * kTcM, *ebuf_b = eb + b * BN;
+            for (int st = 0; st < nst; ++st, ++t) {
+                const int k0 = sk + st * kTcStageK;
+                const uint32_t s = t & 1;
+                mbar_wait_warp(&empty[s], ((t >> 1) & 1) ^ 1, abort_flag, a.error);
                 prod_sync();
                 if (*abort_flag) {
                     ok = false;
                     break;
                 }
-                // exponent fields of the super-chunk: the largest over [sk, ske) of
-                // each row of A and each column of B (at least 1)
-                int *ebuf_a = ea + b * kTcM;
-                int *ebuf_b = eb + b * BN;
-                if (GRAM) {
-                    for (int r = pw; r < kTcM + BN; r += kTcProdWarps) {
-                        const bool isb = r >= kTcM;
-                        const int rr = isb ? r - kTcM : r;
-                        const int gr = isb ? w.nt * BN + rr : w.mt0 + rr;
-                        int em = 1;
-                        if (gr < (isb ? a.N : a.M)) {
-                            const double *src = isb ? a.B + (size_t)gr * a.ldb : a.A + (size_t)gr * a.lda;
-                            for (int k = sk + lane; k < ske; k += 32) em = max(em, tc_exp_field(src[k]));
-                        }
-                        em = (int)__reduce_max_sync(0xffffffffu, (unsigned)em);
-                        if (lane == 0) (isb ? ebuf_b : ebuf_a)[rr] = em;
-                    }
-                } else {
-                    for (int r = p; r < kTcM; r += kTcProdThreads) ebuf_a[r] = 1;
-                    const int sidx = (sk - w.kb) / super_k;
-                    for (int c = p; c < BN; c += kTcProdThreads)
-                        ebuf_b[c] = a.bexps[((size_t)w.nt * a.nsup + sidx) * BN + c];
-                    prod_sync();
-                    const int nseg = (ske - sk + 31) / 32;
-                    for (int item = p; item < kTcM * nseg; item += kTcProdThreads) {
-                        const int r = item % kTcM, seg = item / kTcM;
-                        const int gr = w.mt0 + r;
-                        int em = 1;
-                        if (gr < a.M) {
-                            const int kk = sk + seg * 32, kend = min(ske, kk + 32);
-                            for (int k = kk; k < kend; ++k)
-                                em = max(em, tc_exp_field(a.A[gr + (size_t)k * a.lda]));
-                        }
-                        atomicMax(&ebuf_a[r], em);
-                    }
-                }
-                prod_sync();
-                mbar_arrive(&exfull[b]);
-                // digit planes, one 32-k stage at a time
-                for (int k0 = sk; k0 < ske; k0 += kTcStageK, ++t) {
-                    const uint32_t s = t & 1;
-                    mbar_wait_warp(&empty[s], ((t >> 1) & 1) ^ 1, abort_flag, a.error);
-                    prod_sync();
-                    if (*abort_flag) {
-                        ok = false;
-                        break;
-                    }
-                    uint8_t *abuf = sm + L::stages_off + s * L::stage_bytes;
-                    uint8_t *bbuf = abuf + L::a_bytes;
-                    constexpr int a_items = kTcM * kTcKGroups;
-                    constexpr int b_items = GRAM ? BN * kTcKGroups : 0;
-                    for (int item = p; item < a_items + b_items; item += kTcProdThreads) {
-                        const bool isb = item >= a_items;
-                        const int ii = isb ? item - a_items : item;
+                // a slice of the next super-chunk's exponent pass
+                if (has_next)
+                    exp_items(w1, sk1, ske1, st * per, min(ne1, (st + 1) * per), ea1, eb1);
+                uint8_t *abuf = sm + L::stages_off + s * L::stage_bytes;
+                uint8_t *bbuf = abuf + L::a_bytes;
+                constexpr int a_items = kTcM * kTcKGroups;
+                constexpr int b_items = GRAM ? BN * kTcKGroups : 0;
+                // digit planes of this stage, two items' loads in flight
+                for (int item = p; item < a_items + b_items; item += 2 * kTcProdThreads) {
+                    double v[2][8];
+                    int em[2] = {1, 1};
+#pragma unroll
+                    for (int h = 0; h < 2; ++h) {
+                        const int ii0 = item + h * kTcProdThreads;
+#pragma unroll
+                        for (int q = 0; q < 8; ++q) v[h][q] = 0.0;
+                        if (ii0 >= a_items + b_items) continue;
+                        const bool isb = ii0 >= a_items;
+                        const int ii = isb ? ii0 - a_items : ii0;
                         const int rows = isb ? BN : kTcM;
                         const int r = ii % rows, g = ii / rows;
                         const int k = k0 + g * 8;
-                        double v[8];
-                        int em;
+                        em[h] = isb ? ebuf_b[r] : ebuf_a[r];
                         if (GRAM) {
                             const int gr = isb ? w.nt * BN + r : w.mt0 + r;
-                            em = isb ? ebuf_b[r] : ebuf_a[r];
-                            const bool live = gr < (isb ? a.N : a.M);
+                            if (gr >= (isb ? a.N : a.M)) continue;
                             const double *src =
                                 isb ? a.B + (size_t)gr * a.ldb : a.A + (size_t)gr * a.lda;
-                            if (live && k + 8 <= ske && ((reinterpret_cast<uintptr_t>(src + k) & 15) == 0)) {
+                            if (k + 8 <= ske && (reinterpret_cast<uintptr_t>(src + k) & 15) == 0) {
                                 const double2 *s2 = reinterpret_cast<const double2 *>(src + k);
 #pragma unroll
                                 for (int q = 0; q < 4; ++q) {
                                     const double2 u = __ldg(s2 + q);
-                                    v[2 * q] = u.x;
-                                    v[2 * q + 1] = u.y;
+                                    v[h][2 * q] = u.x;
+                                    v[h][2 * q + 1] = u.y;
                                 }
                             } else {
 #pragma unroll
                                 for (int q = 0; q < 8; ++q)
-                                    v[q] = (live && k + q < ske) ? __ldg(src + k + q) : 0.0;
+                                    if (k + q < ske) v[h][q] = __ldg(src + k + q);
                             }
                         } else {
                             const int gr = w.mt0 + r;
-                            em = ebuf_a[r];
-                            const bool live = gr < a.M;
+                            if (gr >= a.M) continue;
 #pragma unroll
                             for (int q = 0; q < 8; ++q)
-                                v[q] = (live && k + q < ske) ? __ldg(a.A + gr + (size_t)(k + q) * a.lda)
-                                                             : 0.0;
+                                if (k + q < ske)
+                                    v[h][q] = __ldg(a.A + gr + (size_t)(k + q) * a.lda);
                         }
+                    }
+#pragma unroll
+                    for (int h = 0; h < 2; ++h) {
+                        const int ii0 = item + h * kTcProdThreads;
+                        if (ii0 >= a_items + b_items) continue;
+                        const bool isb = ii0 >= a_items;
+                        const int ii = isb ? ii0 - a_items : ii0;
+                        const int rows = isb ? BN : kTcM;
+                        const int r = ii % rows, g = ii / rows;
                         uint4 dg[kTcDigits];
-                        tc_digits8(v, em, dg);
+                        tc_digits8(v[h], em[h], dg);
                         uint8_t *base = (isb ? bbuf : abuf) + (uint32_t)g * tc_lbo(rows) +
                                         (uint32_t)(r >> 3) * 128u + (uint32_t)(r & 7) * 16u;
 #pragma unroll
                         for (int i = 0; i < kTcDigits; ++i)
                             *reinterpret_cast<uint4 *>(base + (uint32_t)i * tc_plane(rows)) = dg[i];
                     }
-                    if (!GRAM) {
-                        // the right operand's prepared planes for this stage
-                        const int sidx = (k0 - w.kb) / kTcStageK;
-                        const uint4 *src = reinterpret_cast<const uint4 *>(
-                            a.bplanes + ((size_t)w.nt * a.nstages + sidx) * L::b_bytes);
-                        uint4 *dst = reinterpret_cast<uint4 *>(bbuf);
-                        for (int i = p; i < (int)(L::b_bytes / 16); i += kTcProdThreads)
-                            dst[i] = __ldg(src + i);
-                    }
-                    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-                    mbar_arrive(&full[s]);
                 }
+                if (!GRAM) {
+                    // the right operand's prepared planes for this stage
+                    const int sidx = (k0 - w.kb) / kTcStageK;
+                    const uint4 *src = reinterpret_cast<const uint4 *>(
+                        a.bplanes + ((size_t)w.nt * a.nstages + sidx) * L::b_bytes);
+                    uint4 *dst = reinterpret_cast<uint4 *>(bbuf);
+                    for (int i = p; i < (int)(L::b_bytes / 16); i += kTcProdThreads)
+                        dst[i] = __ldg(src + i);
+                }
+                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                mbar_arrive(&full[s]);
             }
+            if (!ok || !has_next) break;
+            // the next super-chunk's exponent fields are complete
+            prod_sync();
+            mbar_arrive(&exfull[b1]);
+            it = it1;
+            w = w1;
+            sk = sk1;
+            ++j;
         }
     }
 

@@ -144,11 +144,23 @@ def prodbench():
     return True
 
 
+def tcgram():
+    """One Gram product of the tensor-core digit kernel at n = 524288, 360 x 40
+    (Q 1.5 GB, larger than L2), after one warm-up call: the shape of the 128^3
+    B-orthogonalisation at a quarter of its length, for a profiler capture of
+    k_tc_digits (second launch)."""
+    ms = G.bench_dense_product("gram", 524288, 360, 40, emulated=True, reps=1)
+    print(f"gram n=524288 m=360 w=40: digits {ms:.3f} ms")
+    return True
+
+
 def main(argv):
     what = argv[1] if len(argv) > 1 else "both"
     ok = True
     if what == "prodbench":
         ok &= prodbench()
+    if what == "tcgram":
+        ok &= tcgram()
     if what in ("gram", "both"):
         ok &= gram()
     if what in ("lincomb", "both"):
