@@ -9,7 +9,7 @@
 // every column of the right operand gets an exponent e with |x| < 2^e, |x|
 // becomes the 56-bit fixed-point integer X = |x| 2^(56-e) (truncated), written
 // as 7 digits of 8 bits with x's sign: the leading digit in [0, 256], the
-// others balanced in [-128, 127].  Digits are exact in bf16, the 28 digit
+// others balanced in [-128, 127].  Digits are exact in FP16, the 28 digit
 // pairs with i + j <= 6 are multiplied on the tensor cores and summed into 7
 // level accumulators L_l = sum_{i+j=l} d_i d'_j, which are exact FP32 integers
 // as long as |L_l| < 2^24: 96 consecutive k at most (|L_6| <= 96 (2 * 256 *
@@ -21,7 +21,7 @@
 // Kernel structure (one CTA per SM, persistent over work items):
 //  * warp 0 allocates tensor memory (512 columns: 7 levels x BN) and one of
 //    its threads issues the MMAs (M = 128 rows, N = BN, K = 16 per
-//    instruction, bf16 x bf16 -> f32), committing each stage to an mbarrier;
+//    instruction, f16 x f16 -> f32), committing each stage to an mbarrier;
 //  * 7 producer warps compute exponents and digit planes of the next 32-k
 //    stage into shared memory (two stages, K-major core-matrix layout:
 //    8 rows x 16 bytes per core matrix, padded so stores are conflict-free);
@@ -50,7 +50,9 @@ constexpr int kTcThreads = kTcWarps * 32;  // 640
 constexpr int kTcProdThreads = kTcProdWarps * 32;
 constexpr int kTcDrainThreads = kTcDrainWarps * 32;
 constexpr uint32_t kTcTmemCols = 512;
-constexpr long long kTcWaitPolls = 1LL << 26;  // bounded mbarrier waits (~seconds)
+// bounded mbarrier waits: 4 s of device clock, or this many suspended tests
+constexpr unsigned long long kTcWaitNs = 4000000000ull;
+constexpr long long kTcWaitPolls = 1LL << 22;
 // Exponent-field slots: the producers fill super-chunk j + 1's while they
 // write super-chunk j's digits and the drain folds super-chunk j - 1 with its
 // own, so three slots keep the producers from waiting on the drain.
@@ -127,26 +129,45 @@ __device__ __forceinline__ bool mbar_test(uint64_t *b, uint32_t parity) {
         : "memory");
     return done != 0;
 }
+// The same test, suspending the thread in hardware until the phase completes
+// or about `hint_ns` have passed, so that a waiting warp takes no issue slots
+// from the warps doing the work.
+__device__ __forceinline__ bool mbar_test_suspend(uint64_t *b, uint32_t parity, uint32_t hint_ns) {
+    uint32_t done;
+    asm volatile(
+        "{\n.reg .pred p;\nmbarrier.try_wait.parity.acquire.cta.shared::cta.b64 p, [%1], %2, %3;\n"
+        "selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(done)
+        : "r"(su32(b)), "r"(parity), "r"(hint_ns)
+        : "memory");
+    return done != 0;
+}
+__device__ __forceinline__ unsigned long long tc_global_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
 // Waits for the phase of `parity` to complete; false when the wait ran out
-// or another role gave up (abort flag set).  All lanes of the calling warp
-// must call it together; lane 0 polls and the result is broadcast.
+// (kTcWaitNs on the device clock, or kTcWaitPolls tests) or another role
+// gave up (abort flag set).  All lanes of the calling warp must call it
+// together; lane 0 waits and the result is broadcast.
 __device__ __forceinline__ bool mbar_wait_warp(uint64_t *b, uint32_t parity,
                                                volatile int *abort_flag, int *gerror) {
     int ok = 1;
-    if ((threadIdx.x & 31) == 0) {
+    if ((threadIdx.x & 31) == 0 && !mbar_test(b, parity)) {
+        const unsigned long long t0 = tc_global_ns();
         long long polls = 0;
-        while (!mbar_test(b, parity)) {
-            if ((polls & 63) == 63 && *abort_flag) {
+        while (!mbar_test_suspend(b, parity, 20000u)) {
+            if (*abort_flag) {
                 ok = 0;
                 break;
             }
-            if (++polls > kTcWaitPolls) {
+            if (++polls > kTcWaitPolls || tc_global_ns() - t0 > kTcWaitNs) {
                 *abort_flag = 1;
                 atomicExch(gerror, 1);
                 ok = 0;
                 break;
             }
-            __nanosleep(32);
         }
     }
     ok = __shfl_sync(0xffffffffu, ok, 0);
@@ -163,11 +184,10 @@ __device__ __forceinline__ uint64_t smem_desc(uint32_t addr, uint32_t lbo, uint3
     return (uint64_t)((addr & 0x3FFFFu) >> 4) | ((uint64_t)(lbo >> 4) << 16) |
            ((uint64_t)(sbo >> 4) << 32) | (1ull << 46);
 }
-// kind::f16 instruction descriptor: f32 accumulate, bf16 A and B, both
-// K-major, N >> 3 at bit 17, M >> 4 at bit 24
+// kind::f16 instruction descriptor: f32 accumulate (bit 4), f16 A and B
+// (format 0 at bits 7 and 10), both K-major, N >> 3 at bit 17, M >> 4 at bit 24
 __host__ __device__ constexpr uint32_t tc_idesc(int m, int n) {
-    return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) |
-           ((uint32_t)(m >> 4) << 24);
+    return (1u << 4) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(m >> 4) << 24);
 }
 __device__ __forceinline__ void tc_mma(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc,
                                        uint32_t idesc, uint32_t accumulate) {
@@ -205,43 +225,62 @@ __device__ __forceinline__ int tc_exp_field(double x) {
     return max((int)(((unsigned)__double2hiint(x) >> 20) & 0x7FFu), 1);
 }
 
-// The 7 bf16 digits of 8 values (one row, 8 consecutive k) relative to the
+// X = |x| 2^(1078 - emax) as a 56-bit fixed-point integer (truncated; the
+// caller guarantees emax >= the exponent field of x), plus 0x808080808080,
+// as two words: the 53-bit significand shifted left by 3, then right by
+// emax - field with clamped funnel shifts (no branches).  sgn = x's sign bit.
+__device__ __forceinline__ void tc_fixed56(double x, uint32_t emax, uint32_t &yh, uint32_t &yl,
+                                           uint32_t &sgn) {
+    const uint32_t hi = (uint32_t)__double2hiint(x), lo = (uint32_t)__double2loint(x);
+    const uint32_t ef = (hi >> 20) & 0x7FFu;
+    const uint32_t mhi = (hi & 0xFFFFFu) | (min(ef, 1u) << 20);
+    uint32_t xh = __funnelshift_l(lo, mhi, 3);
+    uint32_t xl = lo << 3;
+    const uint32_t r = emax - max(ef, 1u);
+    const uint32_t r1 = min(r, 32u), r2 = min(r - r1, 32u);
+    xl = __funnelshift_rc(xl, xh, r1);
+    xh = __funnelshift_rc(xh, 0u, r1);
+    xl = __funnelshift_rc(xl, xh, r2);
+    xh = __funnelshift_rc(xh, 0u, r2);
+    asm("add.cc.u32 %0, %2, 0x80808080;\n\taddc.u32 %1, %3, 0x8080;"
+        : "=r"(yl), "=r"(yh)
+        : "r"(xl), "r"(xh));
+    sgn = hi & 0x80000000u;
+}
+
+// (a - b) on two packed FP16 values
+__device__ __forceinline__ uint32_t tc_hsub2(uint32_t a, uint32_t b) {
+    uint32_t d;
+    asm("sub.rn.f16x2 %0, %1, %2;" : "=r"(d) : "r"(a), "r"(b));
+    return d;
+}
+
+// The 7 FP16 digits of 8 values (one row, 8 consecutive k) relative to the
 // exponent field emax: out[i] holds digit i of the 8 values, two per word
-// (lower k in the low half).  With X = |x| 2^(1078 - emax) truncated and
-// Y = X + 0x808080808080, digit 0 is Y >> 48 (in [0, 256]) and digit i >= 1
-// is byte 6 - i of Y less 128 (in [-128, 127]), so that X = sum_i d_i
-// 2^(8 (6 - i)).  The word (sign | 2^23 | field) read as FP32, less
-// (sign | 2^23) for digit 0 and (sign | 2^23 + 128) for the others, is +-d
-// exactly, and its upper 16 bits are its bf16 pattern.
+// (lower k in the low half).  With Y = X + 0x808080808080 (tc_fixed56),
+// digit 0 is Y >> 48 (in [0, 256]) and digit i >= 1 is byte 6 - i of Y less
+// 128 (in [-128, 127]), so that X = sum_i d_i 2^(8 (6 - i)); each carries x's
+// sign.  A digit is formed for two values at once: the FP16 pattern
+// sign | 0x6400 | field is +-(1024 + field) exactly (ulp 1 on [1024, 2048)),
+// and subtracting +-1024 (digit 0) or +-(1024 + 128) leaves +-d exactly.
 __device__ __forceinline__ void tc_digits8(const double (&v)[8], int emax, uint4 (&out)[kTcDigits]) {
     uint32_t w[kTcDigits][4];
 #pragma unroll
     for (int e = 0; e < 8; e += 2) {
-        uint32_t f[2][kTcDigits];
-#pragma unroll
-        for (int h = 0; h < 2; ++h) {
-            const double x = v[e + h];
-            const uint32_t hi = (uint32_t)__double2hiint(x), lo = (uint32_t)__double2loint(x);
-            const int ef = (int)((hi >> 20) & 0x7FFu);
-            const uint32_t mhi = (hi & 0xFFFFFu) | (ef != 0 ? 0x100000u : 0u);
-            const unsigned long long mant = ((unsigned long long)mhi << 32) | lo;
-            const int sh = max(ef, 1) - emax + 3;  // <= 3
-            const unsigned long long X =
-                sh >= 0 ? (mant << sh) : (sh > -64 ? (mant >> (-sh)) : 0ull);
-            const unsigned long long Y = X + 0x0000808080808080ull;
-            const uint32_t yh = (uint32_t)(Y >> 32), yl = (uint32_t)Y;
-            const uint32_t mg = 0x4B000000u | (hi & 0x80000000u);
-            const float off = __uint_as_float(mg | 0x80u);
-            f[h][0] = __float_as_uint(__uint_as_float((yh >> 16) | mg) - __uint_as_float(mg));
-            f[h][1] = __float_as_uint(__uint_as_float(__byte_perm(yh, mg, 0x7651)) - off);
-            f[h][2] = __float_as_uint(__uint_as_float(__byte_perm(yh, mg, 0x7650)) - off);
-            f[h][3] = __float_as_uint(__uint_as_float(__byte_perm(yl, mg, 0x7653)) - off);
-            f[h][4] = __float_as_uint(__uint_as_float(__byte_perm(yl, mg, 0x7652)) - off);
-            f[h][5] = __float_as_uint(__uint_as_float(__byte_perm(yl, mg, 0x7651)) - off);
-            f[h][6] = __float_as_uint(__uint_as_float(__byte_perm(yl, mg, 0x7650)) - off);
-        }
-#pragma unroll
-        for (int i = 0; i < kTcDigits; ++i) w[i][e / 2] = __byte_perm(f[0][i], f[1][i], 0x7632);
+        uint32_t yh0, yl0, s0, yh1, yl1, s1;
+        tc_fixed56(v[e], (uint32_t)emax, yh0, yl0, s0);
+        tc_fixed56(v[e + 1], (uint32_t)emax, yh1, yl1, s1);
+        const uint32_t M = 0x64006400u | (s0 >> 16) | s1;  // +-1024 in each half
+        const uint32_t Mb = M | 0x00800080u;                // +-(1024 + 128)
+        w[0][e / 2] = tc_hsub2((yh0 >> 16) | (yh1 & 0xFFFF0000u) | M, M);
+        // byte 6 - i of Y: bytes 4, 5 in the high word, 0..3 in the low word;
+        // the permutation puts value 0's byte in half 0 and value 1's in half 1
+        w[1][e / 2] = tc_hsub2((__byte_perm(yh0, yh1, 0x0501) & 0x00FF00FFu) | M, Mb);
+        w[2][e / 2] = tc_hsub2((__byte_perm(yh0, yh1, 0x0400) & 0x00FF00FFu) | M, Mb);
+        w[3][e / 2] = tc_hsub2((__byte_perm(yl0, yl1, 0x0703) & 0x00FF00FFu) | M, Mb);
+        w[4][e / 2] = tc_hsub2((__byte_perm(yl0, yl1, 0x0602) & 0x00FF00FFu) | M, Mb);
+        w[5][e / 2] = tc_hsub2((__byte_perm(yl0, yl1, 0x0501) & 0x00FF00FFu) | M, Mb);
+        w[6][e / 2] = tc_hsub2((__byte_perm(yl0, yl1, 0x0400) & 0x00FF00FFu) | M, Mb);
     }
 #pragma unroll
     for (int i = 0; i < kTcDigits; ++i) out[i] = make_uint4(w[i][0], w[i][1], w[i][2], w[i][3]);
