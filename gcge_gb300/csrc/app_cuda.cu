@@ -98,6 +98,7 @@ void SlotStage::release_on(cudaStream_t st) {
     dbeta.release_on(st);
     dres.release_on(st);
     scr.release_on(st);
+    tc_exps.release_on(st);
 }
 
 int current_device() {

@@ -147,6 +147,8 @@ struct PinnedBuf {
 struct SlotStage {
     DevBuf<double> dcoef, dbeta, dres, scr;
     PinnedBuf<double> hstage, hres;
+    // exponent fields of the tensor-core digit products' operands (ozaki_tc.cu)
+    DevBuf<int> tc_exps;
     void release_on(cudaStream_t st);
 };
 SlotStage &slot_stage();

@@ -18,20 +18,34 @@
 // words are converted to FP64 with the super-chunk's scale and added.  Error:
 // below 2^-55 of the super-chunk's largest |x| |y| per product.
 //
-// Kernel structure (one CTA per SM, persistent over work items):
-//  * warp 0 allocates tensor memory (512 columns: 7 levels x BN) and one of
-//    its threads issues the MMAs (M = 128 rows, N = BN, K = 16 per
-//    instruction, f16 x f16 -> f32), committing each stage to an mbarrier;
-//  * 7 producer warps compute exponents and digit planes of the next 32-k
-//    stage into shared memory (two stages, K-major core-matrix layout:
-//    8 rows x 16 bytes per core matrix, padded so stores are conflict-free);
-//  * 12 drain warps read the level accumulators of each 96-k chunk from
-//    tensor memory (warp w reads lanes 32 (w % 4) .. + 31), fold them into
-//    int64 registers, and at each super-chunk end into FP64 accumulators in
-//    shared memory; at the end of a work item they write the result.
+// Data path, per CTA (one per SM, persistent over work items):
+//  * exponent fields come from a streaming pre-pass (k_tc_expcols /
+//    k_tc_exprows: per column of the Gram operands over each 384-row
+//    super-chunk, per row of the linear combination's left operand over each
+//    480-column super-chunk);
+//  * one producer thread issues bulk tensor copies (cp.async.bulk.tensor.2d,
+//    TMA) of the raw FP64 tiles of each 32-k raw stage, two raw stages ahead,
+//    into shared memory (Gram tiles: 16 k x rows boxes with the 128-byte
+//    swizzle, so that a lane per row reads them without bank conflicts);
+//  * 7 producer warps turn each 16-k half of a raw stage into the 7 FP16
+//    digit planes of a digit stage (two digit stages, K-major core-matrix
+//    layout: 8 rows x 16 bytes per core matrix); the right operand of a linear
+//    combination is prepared once per call (k_tc_bprep) and copied into each
+//    digit stage with cp.async.bulk;
+//  * one thread of warp 0 issues the 28 MMAs of each digit stage (M = 128 rows,
+//    N = BN, K = 16, f16 x f16 -> f32 into 7 level accumulators in tensor
+//    memory, 7 x BN of its 512 columns) and commits each stage to an mbarrier;
+//  * 12 drain warps read the levels of each 96-k chunk from tensor memory
+//    (warp w reads lanes 32 (w % 4) .. + 31), fold them into int64 registers,
+//    and at each super-chunk end into FP64 accumulators in shared memory; at
+//    the end of a work item they write the result.
 // Every wait on an mbarrier is bounded; a wait that runs out sets the error
 // word and every role stops at its next wait, so the kernel always returns.
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
 #include <cstdint>
+#include <mutex>
 
 #include "common.cuh"
 
@@ -40,8 +54,9 @@ namespace {
 
 constexpr int kTcDigits = 7;
 constexpr int kTcM = 128;      // output rows per tile (tensor-memory lanes)
-constexpr int kTcStageK = 32;  // k per pipeline stage (two 16-k MMA steps)
-constexpr int kTcDrainStages = 3;
+constexpr int kTcStageK = 16;  // k per digit stage (one MMA step)
+constexpr int kTcRawK = 32;    // k per raw (TMA) stage: two digit stages
+constexpr int kTcDrainStages = 6;
 constexpr int kTcDrainK = kTcStageK * kTcDrainStages;  // 96: exact FP32 level sums
 constexpr int kTcKGroups = kTcStageK / 8;              // core matrices along k per stage
 constexpr int kTcProdWarps = 7, kTcDrainWarps = 12;
@@ -53,58 +68,65 @@ constexpr uint32_t kTcTmemCols = 512;
 // bounded mbarrier waits: 4 s of device clock, or this many suspended tests
 constexpr unsigned long long kTcWaitNs = 4000000000ull;
 constexpr long long kTcWaitPolls = 1LL << 22;
-// Exponent-field slots: the producers fill super-chunk j + 1's while they
-// write super-chunk j's digits and the drain folds super-chunk j - 1 with its
-// own, so three slots keep the producers from waiting on the drain.
+// exponent-field slots: the producers fill super-chunk j + 1's while the
+// drain folds super-chunk j - 1 with its own
 constexpr int kTcExpSlots = 3;
+constexpr int kTcSuperGram = 4 * kTcDrainK;     // 384 rows of the Gram operands
+constexpr int kTcSuperLincomb = 5 * kTcDrainK;  // 480: K up to 480 in one super-chunk
 
-// Byte layout of one operand tile of R rows in a stage: plane i (digit),
-// k-group g (8 consecutive k), row r: i * plane + g * lbo + (r / 8) * 128 +
-// (r % 8) * 16, with lbo = R * 16 + 16 (the pad keeps the producers' 16-byte
-// stores of the 8 k-groups of a row on different banks).
+// Byte layout of one operand tile of R rows in a digit stage: plane i
+// (digit), k-group g (8 consecutive k), row r: i * plane + g * lbo +
+// (r / 8) * 128 + (r % 8) * 16, with lbo = R * 16 + 16 (the pad keeps the
+// producers' 16-byte stores of the k-groups of a row on different banks).
 __host__ __device__ constexpr uint32_t tc_lbo(int rows) { return (uint32_t)rows * 16u + 16u; }
 __host__ __device__ constexpr uint32_t tc_plane(int rows) { return kTcKGroups * tc_lbo(rows); }
 __host__ __device__ constexpr uint32_t tc_tile_bytes(int rows) {
     return kTcDigits * tc_plane(rows);
 }
+__host__ __device__ constexpr uint32_t tc_round(uint32_t x, uint32_t a) { return (x + a - 1) / a * a; }
 
-template <int BN>
+// Shared memory (offsets from a 1024-byte aligned base).  Raw stage of a
+// Gram: A boxes [2][128 rows][16 k] and B boxes [2][BN rows][16 k] of FP64 in
+// the 128-byte swizzle; of a linear combination: A box [32 k][128 rows].
+template <int BN, bool GRAM>
 struct TcLayout {
+    static constexpr uint32_t a_box = GRAM ? 16u * kTcM * 8u : (uint32_t)kTcRawK * kTcM * 8u;
+    static constexpr uint32_t b_box = GRAM ? 16u * BN * 8u : 0u;
+    static constexpr uint32_t raw_bytes = GRAM ? 2 * (a_box + b_box) : a_box;
+    static constexpr uint32_t raw_off = 0;  // [2] raw stages
     static constexpr uint32_t a_bytes = tc_tile_bytes(kTcM);
     static constexpr uint32_t b_bytes = tc_tile_bytes(BN);
     static constexpr uint32_t stage_bytes = a_bytes + b_bytes;
-    static constexpr uint32_t stages_off = 0;
-    static constexpr uint32_t acc_off = 2 * stage_bytes;  // double acc[BN][kTcM]
+    static constexpr uint32_t dig_off = tc_round(raw_off + 2 * raw_bytes, 1024);  // [2] digit stages
+    static constexpr uint32_t acc_off = dig_off + 2 * stage_bytes;  // double acc[BN][kTcM]
     static constexpr uint32_t ea_off = acc_off + (uint32_t)BN * kTcM * 8;  // int ea[3][kTcM]
     static constexpr uint32_t eb_off = ea_off + kTcExpSlots * kTcM * 4;     // int eb[3][BN]
-    static constexpr uint32_t bar_off = (eb_off + kTcExpSlots * BN * 4 + 15) / 16 * 16;
-    // full[2] empty[2] accf tfree exfull[3] exfree[3] final
-    static constexpr int nbars = 7 + 2 * kTcExpSlots;
+    static constexpr uint32_t bar_off = tc_round(eb_off + kTcExpSlots * BN * 4, 16);
+    // full[2] empty[2] rfull[2] accf tfree exfull[3] exfree[3] final
+    static constexpr int nbars = 9 + 2 * kTcExpSlots;
     static constexpr uint32_t misc_off = bar_off + nbars * 8;  // tmem slot, abort flag
     static constexpr uint32_t bytes = misc_off + 16;
+    static constexpr uint32_t alloc_bytes = bytes + 1024;  // room to align the base
 };
 
 struct TcArgs {
     int M, N, K;
-    // gram: A = Q, element (k, r) at A[k + r lda]; B = P, element (k, c) at
-    // B[k + c ldb].  lincomb: A = X, element (r, k) at A[r + k lda]; B = C,
-    // whose digit planes and exponents were prepared by k_tc_bprep.
-    const double *A;
+    const double *A;  // gram: Q (k, r) at A[k + r lda]; lincomb: X (r, k) at A[r + k lda]
     size_t lda;
-    const double *B;
-    size_t ldb;
-    int super_k;    // k per shared exponent (multiple of kTcDrainK)
-    int kchunk;     // gram: k per work item (multiple of super_k)
-    int items;      // work items
+    int super_k;      // k per shared exponent (multiple of kTcDrainK)
+    int kchunk;       // gram: k per work item (multiple of super_k)
+    int items;        // work items
     int mtiles, ntiles;
-    double *out;    // gram: partials [kz][M x N]; lincomb: Y (ldo)
+    double *out;      // gram: partials [kz][M x N]; lincomb: Y (ldo)
     size_t ldo;
     const double *beta;
     int incb;
     double alpha;
-    const uint8_t *bplanes;  // lincomb: [ntile][stage][b_bytes]
-    const int *bexps;        // lincomb: [ntile][super][BN]
-    int nstages, nsup;       // lincomb: stages and super-chunks of K
+    // exponent fields: gram: eA [super][M], eB [super][N]; lincomb: eA
+    // [super][M] (rows of X), eB = the prepared right operand's [ntile][super][BN]
+    const int *eA, *eB;
+    const uint8_t *bplanes;  // lincomb: [ntile][digit stage][b_bytes]
+    int nstages, nsup;       // lincomb: digit stages and super-chunks of K
     int *error;
 };
 
@@ -286,14 +308,43 @@ __device__ __forceinline__ void tc_digits8(const double (&v)[8], int emax, uint4
     for (int i = 0; i < kTcDigits; ++i) out[i] = make_uint4(w[i][0], w[i][1], w[i][2], w[i][3]);
 }
 
+// ---------------------------------------------------------------- bulk copies
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *b, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.release.cta.shared::cta.b64 _, [%0], %1;" ::"r"(
+                     su32(b)),
+                 "r"(bytes)
+                 : "memory");
+}
+// 2D tile of a tensor map into shared memory, completing on an mbarrier
+__device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap *map, int x, int y,
+                                            uint64_t *bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes "
+        "[%0], [%1, {%2, %3}], [%4];" ::"r"(dst),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(su32(bar))
+        : "memory");
+}
+
 // exact int64 -> double for |t| < 2^51
 __device__ __forceinline__ double tc_i64_to_f64(long long t) {
     return __longlong_as_double(t + 0x4338000000000000LL) - 6755399441055744.0;
 }
 
-// ---------------------------------------------------------------- kernel
+// Waits, with a bound of its own and regardless of the abort flag, for a
+// phase that asynchronous work of this CTA still completes (bulk copies or
+// MMAs in flight at teardown).  Lane 0 of the calling warp waits.
+__device__ __forceinline__ void mbar_wait_teardown(uint64_t *b, uint32_t parity) {
+    if ((threadIdx.x & 31) == 0) {
+        const unsigned long long t0 = tc_global_ns();
+        while (!mbar_test_suspend(b, parity, 20000u))
+            if (tc_global_ns() - t0 > 1000000000ull) break;
+    }
+    __syncwarp();
+}
+
+// ---------------------------------------------------------------- work items
 // Work item `it`: gram: (m tile, n tile, k range); lincomb: (m tile = 128
-// rows of X and Y, n tile).  Fills its output tile coordinates and k range.
+// rows of X and Y, n tile).
 struct TcItem {
     int mt0, nt, kb, ke;
 };
@@ -313,17 +364,56 @@ __device__ __forceinline__ TcItem tc_item(const TcArgs &a, int it) {
     }
     return w;
 }
+// A position in this CTA's sequence of raw stages: work item, super-chunk
+// start, raw stage start.
+struct TcCursor {
+    TcItem w;
+    int it, sk, k0;
+    bool valid;
+};
+template <bool GRAM>
+__device__ __forceinline__ void cur_init(const TcArgs &a, TcCursor &c) {
+    c.it = blockIdx.x;
+    c.valid = c.it < a.items;
+    if (c.valid) {
+        c.w = tc_item<GRAM>(a, c.it);
+        c.sk = c.k0 = c.w.kb;
+    }
+}
+template <bool GRAM>
+__device__ __forceinline__ void cur_next(const TcArgs &a, TcCursor &c) {
+    const int ske = min(c.w.ke, c.sk + a.super_k);
+    c.k0 += kTcRawK;
+    if (c.k0 < ske) return;
+    c.sk += a.super_k;
+    if (c.sk < c.w.ke) {
+        c.k0 = c.sk;
+        return;
+    }
+    c.it += gridDim.x;
+    c.valid = c.it < a.items;
+    if (c.valid) {
+        c.w = tc_item<GRAM>(a, c.it);
+        c.sk = c.k0 = c.w.kb;
+    }
+}
 
+// ---------------------------------------------------------------- kernel
 template <int BN, bool GRAM>
-__global__ void __launch_bounds__(kTcThreads, 1) k_tc_digits(TcArgs a) {
-    using L = TcLayout<BN>;
-    extern __shared__ __align__(1024) uint8_t sm[];
+__global__ void __launch_bounds__(kTcThreads, 1)
+    k_tc_digits(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB,
+                TcArgs a) {
+    using L = TcLayout<BN, GRAM>;
+    extern __shared__ __align__(1024) uint8_t sm_raw[];
+    // 1024-byte aligned base (the 128-byte swizzle of the bulk copies needs it)
+    uint8_t *sm = sm_raw + ((1024u - (su32(sm_raw) & 1023u)) & 1023u);
     double *acc = reinterpret_cast<double *>(sm + L::acc_off);  // [BN][kTcM]
     int *ea = reinterpret_cast<int *>(sm + L::ea_off);           // [3][kTcM]
     int *eb = reinterpret_cast<int *>(sm + L::eb_off);           // [3][BN]
     uint64_t *bars = reinterpret_cast<uint64_t *>(sm + L::bar_off);
-    uint64_t *full = bars, *empty = bars + 2, *accf = bars + 4, *tfree = bars + 5;
-    uint64_t *exfull = bars + 6, *exfree = bars + 6 + kTcExpSlots, *fin = bars + 6 + 2 * kTcExpSlots;
+    uint64_t *full = bars, *empty = bars + 2, *rfull = bars + 4, *accf = bars + 6;
+    uint64_t *tfree = bars + 7, *exfull = bars + 8, *exfree = bars + 8 + kTcExpSlots;
+    uint64_t *fin = bars + 8 + 2 * kTcExpSlots;
     uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(sm + L::misc_off);
     volatile int *abort_flag = reinterpret_cast<volatile int *>(sm + L::misc_off + 4);
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -333,6 +423,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_tc_digits(TcArgs a) {
         for (int s = 0; s < 2; ++s) {
             mbar_init(&full[s], kTcProdThreads);
             mbar_init(&empty[s], 1);
+            mbar_init(&rfull[s], 1);
         }
         for (int s = 0; s < kTcExpSlots; ++s) {
             mbar_init(&exfull[s], kTcProdThreads);
@@ -360,7 +451,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_tc_digits(TcArgs a) {
     if (warp == 0) {
         // ------------------------------------------------------------ MMA issuer
         constexpr uint32_t idesc = tc_idesc(kTcM, BN);
-        uint32_t t = 0, d = 0;  // stages and drain chunks issued so far
+        uint32_t t = 0, d = 0;  // digit stages and drain chunks issued so far
         bool ok = true;
         for (int it = blockIdx.x; it < a.items && ok; it += gridDim.x) {
             const TcItem w = tc_item<GRAM>(a, it);
@@ -370,7 +461,6 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_tc_digits(TcArgs a) {
                     break;
                 }
                 tc_fence_after();
-                uint32_t started = 0;  // levels written in this drain chunk
                 const int nst = min(kTcDrainStages, (w.ke - k0 + kTcStageK - 1) / kTcStageK);
                 for (int st = 0; st < nst; ++st, ++t) {
                     const uint32_t s = t & 1;
@@ -380,25 +470,21 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_tc_digits(TcArgs a) {
                     }
                     tc_fence_after();
                     if (lane == 0) {
-                        const uint32_t abase = sbase + L::stages_off + s * L::stage_bytes;
+                        const uint32_t abase = sbase + L::dig_off + s * L::stage_bytes;
                         const uint32_t bbase = abase + L::a_bytes;
 #pragma unroll
-                        for (int ks = 0; ks < kTcStageK / 16; ++ks) {
+                        for (int i = 0; i < kTcDigits; ++i) {
+                            const uint64_t ad =
+                                smem_desc(abase + i * tc_plane(kTcM), tc_lbo(kTcM), 128);
 #pragma unroll
-                            for (int i = 0; i < kTcDigits; ++i) {
-                                const uint64_t ad =
-                                    smem_desc(abase + i * tc_plane(kTcM) + 2 * ks * tc_lbo(kTcM),
-                                              tc_lbo(kTcM), 128);
-#pragma unroll
-                                for (int j = 0; j + i < kTcDigits; ++j) {
-                                    const uint64_t bd =
-                                        smem_desc(bbase + j * tc_plane(BN) + 2 * ks * tc_lbo(BN),
-                                                  tc_lbo(BN), 128);
-                                    const int l = i + j;
-                                    tc_mma(tmem + (uint32_t)(l * BN), ad, bd, idesc,
-                                           (started >> l) & 1u);
-                                    started |= 1u << l;
-                                }
+                            for (int j = 0; j + i < kTcDigits; ++j) {
+                                const uint64_t bd =
+                                    smem_desc(bbase + j * tc_plane(BN), tc_lbo(BN), 128);
+                                const int l = i + j;
+                                // the first product into a level in a drain chunk
+                                // overwrites it (level l first meets i = 0)
+                                tc_mma(tmem + (uint32_t)(l * BN), ad, bd, idesc,
+                                       (st > 0 || i > 0) ? 1u : 0u);
                             }
                         }
                         tc_commit(&empty[s]);
@@ -411,14 +497,14 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_tc_digits(TcArgs a) {
         // all issued MMAs complete before tensor memory is freed
         if (lane == 0) tc_commit(fin);
         __syncwarp();
-        mbar_wait_warp(fin, 0, abort_flag, a.error);
+        mbar_wait_teardown(fin, 0);
     } else if (warp >= 4 && warp < 4 + kTcDrainWarps) {
         // ------------------------------------------------------------ drain
-        const int q = warp & 3;                 // tensor-memory lane quarter
-        const int third = (warp - 4) >> 2;      // column-group share
-        const int row = q * 32 + lane;          // output row within the tile
-        constexpr int NG = BN / 8;              // 8-column groups
-        constexpr int GPT = (NG + 2) / 3;       // groups per drain thread (at most)
+        const int q = warp & 3;             // tensor-memory lane quarter
+        const int third = (warp - 4) >> 2;  // column-group share
+        const int row = q * 32 + lane;      // output row within the tile
+        constexpr int NG = BN / 8;          // 8-column groups
+        constexpr int GPT = (NG + 2) / 3;   // groups per drain thread (at most)
         long long thi[GPT * 8], tlo[GPT * 8];
 #pragma unroll
         for (int c = 0; c < GPT * 8; ++c) thi[c] = tlo[c] = 0;
@@ -438,17 +524,24 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_tc_digits(TcArgs a) {
                     tc_fence_after();
 #pragma unroll
                     for (int l = 0; l < kTcDigits; ++l) {
+                        uint32_t v[GPT][8];
+#pragma unroll
+                        for (int gi = 0; gi < GPT; ++gi) {
+                            const int g = third + 3 * gi;
+                            if (g < NG)
+                                tc_ld8(tmem + ((uint32_t)(q * 32) << 16) +
+                                           (uint32_t)(l * BN + g * 8),
+                                       v[gi]);
+                        }
+                        tc_wait_ld();
 #pragma unroll
                         for (int gi = 0; gi < GPT; ++gi) {
                             const int g = third + 3 * gi;
                             if (g >= NG) break;
-                            uint32_t v[8];
-                            tc_ld8(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(l * BN + g * 8),
-                                   v);
-                            tc_wait_ld();
 #pragma unroll
                             for (int cc = 0; cc < 8; ++cc) {
-                                const long long L = (long long)__float2int_rn(__uint_as_float(v[cc]));
+                                const long long L =
+                                    (long long)__float2int_rn(__uint_as_float(v[gi][cc]));
                                 // hi: levels 0..3 in units of level 3; lo: 4..6 in units of 6
                                 if (l <= 3) thi[gi * 8 + cc] += L << (8 * (3 - l));
                                 else tlo[gi * 8 + cc] += L << (8 * (6 - l));
@@ -520,132 +613,86 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_tc_digits(TcArgs a) {
         }
     } else {
         // ------------------------------------------------------------ producers
-        // The super-chunks of this CTA's work items form one sequence j = 0, 1,
-        // ...; while the producers write the digit planes of super-chunk j,
-        // each stage also takes a slice of the exponent pass of super-chunk
-        // j + 1 (its first reads of those data from HBM), so the exponent pass
-        // overlaps the digit work instead of stalling it, and the digit pass
-        // reads data the exponent pass brought into L2.
         const int pw = warp < 4 ? warp - 1 : warp - (4 + kTcDrainWarps) + 3;  // 0..6
         const int p = pw * 32 + lane;                                          // 0..223
         auto prod_sync = [] { asm volatile("bar.sync 1, %0;" ::"n"(kTcProdThreads) : "memory"); };
-        constexpr int RX = GRAM ? kTcM + BN : kTcM;  // rows of the exponent pass
-        // exponent items [e0, e1) of super-chunk (w, sk, ske) into slot buffers
-        auto exp_items = [&](const TcItem &w, int sk, int ske, int e0, int e1, int *ebuf_a,
-                             int *ebuf_b) {
-            for (int e = e0 + p; e < e1; e += 2 * kTcProdThreads) {
-                int em2[2] = {1, 1};
-                int rr2[2] = {-1, -1};
-                double v[2][8];
-#pragma unroll
-                for (int h = 0; h < 2; ++h) {
-                    const int ee = e + h * kTcProdThreads;
-#pragma unroll
-                    for (int q = 0; q < 8; ++q) v[h][q] = 0.0;
-                    if (ee >= e1) continue;
-                    const int r = ee % RX, g = ee / RX;
-                    const int k = sk + g * 8;
-                    rr2[h] = r;
-                    if (GRAM) {
-                        const bool isb = r >= kTcM;
-                        const int gr = isb ? w.nt * BN + (r - kTcM) : w.mt0 + r;
-                        if (gr >= (isb ? a.N : a.M)) continue;
-                        const double *src =
-                            isb ? a.B + (size_t)gr * a.ldb : a.A + (size_t)gr * a.lda;
-                        if (k + 8 <= ske && (reinterpret_cast<uintptr_t>(src + k) & 15) == 0) {
-                            const double2 *s2 = reinterpret_cast<const double2 *>(src + k);
-#pragma unroll
-                            for (int q = 0; q < 4; ++q) {
-                                const double2 u = __ldg(s2 + q);
-                                v[h][2 * q] = u.x;
-                                v[h][2 * q + 1] = u.y;
-                            }
-                        } else {
-#pragma unroll
-                            for (int q = 0; q < 8; ++q)
-                                if (k + q < ske) v[h][q] = __ldg(src + k + q);
-                        }
-                    } else {
-                        const int gr = w.mt0 + r;
-                        if (gr >= a.M) continue;
-#pragma unroll
-                        for (int q = 0; q < 8; ++q)
-                            if (k + q < ske) v[h][q] = __ldg(a.A + gr + (size_t)(k + q) * a.lda);
-                    }
-                }
-#pragma unroll
-                for (int h = 0; h < 2; ++h) {
-                    if (rr2[h] < 0) continue;
-#pragma unroll
-                    for (int q = 0; q < 8; ++q) em2[h] = max(em2[h], tc_exp_field(v[h][q]));
-                    const int r = rr2[h];
-                    if (GRAM && r >= kTcM) atomicMax(&ebuf_b[r - kTcM], em2[h]);
-                    else atomicMax(&ebuf_a[r], em2[h]);
-                }
-            }
-        };
-        // slot buffers of super-chunk (w, sk): set to 1 (the minimum field),
-        // or, for the right operand of a linear combination, its prepared fields
-        auto exp_init = [&](const TcItem &w, int sk, int *ebuf_a, int *ebuf_b) {
-            for (int r = p; r < kTcM; r += kTcProdThreads) ebuf_a[r] = 1;
+        // bulk tensor copies of raw stage q (cursor c) into raw buffer q % 2
+        auto issue = [&](uint32_t q, const TcCursor &c) {
+            const uint32_t r = q & 1;
+            const uint32_t base = sbase + L::raw_off + r * L::raw_bytes;
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            mbar_expect_tx(&rfull[r], L::raw_bytes);
             if (GRAM) {
-                for (int c = p; c < BN; c += kTcProdThreads) ebuf_b[c] = 1;
+                tma_load_2d(base, &mapA, c.k0, c.w.mt0, &rfull[r]);
+                tma_load_2d(base + L::a_box, &mapA, c.k0 + 16, c.w.mt0, &rfull[r]);
+                tma_load_2d(base + 2 * L::a_box, &mapB, c.k0, c.w.nt * BN, &rfull[r]);
+                tma_load_2d(base + 2 * L::a_box + L::b_box, &mapB, c.k0 + 16, c.w.nt * BN,
+                            &rfull[r]);
             } else {
-                const int sidx = (sk - w.kb) / super_k;
-                for (int c = p; c < BN; c += kTcProdThreads)
-                    ebuf_b[c] = a.bexps[((size_t)w.nt * a.nsup + sidx) * BN + c];
+                tma_load_2d(base, &mapA, c.w.mt0, c.k0, &rfull[r]);
             }
         };
-        auto n_exp_items = [&](int sk, int ske) { return RX * ((ske - sk + 7) / 8); };
+        // exponent fields of super-chunk (w, sk) into slot b
+        auto load_exps = [&](const TcItem &w, int sk, uint32_t b) {
+            const int sidx = (sk - (GRAM ? 0 : w.kb)) / super_k;
+            for (int r = p; r < kTcM; r += kTcProdThreads) {
+                const int gr = w.mt0 + r;
+                ea[b * kTcM + r] = gr < a.M ? a.eA[(size_t)sidx * a.M + gr] : 1;
+            }
+            for (int c = p; c < BN; c += kTcProdThreads) {
+                const int gc = w.nt * BN + c;
+                if (GRAM) eb[b * BN + c] = gc < a.N ? a.eB[(size_t)sidx * a.N + gc] : 1;
+                else eb[b * BN + c] = a.eB[((size_t)w.nt * a.nsup + sidx) * BN + c];
+            }
+        };
 
-        uint32_t t = 0, j = 0;
-        bool ok = true;
-        int it = blockIdx.x;
-        TcItem w = tc_item<GRAM>(a, it);
-        int sk = w.kb;
-        // prologue: the exponent pass of the first super-chunk on its own
-        {
-            const int ske = min(w.ke, sk + super_k);
-            exp_init(w, sk, ea, eb);
-            prod_sync();
-            exp_items(w, sk, ske, 0, n_exp_items(sk, ske), ea, eb);
-            prod_sync();
-            mbar_arrive(&exfull[0]);
+        TcCursor cons, tma;
+        cur_init<GRAM>(a, cons);
+        tma = cons;
+        uint32_t issued = 0;  // raw stages issued
+        if (p == 0) {
+            for (int i = 0; i < 2 && tma.valid; ++i) {
+                issue(issued++, tma);
+                cur_next<GRAM>(a, tma);
+            }
         }
-        while (ok) {
-            const int ske = min(w.ke, sk + super_k);
-            const uint32_t b = j % kTcExpSlots;
-            // the next super-chunk of the sequence (same work item, or the
-            // CTA's next one)
-            int it1 = it, sk1 = ske;
-            if (sk1 >= w.ke) {
-                it1 = it + gridDim.x;
-                sk1 = -1;
+        // the first super-chunk's exponent fields
+        load_exps(cons.w, cons.sk, 0);
+        prod_sync();
+        mbar_arrive(&exfull[0]);
+        uint32_t q = 0, t = 0, j = 0;  // raw stages, digit stages, super-chunks consumed
+        bool ok = true;
+        while (ok && cons.valid) {
+            const int ske = min(cons.w.ke, cons.sk + super_k);
+            if (cons.k0 == cons.sk) {
+                // at a super-chunk start: the next super-chunk's exponent fields
+                TcCursor nx = cons;
+                nx.k0 = ske - kTcRawK;  // the super-chunk's last raw stage
+                if (nx.k0 < nx.sk) nx.k0 = nx.sk;
+                cur_next<GRAM>(a, nx);
+                while (nx.valid && nx.k0 != nx.sk) cur_next<GRAM>(a, nx);
+                if (nx.valid) {
+                    const uint32_t b1 = (j + 1) % kTcExpSlots;
+                    // every producer wait is followed by a producer barrier and a
+                    // check of the abort flag, so that all producer warps leave
+                    // together (none is left waiting at a barrier the others skip)
+                    if (j + 1 >= kTcExpSlots)
+                        mbar_wait_warp(&exfree[b1], ((j + 1 - kTcExpSlots) / kTcExpSlots) & 1,
+                                       abort_flag, a.error);
+                    prod_sync();
+                    if (*abort_flag) break;
+                    load_exps(nx.w, nx.sk, b1);
+                    prod_sync();
+                    mbar_arrive(&exfull[b1]);
+                }
             }
-            const bool has_next = it1 < a.items;
-            TcItem w1 = w;
-            if (has_next && sk1 < 0) {
-                w1 = tc_item<GRAM>(a, it1);
-                sk1 = w1.kb;
-            }
-            const int ske1 = has_next ? min(w1.ke, sk1 + super_k) : 0;
-            const uint32_t b1 = (j + 1) % kTcExpSlots;
-            int *ea1 = ea + b1 * kTcM, *eb1 = eb + b1 * BN;
-            // every producer wait is followed by a producer barrier and a check
-            // of the abort flag, so that all producer warps leave together
-            // (none is left waiting at a barrier the others skip)
-            if (has_next && j + 1 >= kTcExpSlots)
-                mbar_wait_warp(&exfree[b1], ((j + 1 - kTcExpSlots) / kTcExpSlots) & 1, abort_flag,
-                               a.error);
-            prod_sync();
-            if (*abort_flag) break;
-            if (has_next) exp_init(w1, sk1, ea1, eb1);
-            const int nst = (ske - sk + kTcStageK - 1) / kTcStageK;
-            const int ne1 = has_next ? n_exp_items(sk1, ske1) : 0;
-            const int per = (ne1 + nst - 1) / nst;
-            const int *ebuf_a = ea + b * kTcM, *ebuf_b = eb + b * BN;
-            for (int st = 0; st < nst; ++st, ++t) {
-                const int k0 = sk + st * kTcStageK;
+            const uint32_t r = q & 1;
+            mbar_wait_warp(&rfull[r], (q >> 1) & 1, abort_flag, a.error);
+            const uint8_t *raw = sm + L::raw_off + r * L::raw_bytes;
+            const int *ebuf_a = ea + (j % kTcExpSlots) * kTcM;
+            const int *ebuf_b = eb + (j % kTcExpSlots) * BN;
+            const int nd = min(2, (ske - cons.k0 + kTcStageK - 1) / kTcStageK);
+            for (int dd = 0; dd < nd; ++dd, ++t) {
                 const uint32_t s = t & 1;
                 mbar_wait_warp(&empty[s], ((t >> 1) & 1) ^ 1, abort_flag, a.error);
                 prod_sync();
@@ -653,94 +700,78 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_tc_digits(TcArgs a) {
                     ok = false;
                     break;
                 }
-                // a slice of the next super-chunk's exponent pass
-                if (has_next)
-                    exp_items(w1, sk1, ske1, st * per, min(ne1, (st + 1) * per), ea1, eb1);
-                uint8_t *abuf = sm + L::stages_off + s * L::stage_bytes;
+                uint8_t *abuf = sm + L::dig_off + s * L::stage_bytes;
                 uint8_t *bbuf = abuf + L::a_bytes;
-                constexpr int a_items = kTcM * kTcKGroups;
-                constexpr int b_items = GRAM ? BN * kTcKGroups : 0;
-                // digit planes of this stage, two items' loads in flight
-                for (int item = p; item < a_items + b_items; item += 2 * kTcProdThreads) {
-                    double v[2][8];
-                    int em[2] = {1, 1};
-#pragma unroll
-                    for (int h = 0; h < 2; ++h) {
-                        const int ii0 = item + h * kTcProdThreads;
-#pragma unroll
-                        for (int q = 0; q < 8; ++q) v[h][q] = 0.0;
-                        if (ii0 >= a_items + b_items) continue;
-                        const bool isb = ii0 >= a_items;
-                        const int ii = isb ? ii0 - a_items : ii0;
-                        const int rows = isb ? BN : kTcM;
-                        const int r = ii % rows, g = ii / rows;
-                        const int k = k0 + g * 8;
-                        em[h] = isb ? ebuf_b[r] : ebuf_a[r];
-                        if (GRAM) {
-                            const int gr = isb ? w.nt * BN + r : w.mt0 + r;
-                            if (gr >= (isb ? a.N : a.M)) continue;
-                            const double *src =
-                                isb ? a.B + (size_t)gr * a.ldb : a.A + (size_t)gr * a.lda;
-                            if (k + 8 <= ske && (reinterpret_cast<uintptr_t>(src + k) & 15) == 0) {
-                                const double2 *s2 = reinterpret_cast<const double2 *>(src + k);
-#pragma unroll
-                                for (int q = 0; q < 4; ++q) {
-                                    const double2 u = __ldg(s2 + q);
-                                    v[h][2 * q] = u.x;
-                                    v[h][2 * q + 1] = u.y;
-                                }
-                            } else {
-#pragma unroll
-                                for (int q = 0; q < 8; ++q)
-                                    if (k + q < ske) v[h][q] = __ldg(src + k + q);
-                            }
-                        } else {
-                            const int gr = w.mt0 + r;
-                            if (gr >= a.M) continue;
-#pragma unroll
-                            for (int q = 0; q < 8; ++q)
-                                if (k + q < ske)
-                                    v[h][q] = __ldg(a.A + gr + (size_t)(k + q) * a.lda);
-                        }
-                    }
-#pragma unroll
-                    for (int h = 0; h < 2; ++h) {
-                        const int ii0 = item + h * kTcProdThreads;
-                        if (ii0 >= a_items + b_items) continue;
-                        const bool isb = ii0 >= a_items;
-                        const int ii = isb ? ii0 - a_items : ii0;
-                        const int rows = isb ? BN : kTcM;
-                        const int r = ii % rows, g = ii / rows;
-                        uint4 dg[kTcDigits];
-                        tc_digits8(v[h], em[h], dg);
-                        uint8_t *base = (isb ? bbuf : abuf) + (uint32_t)g * tc_lbo(rows) +
-                                        (uint32_t)(r >> 3) * 128u + (uint32_t)(r & 7) * 16u;
-#pragma unroll
-                        for (int i = 0; i < kTcDigits; ++i)
-                            *reinterpret_cast<uint4 *>(base + (uint32_t)i * tc_plane(rows)) = dg[i];
-                    }
-                }
                 if (!GRAM) {
-                    // the right operand's prepared planes for this stage
-                    const int sidx = (k0 - w.kb) / kTcStageK;
+                    // the right operand's prepared planes of this digit stage (from
+                    // L2; the digit stage's full barrier covers them like the
+                    // producers' own stores)
                     const uint4 *src = reinterpret_cast<const uint4 *>(
-                        a.bplanes + ((size_t)w.nt * a.nstages + sidx) * L::b_bytes);
+                        a.bplanes +
+                        ((size_t)cons.w.nt * a.nstages + (cons.k0 - cons.w.kb) / kTcStageK + dd) *
+                            L::b_bytes);
                     uint4 *dst = reinterpret_cast<uint4 *>(bbuf);
                     for (int i = p; i < (int)(L::b_bytes / 16); i += kTcProdThreads)
                         dst[i] = __ldg(src + i);
                 }
+                // digit planes of this 16-k half of the raw stage
+                constexpr int a_items = kTcM * kTcKGroups;
+                constexpr int b_items = GRAM ? BN * kTcKGroups : 0;
+                for (int item = p; item < a_items + b_items; item += kTcProdThreads) {
+                    const bool isb = item >= a_items;
+                    const int ii = isb ? item - a_items : item;
+                    const int rows = isb ? BN : kTcM;
+                    const int rr = ii % rows, g = ii / rows;
+                    double v[8];
+                    if (GRAM) {
+                        // box dd of the operand: rr's 16 k as 8 chunks of 16
+                        // bytes, chunk c stored at chunk c ^ (rr % 8)
+                        const uint8_t *box = raw + (isb ? 2 * L::a_box + dd * L::b_box
+                                                        : dd * L::a_box) +
+                                             (uint32_t)rr * 128u;
+#pragma unroll
+                        for (int qq = 0; qq < 4; ++qq) {
+                            const int c = 4 * g + qq;
+                            const double2 u = *reinterpret_cast<const double2 *>(
+                                box + (uint32_t)((c ^ (rr & 7)) << 4));
+                            v[2 * qq] = u.x;
+                            v[2 * qq + 1] = u.y;
+                        }
+                    } else {
+                        // box [32 k][128 rows]
+                        const double *col = reinterpret_cast<const double *>(raw) +
+                                            (size_t)(dd * kTcStageK + g * 8) * kTcM + rr;
+#pragma unroll
+                        for (int qq = 0; qq < 8; ++qq) v[qq] = col[(size_t)qq * kTcM];
+                    }
+                    uint4 dg[kTcDigits];
+                    tc_digits8(v, isb ? ebuf_b[rr] : ebuf_a[rr], dg);
+                    uint8_t *base = (isb ? bbuf : abuf) + (uint32_t)g * tc_lbo(rows) +
+                                    (uint32_t)(rr >> 3) * 128u + (uint32_t)(rr & 7) * 16u;
+#pragma unroll
+                    for (int i = 0; i < kTcDigits; ++i)
+                        *reinterpret_cast<uint4 *>(base + (uint32_t)i * tc_plane(rows)) = dg[i];
+                }
                 asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
                 mbar_arrive(&full[s]);
             }
-            if (!ok || !has_next) break;
-            // the next super-chunk's exponent fields are complete
+            if (!ok) break;
+            // raw buffer r is read: refill it with raw stage q + 2
             prod_sync();
-            mbar_arrive(&exfull[b1]);
-            it = it1;
-            w = w1;
-            sk = sk1;
-            ++j;
+            if (*abort_flag) break;
+            if (p == 0 && tma.valid) {
+                issue(issued++, tma);
+                cur_next<GRAM>(a, tma);
+            }
+            ++q;
+            const int sk_before = cons.sk, it_before = cons.it;
+            cur_next<GRAM>(a, cons);
+            if (cons.valid && (cons.sk != sk_before || cons.it != it_before)) ++j;
         }
+        // raw stages still in flight (an abort) land before the CTA exits
+        if (pw == 0)
+            for (uint32_t qq = q; qq < issued; ++qq)
+                mbar_wait_teardown(&rfull[qq & 1], (qq >> 1) & 1);
     }
 
     tc_fence_before();
@@ -753,15 +784,65 @@ __global__ void __launch_bounds__(kTcThreads, 1) k_tc_digits(TcArgs a) {
     }
 }
 
+// Exponent fields for the Gram operands: out[s * ncols + c] = the largest
+// exponent field (at least 1) of column c of X (n x ncols, leading dimension
+// ld, 16-byte aligned columns) over rows [s super, (s + 1) super).  One warp
+// per (super-chunk, column), 16-byte loads.
+__global__ void __launch_bounds__(256) k_tc_expcols(const double *__restrict__ X, size_t ld,
+                                                    int n, int ncols, int super, int nsup,
+                                                    int *__restrict__ out) {
+    const int lane = threadIdx.x & 31;
+    const long long nw = (long long)gridDim.x * 8;
+    for (long long wid = (long long)blockIdx.x * 8 + (threadIdx.x >> 5);
+         wid < (long long)nsup * ncols; wid += nw) {
+        const int c = (int)(wid / nsup), s = (int)(wid % nsup);
+        const int r0 = s * super, r1 = min(n, r0 + super);
+        const double *col = X + (size_t)c * ld;
+        int em = 1;
+        for (int r = r0 + 2 * lane; r < r1; r += 64) {
+            if (r + 1 < r1) {
+                const double2 u = __ldg(reinterpret_cast<const double2 *>(col + r));
+                em = max(em, max(tc_exp_field(u.x), tc_exp_field(u.y)));
+            } else {
+                em = max(em, tc_exp_field(__ldg(col + r)));
+            }
+        }
+        em = (int)__reduce_max_sync(0xffffffffu, (unsigned)em);
+        if (lane == 0) out[(size_t)s * ncols + c] = em;
+    }
+}
+
+// Exponent fields for the left operand of a linear combination:
+// out[s * n + r] = the largest exponent field (at least 1) of row r of X
+// (n x K, leading dimension ld) over columns [s super, (s + 1) super).
+__global__ void __launch_bounds__(256) k_tc_exprows(const double *__restrict__ X, size_t ld,
+                                                    int n, int K, int super,
+                                                    int *__restrict__ out) {
+    const int r = blockIdx.x * 256 + threadIdx.x, s = blockIdx.y;
+    if (r >= n) return;
+    const int k0 = s * super, k1 = min(K, k0 + super);
+    int em = 1;
+    int k = k0;
+    for (; k + 8 <= k1; k += 8) {
+        double v[8];
+#pragma unroll
+        for (int q = 0; q < 8; ++q) v[q] = __ldg(X + r + (size_t)(k + q) * ld);
+#pragma unroll
+        for (int q = 0; q < 8; ++q) em = max(em, tc_exp_field(v[q]));
+    }
+    for (; k < k1; ++k) em = max(em, tc_exp_field(__ldg(X + r + (size_t)k * ld)));
+    out[(size_t)s * n + r] = em;
+}
+
 // Right operand of a linear combination (C, K x N, element (k, c) at
 // C[k + c ldc]) prepared once per call: block (super-chunk, n tile) writes the
-// exponent fields of its BN columns and the digit planes of each 32-k stage
-// of the super-chunk in the stage layout of the product kernel.
+// exponent fields of its BN columns and the digit planes of each 16-k digit
+// stage of the super-chunk in the stage layout of the product kernel.
 template <int BN>
 __global__ void __launch_bounds__(256) k_tc_bprep(const double *__restrict__ C, size_t ldc, int N,
                                                   int K, int super_k, uint8_t *__restrict__ planes,
                                                   int *__restrict__ exps, int nstages, int nsup) {
-    using L = TcLayout<BN>;
+    constexpr uint32_t bb = tc_tile_bytes(BN);
     __shared__ int em_s[BN];
     const int sidx = blockIdx.x, nt = blockIdx.y;
     const int sk = sidx * super_k, ske = min(K, sk + super_k);
@@ -779,7 +860,7 @@ __global__ void __launch_bounds__(256) k_tc_bprep(const double *__restrict__ C, 
     }
     __syncthreads();
     for (int k0 = sk; k0 < ske; k0 += kTcStageK) {
-        uint8_t *dst = planes + ((size_t)nt * nstages + k0 / kTcStageK) * L::b_bytes;
+        uint8_t *dst = planes + ((size_t)nt * nstages + k0 / kTcStageK) * bb;
         for (int item = threadIdx.x; item < BN * kTcKGroups; item += 256) {
             const int c = item % BN, g = item / BN;
             const int gc = nt * BN + c, k = k0 + g * 8;
@@ -827,29 +908,29 @@ __global__ void __launch_bounds__(256) k_tc_reduce(const double *__restrict__ pa
 
 int tc_bn(int n) { return n <= 16 ? 16 : (n <= 32 ? 32 : 48); }
 
-constexpr int kTcSuperGram = 4 * kTcDrainK;     // 384
-constexpr int kTcSuperLincomb = 5 * kTcDrainK;  // 480: K up to 480 in one super-chunk
-
 template <int BN, bool GRAM>
-void launch_tc(const TcArgs &a, int grid, cudaStream_t st) {
-    using L = TcLayout<BN>;
+void launch_tc(const CUtensorMap &ma, const CUtensorMap &mb, const TcArgs &a, int grid,
+               cudaStream_t st) {
+    using L = TcLayout<BN, GRAM>;
     static PerDevice<bool> smem_set;
     smem_set.get([] {
         GCGE_CUDA(cudaFuncSetAttribute(k_tc_digits<BN, GRAM>,
-                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L::bytes));
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)L::alloc_bytes));
         return true;
     });
-    k_tc_digits<BN, GRAM><<<grid, kTcThreads, L::bytes, st>>>(a);
+    k_tc_digits<BN, GRAM><<<grid, kTcThreads, L::alloc_bytes, st>>>(ma, mb, a);
     GCGE_CHECK_LAUNCH();
     count_launch();
 }
 
 template <bool GRAM>
-void launch_tc_bn(const TcArgs &a, int bn, int grid, cudaStream_t st) {
+void launch_tc_bn(const CUtensorMap &ma, const CUtensorMap &mb, const TcArgs &a, int bn, int grid,
+                  cudaStream_t st) {
     switch (bn) {
-        case 16: launch_tc<16, GRAM>(a, grid, st); break;
-        case 32: launch_tc<32, GRAM>(a, grid, st); break;
-        default: launch_tc<48, GRAM>(a, grid, st); break;
+        case 16: launch_tc<16, GRAM>(ma, mb, a, grid, st); break;
+        case 32: launch_tc<32, GRAM>(ma, mb, a, grid, st); break;
+        default: launch_tc<48, GRAM>(ma, mb, a, grid, st); break;
     }
 }
 
@@ -863,6 +944,42 @@ int *tc_error_word() {
         GCGE_CUDA(cudaMemset(p, 0, sizeof(int)));
         return p;
     });
+}
+
+// cuTensorMapEncodeTiled from the driver (the library links the static
+// runtime, not the driver library)
+PFN_cuTensorMapEncodeTiled_v12000 tc_encode_fn() {
+    static std::once_flag once;
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    std::call_once(once, [] {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000,
+                                             cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+        else
+            cudaGetLastError();
+    });
+    return fn;
+}
+
+// 2D FP64 tensor map of a column-major block: dim0 (contiguous) x dim1 with
+// row pitch ld doubles, box0 x box1 elements; false where the layout cannot
+// be described (the caller then uses the FP64 kernels).
+bool tc_map(CUtensorMap *map, const double *base, int dim0, int dim1, size_t ld, int box0,
+            int box1, bool swizzle) {
+    PFN_cuTensorMapEncodeTiled_v12000 enc = tc_encode_fn();
+    if (!enc || (reinterpret_cast<uintptr_t>(base) & 15) || (ld * 8) % 16 || dim0 < 1 || dim1 < 1)
+        return false;
+    const cuuint64_t dims[2] = {(cuuint64_t)dim0, (cuuint64_t)dim1};
+    const cuuint64_t strides[1] = {(cuuint64_t)ld * 8};
+    const cuuint32_t box[2] = {(cuuint32_t)box0, (cuuint32_t)box1};
+    const cuuint32_t estr[2] = {1, 1};
+    return enc(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 2, const_cast<double *>(base), dims, strides,
+               box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+               swizzle ? CU_TENSOR_MAP_SWIZZLE_128B : CU_TENSOR_MAP_SWIZZLE_NONE,
+               CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
 size_t tc_bprep_bytes(int k, int m) {
@@ -883,7 +1000,7 @@ bool tc_digits_available() {
         const int dev = current_device();
         cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, dev);
         cudaDeviceGetAttribute(&minor, cudaDevAttrComputeCapabilityMinor, dev);
-        return (major == 10 && minor == 3) ? 1 : 0;
+        return (major == 10 && minor == 3 && tc_encode_fn() != nullptr) ? 1 : 0;
     }) != 0;
 }
 
@@ -900,7 +1017,9 @@ void tc_check_error(cudaStream_t st) {
 }
 
 // C (m x w, ldc) = Q^T P for Q n x m (ldq), P n x w (ldp): split-k partials
-// in scratch (scratch_elems doubles), then a fixed-order sum.
+// in scratch (scratch_elems doubles), then a fixed-order sum.  Operands that a
+// tensor map cannot describe (an odd leading dimension, a base not 16-byte
+// aligned) go through the FP64 kernel.
 void tc_gram(int n, int m, int w, const double *Q, int ldq, const double *P, int ldp, double *C,
              int ldc, double *scratch, size_t scratch_elems, cudaStream_t st) {
     if (m <= 0 || w <= 0) return;
@@ -909,19 +1028,35 @@ void tc_gram(int n, int m, int w, const double *Q, int ldq, const double *P, int
         return;
     }
     const int bn = tc_bn(w);
+    CUtensorMap ma, mb;
+    if (!tc_map(&ma, Q, n, m, (size_t)ldq, 16, kTcM, true) ||
+        !tc_map(&mb, P, n, w, (size_t)ldp, 16, bn, true)) {
+        gram(n, m, w, Q, ldq, P, ldp, C, ldc, scratch, scratch_elems, st);
+        return;
+    }
     TcArgs a{};
     a.M = m;
     a.N = w;
     a.K = n;
     a.A = Q;
     a.lda = (size_t)ldq;
-    a.B = P;
-    a.ldb = (size_t)ldp;
     a.super_k = kTcSuperGram;
     a.mtiles = (m + kTcM - 1) / kTcM;
     a.ntiles = (w + bn - 1) / bn;
     const int mn = a.mtiles * a.ntiles;
     const int sms = device_sms();
+    // exponent fields of both operands per 384-row super-chunk
+    const int nsup = (n + kTcSuperGram - 1) / kTcSuperGram;
+    DevBuf<int> &eb = slot_stage().tc_exps;
+    eb.alloc((size_t)nsup * (m + w));
+    int *eA = eb.p, *eB = eb.p + (size_t)nsup * m;
+    const int gx = std::min<long long>(4 * sms, ((long long)nsup * std::max(m, w) + 7) / 8);
+    k_tc_expcols<<<gx, 256, 0, st>>>(Q, (size_t)ldq, n, m, kTcSuperGram, nsup, eA);
+    k_tc_expcols<<<gx, 256, 0, st>>>(P, (size_t)ldp, n, w, kTcSuperGram, nsup, eB);
+    GCGE_CHECK_LAUNCH();
+    count_launch(2);
+    a.eA = eA;
+    a.eB = eB;
     // one wave of one CTA per SM over all work items
     int z = std::max(1, sms / mn);
     long long kc = ((long long)(n + z - 1) / z + kTcSuperGram - 1) / kTcSuperGram * kTcSuperGram;
@@ -933,7 +1068,7 @@ void tc_gram(int n, int m, int w, const double *Q, int ldq, const double *P, int
     a.items = z * mn;
     a.out = scratch;
     a.error = tc_error_word();
-    launch_tc_bn<true>(a, bn, std::min(a.items, sms), st);
+    launch_tc_bn<true>(ma, mb, a, bn, std::min(a.items, sms), st);
     const int tot = m * w;
     k_tc_reduce<<<(tot + 31) / 32, 256, 0, st>>>(scratch, z, m, w, C, ldc);
     GCGE_CHECK_LAUNCH();
@@ -949,6 +1084,11 @@ void tc_lincomb(int n, int k, int m, const double *X, int ldx, const double *C, 
                 void *scratch, size_t scratch_bytes) {
     if (n <= 0 || m <= 0) return;
     const int bn = tc_bn(m);
+    CUtensorMap ma;
+    if (!tc_map(&ma, X, n, k, (size_t)ldx, kTcM, kTcRawK, false)) {
+        lincomb(n, k, m, X, ldx, C, ldc, Y, ldy, beta_dev, incb, st, alpha);
+        return;
+    }
     GCGE_REQUIRE(scratch && scratch_bytes >= tc_bprep_bytes(k, m), GCGE_ERR_ARG,
                  "tc_lincomb: scratch too small");
     TcArgs a{};
@@ -971,19 +1111,25 @@ void tc_lincomb(int n, int k, int m, const double *X, int ldx, const double *C, 
     a.error = tc_error_word();
     uint8_t *planes = static_cast<uint8_t *>(scratch);
     const size_t pbytes = (size_t)a.ntiles * a.nstages * tc_tile_bytes(bn);
-    int *exps = reinterpret_cast<int *>(
+    int *bexps = reinterpret_cast<int *>(
         (reinterpret_cast<uintptr_t>(planes + pbytes) + 255) & ~(uintptr_t)255);
     const dim3 pg(a.nsup, a.ntiles);
     switch (bn) {
-        case 16: k_tc_bprep<16><<<pg, 256, 0, st>>>(C, (size_t)ldc, m, k, kTcSuperLincomb, planes, exps, a.nstages, a.nsup); break;
-        case 32: k_tc_bprep<32><<<pg, 256, 0, st>>>(C, (size_t)ldc, m, k, kTcSuperLincomb, planes, exps, a.nstages, a.nsup); break;
-        default: k_tc_bprep<48><<<pg, 256, 0, st>>>(C, (size_t)ldc, m, k, kTcSuperLincomb, planes, exps, a.nstages, a.nsup); break;
+        case 16: k_tc_bprep<16><<<pg, 256, 0, st>>>(C, (size_t)ldc, m, k, kTcSuperLincomb, planes, bexps, a.nstages, a.nsup); break;
+        case 32: k_tc_bprep<32><<<pg, 256, 0, st>>>(C, (size_t)ldc, m, k, kTcSuperLincomb, planes, bexps, a.nstages, a.nsup); break;
+        default: k_tc_bprep<48><<<pg, 256, 0, st>>>(C, (size_t)ldc, m, k, kTcSuperLincomb, planes, bexps, a.nstages, a.nsup); break;
     }
+    // exponent fields of the rows of X per super-chunk of its columns
+    DevBuf<int> &eb = slot_stage().tc_exps;
+    eb.alloc((size_t)a.nsup * n);
+    k_tc_exprows<<<dim3((n + 255) / 256, a.nsup), 256, 0, st>>>(X, (size_t)ldx, n, k,
+                                                              kTcSuperLincomb, eb.p);
     GCGE_CHECK_LAUNCH();
-    count_launch();
+    count_launch(2);
     a.bplanes = planes;
-    a.bexps = exps;
-    launch_tc_bn<false>(a, bn, std::min(a.items, device_sms()), st);
+    a.eA = eb.p;
+    a.eB = bexps;
+    launch_tc_bn<false>(ma, ma, a, bn, std::min(a.items, device_sms()), st);
 }
 
 }  // namespace gcge
