@@ -87,19 +87,22 @@ __host__ __device__ constexpr uint32_t tc_round(uint32_t x, uint32_t a) { return
 
 // Shared memory (offsets from a 1024-byte aligned base).  Raw stage of a
 // Gram: A boxes [2][128 rows][16 k] and B boxes [2][BN rows][16 k] of FP64 in
-// the 128-byte swizzle; of a linear combination: A box [32 k][128 rows].
+// the 128-byte swizzle; of a linear combination: A box [32 k][128 rows] and
+// the right operand's prepared digit planes of its two digit stages.  A
+// linear combination covers at most one super-chunk per work item (the host
+// splits longer contractions), so only the Gram keeps FP64 accumulators.
 template <int BN, bool GRAM>
 struct TcLayout {
-    static constexpr uint32_t a_box = GRAM ? 16u * kTcM * 8u : (uint32_t)kTcRawK * kTcM * 8u;
-    static constexpr uint32_t b_box = GRAM ? 16u * BN * 8u : 0u;
-    static constexpr uint32_t raw_bytes = GRAM ? 2 * (a_box + b_box) : a_box;
-    static constexpr uint32_t raw_off = 0;  // [2] raw stages
     static constexpr uint32_t a_bytes = tc_tile_bytes(kTcM);
     static constexpr uint32_t b_bytes = tc_tile_bytes(BN);
+    static constexpr uint32_t a_box = GRAM ? 16u * kTcM * 8u : (uint32_t)kTcRawK * kTcM * 8u;
+    static constexpr uint32_t b_box = GRAM ? 16u * BN * 8u : b_bytes;  // lincomb: planes
+    static constexpr uint32_t raw_bytes = tc_round(a_box + 2 * b_box, 1024);
+    static constexpr uint32_t raw_off = 0;  // [2] raw stages
     static constexpr uint32_t stage_bytes = a_bytes + b_bytes;
     static constexpr uint32_t dig_off = tc_round(raw_off + 2 * raw_bytes, 1024);  // [2] digit stages
     static constexpr uint32_t acc_off = dig_off + 2 * stage_bytes;  // double acc[BN][kTcM]
-    static constexpr uint32_t ea_off = acc_off + (uint32_t)BN * kTcM * 8;  // int ea[3][kTcM]
+    static constexpr uint32_t ea_off = acc_off + (GRAM ? (uint32_t)BN * kTcM * 8 : 0u);  // int ea[3][kTcM]
     static constexpr uint32_t eb_off = ea_off + kTcExpSlots * kTcM * 4;     // int eb[3][BN]
     static constexpr uint32_t bar_off = tc_round(eb_off + kTcExpSlots * BN * 4, 16);
     // full[2] empty[2] rfull[2] accf tfree exfull[3] exfree[3] final
@@ -127,6 +130,7 @@ struct TcArgs {
     const int *eA, *eB;
     const uint8_t *bplanes;  // lincomb: [ntile][digit stage][b_bytes]
     int nstages, nsup;       // lincomb: digit stages and super-chunks of K
+    int accumulate;          // lincomb: add to Y (later blocks of a split contraction)
     int *error;
 };
 
@@ -314,6 +318,16 @@ __device__ __forceinline__ void mbar_expect_tx(uint64_t *b, uint32_t bytes) {
                      su32(b)),
                  "r"(bytes)
                  : "memory");
+}
+// contiguous bytes (16-byte aligned, a multiple of 16) into shared memory,
+// completing on an mbarrier
+__device__ __forceinline__ void bulk_load(uint32_t dst, const void *src, uint32_t bytes,
+                                          uint64_t *bar) {
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, "
+        "[%3];" ::"r"(dst),
+        "l"(src), "r"(bytes), "r"(su32(bar))
+        : "memory");
 }
 // 2D tile of a tensor map into shared memory, completing on an mbarrier
 __device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap *map, int x, int y,
@@ -512,8 +526,10 @@ __global__ void __launch_bounds__(kTcThreads, 1)
         bool ok = true;
         for (int it = blockIdx.x; it < a.items && ok; it += gridDim.x) {
             const TcItem w = tc_item<GRAM>(a, it);
-            for (int c = third; c < NG; c += 3)
-                for (int cc = 0; cc < 8; ++cc) acc[(c * 8 + cc) * kTcM + row] = 0.0;
+            const int grow = w.mt0 + row;
+            if (GRAM)
+                for (int c = third; c < NG; c += 3)
+                    for (int cc = 0; cc < 8; ++cc) acc[(c * 8 + cc) * kTcM + row] = 0.0;
             for (int sk = w.kb; sk < w.ke && ok; sk += super_k, ++sc) {
                 const int ske = min(w.ke, sk + super_k);
                 for (int k0 = sk; k0 < ske; k0 += kTcDrainK, ++d) {
@@ -524,24 +540,18 @@ __global__ void __launch_bounds__(kTcThreads, 1)
                     tc_fence_after();
 #pragma unroll
                     for (int l = 0; l < kTcDigits; ++l) {
-                        uint32_t v[GPT][8];
-#pragma unroll
-                        for (int gi = 0; gi < GPT; ++gi) {
-                            const int g = third + 3 * gi;
-                            if (g < NG)
-                                tc_ld8(tmem + ((uint32_t)(q * 32) << 16) +
-                                           (uint32_t)(l * BN + g * 8),
-                                       v[gi]);
-                        }
-                        tc_wait_ld();
 #pragma unroll
                         for (int gi = 0; gi < GPT; ++gi) {
                             const int g = third + 3 * gi;
                             if (g >= NG) break;
+                            uint32_t v[8];
+                            tc_ld8(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(l * BN + g * 8),
+                                   v);
+                            tc_wait_ld();
 #pragma unroll
                             for (int cc = 0; cc < 8; ++cc) {
                                 const long long L =
-                                    (long long)__float2int_rn(__uint_as_float(v[gi][cc]));
+                                    (long long)__float2int_rn(__uint_as_float(v[cc]));
                                 // hi: levels 0..3 in units of level 3; lo: 4..6 in units of 6
                                 if (l <= 3) thi[gi * 8 + cc] += L << (8 * (3 - l));
                                 else tlo[gi * 8 + cc] += L << (8 * (6 - l));
@@ -552,7 +562,8 @@ __global__ void __launch_bounds__(kTcThreads, 1)
                     mbar_arrive(tfree);
                 }
                 if (!ok) break;
-                // fold the super-chunk into the FP64 accumulators
+                // fold the super-chunk: into the FP64 accumulators (Gram), or
+                // straight into Y (a linear combination's single super-chunk)
                 const uint32_t b = sc % kTcExpSlots;
                 if (!mbar_wait_warp(&exfull[b], (sc / kTcExpSlots) & 1, abort_flag, a.error)) {
                     ok = false;
@@ -567,46 +578,51 @@ __global__ void __launch_bounds__(kTcThreads, 1)
                     for (int cc = 0; cc < 8; ++cc) {
                         const int c = g * 8 + cc;
                         const int ec = eb[b * BN + c];
-                        double &A = acc[c * kTcM + row];
-                        if (er == 0x7FF || ec == 0x7FF) {
-                            A = __longlong_as_double(0x7FF8000000000000LL);
+                        // the super-chunk's sum: v 2^(er + ec - 2108), or NaN
+                        const bool nan = er == 0x7FF || ec == 0x7FF;
+                        const int fld = er + ec - 1085;  // exponent field of the scale
+                        const double sc2 = fld <= 0 ? 0.0
+                                           : fld >= 2047
+                                               ? __longlong_as_double(0x7FF0000000000000LL)
+                                               : __longlong_as_double((long long)fld << 52);
+                        const double v = fma(tc_i64_to_f64(thi[gi * 8 + cc]), 16777216.0,
+                                             tc_i64_to_f64(tlo[gi * 8 + cc]));
+                        thi[gi * 8 + cc] = tlo[gi * 8 + cc] = 0;
+                        if (GRAM) {
+                            double &A = acc[c * kTcM + row];
+                            if (nan) A = __longlong_as_double(0x7FF8000000000000LL);
+                            else if (fld > 0) A = fma(v, sc2, A);
                         } else {
-                            const int fld = er + ec - 1085;  // exponent field of the scale
-                            if (fld > 0) {
-                                const double sc2 = fld >= 2047
-                                                       ? __longlong_as_double(0x7FF0000000000000LL)
-                                                       : __longlong_as_double((long long)fld << 52);
-                                const double v = fma(tc_i64_to_f64(thi[gi * 8 + cc]), 16777216.0,
-                                                     tc_i64_to_f64(tlo[gi * 8 + cc]));
-                                A = fma(v, sc2, A);
+                            const double val =
+                                nan ? __longlong_as_double(0x7FF8000000000000LL) : v * sc2;
+                            const int col = w.nt * BN + c;
+                            if (grow < a.M && col < a.N) {
+                                double *dst = a.out + grow + (size_t)col * a.ldo;
+                                double y = a.alpha * val;
+                                if (a.accumulate) {
+                                    y += *dst;
+                                } else if (a.beta != nullptr) {
+                                    const double bb =
+                                        a.beta[a.incb == 0 ? 0 : (size_t)col * a.incb];
+                                    if (bb != 0.0) y = fma(bb, *dst, y);
+                                }
+                                *dst = y;
                             }
                         }
-                        thi[gi * 8 + cc] = tlo[gi * 8 + cc] = 0;
                     }
                 }
                 mbar_arrive(&exfree[b]);
             }
             if (!ok) break;
-            // the work item's result
-            const int grow = w.mt0 + row;
-            if (grow < a.M) {
+            // the work item's result (Gram: split-k partials)
+            if (GRAM && grow < a.M) {
+                const int z = it / (a.mtiles * a.ntiles);
                 for (int g = third; g < NG; g += 3) {
                     for (int cc = 0; cc < 8; ++cc) {
                         const int col = w.nt * BN + g * 8 + cc;
-                        if (col >= a.N) continue;
-                        const double v = acc[(g * 8 + cc) * kTcM + row];
-                        if (GRAM) {
-                            const int z = it / (a.mtiles * a.ntiles);
-                            a.out[(size_t)z * a.M * a.N + grow + (size_t)col * a.M] = v;
-                        } else {
-                            double y = a.alpha * v;
-                            double *dst = a.out + grow + (size_t)col * a.ldo;
-                            if (a.beta != nullptr) {
-                                const double bb = a.beta[a.incb == 0 ? 0 : (size_t)col * a.incb];
-                                if (bb != 0.0) y = fma(bb, *dst, y);
-                            }
-                            *dst = y;
-                        }
+                        if (col < a.N)
+                            a.out[(size_t)z * a.M * a.N + grow + (size_t)col * a.M] =
+                                acc[(g * 8 + cc) * kTcM + row];
                     }
                 }
             }
@@ -621,15 +637,25 @@ __global__ void __launch_bounds__(kTcThreads, 1)
             const uint32_t r = q & 1;
             const uint32_t base = sbase + L::raw_off + r * L::raw_bytes;
             asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-            mbar_expect_tx(&rfull[r], L::raw_bytes);
             if (GRAM) {
+                mbar_expect_tx(&rfull[r], 2 * (L::a_box + L::b_box));
                 tma_load_2d(base, &mapA, c.k0, c.w.mt0, &rfull[r]);
                 tma_load_2d(base + L::a_box, &mapA, c.k0 + 16, c.w.mt0, &rfull[r]);
                 tma_load_2d(base + 2 * L::a_box, &mapB, c.k0, c.w.nt * BN, &rfull[r]);
                 tma_load_2d(base + 2 * L::a_box + L::b_box, &mapB, c.k0 + 16, c.w.nt * BN,
                             &rfull[r]);
             } else {
+                // the A box and the prepared planes of the stage's digit stages
+                const int ske = min(c.w.ke, c.sk + super_k);
+                const int nd = min(2, (ske - c.k0 + kTcStageK - 1) / kTcStageK);
+                mbar_expect_tx(&rfull[r], L::a_box + nd * L::b_box);
                 tma_load_2d(base, &mapA, c.w.mt0, c.k0, &rfull[r]);
+                const uint8_t *src =
+                    a.bplanes +
+                    ((size_t)c.w.nt * a.nstages + (c.k0 - c.w.kb) / kTcStageK) * L::b_bytes;
+                for (int dd = 0; dd < nd; ++dd)
+                    bulk_load(base + L::a_box + dd * L::b_box, src + (size_t)dd * L::b_bytes,
+                              L::b_bytes, &rfull[r]);
             }
         };
         // exponent fields of super-chunk (w, sk) into slot b
@@ -703,54 +729,71 @@ __global__ void __launch_bounds__(kTcThreads, 1)
                 uint8_t *abuf = sm + L::dig_off + s * L::stage_bytes;
                 uint8_t *bbuf = abuf + L::a_bytes;
                 if (!GRAM) {
-                    // the right operand's prepared planes of this digit stage (from
-                    // L2; the digit stage's full barrier covers them like the
-                    // producers' own stores)
-                    const uint4 *src = reinterpret_cast<const uint4 *>(
-                        a.bplanes +
-                        ((size_t)cons.w.nt * a.nstages + (cons.k0 - cons.w.kb) / kTcStageK + dd) *
-                            L::b_bytes);
+                    // the right operand's prepared planes of this digit stage, from
+                    // the raw stage (the digit stage's full barrier covers them like
+                    // the producers' own stores)
+                    const uint4 *src =
+                        reinterpret_cast<const uint4 *>(raw + L::a_box + dd * L::b_box);
                     uint4 *dst = reinterpret_cast<uint4 *>(bbuf);
                     for (int i = p; i < (int)(L::b_bytes / 16); i += kTcProdThreads)
-                        dst[i] = __ldg(src + i);
+                        dst[i] = src[i];
                 }
-                // digit planes of this 16-k half of the raw stage
+                // digit planes of this 16-k half of the raw stage, two items
+                // at a time (independent instruction streams)
                 constexpr int a_items = kTcM * kTcKGroups;
                 constexpr int b_items = GRAM ? BN * kTcKGroups : 0;
-                for (int item = p; item < a_items + b_items; item += kTcProdThreads) {
-                    const bool isb = item >= a_items;
-                    const int ii = isb ? item - a_items : item;
-                    const int rows = isb ? BN : kTcM;
-                    const int rr = ii % rows, g = ii / rows;
-                    double v[8];
-                    if (GRAM) {
-                        // box dd of the operand: rr's 16 k as 8 chunks of 16
-                        // bytes, chunk c stored at chunk c ^ (rr % 8)
-                        const uint8_t *box = raw + (isb ? 2 * L::a_box + dd * L::b_box
-                                                        : dd * L::a_box) +
-                                             (uint32_t)rr * 128u;
+                constexpr int n_items = a_items + b_items;
+                for (int item0 = p; item0 < n_items; item0 += 2 * kTcProdThreads) {
+                    double v[2][8];
+                    int em[2] = {1, 1};
+                    uint8_t *dstb[2] = {nullptr, nullptr};
+                    uint32_t pl[2] = {0, 0};
 #pragma unroll
-                        for (int qq = 0; qq < 4; ++qq) {
-                            const int c = 4 * g + qq;
-                            const double2 u = *reinterpret_cast<const double2 *>(
-                                box + (uint32_t)((c ^ (rr & 7)) << 4));
-                            v[2 * qq] = u.x;
-                            v[2 * qq + 1] = u.y;
+                    for (int h = 0; h < 2; ++h) {
+                        const int item = item0 + h * kTcProdThreads;
+                        const bool live = item < n_items;
+                        const int it2 = live ? item : item0;
+                        const bool isb = it2 >= a_items;
+                        const int ii = isb ? it2 - a_items : it2;
+                        const int rows = isb ? BN : kTcM;
+                        const int rr = ii % rows, g = ii / rows;
+                        if (GRAM) {
+                            // box dd of the operand: rr's 16 k as 8 chunks of 16
+                            // bytes, chunk c stored at chunk c ^ (rr % 8)
+                            const uint8_t *box = raw + (isb ? 2 * L::a_box + dd * L::b_box
+                                                            : dd * L::a_box) +
+                                                 (uint32_t)rr * 128u;
+#pragma unroll
+                            for (int qq = 0; qq < 4; ++qq) {
+                                const int c = 4 * g + qq;
+                                const double2 u = *reinterpret_cast<const double2 *>(
+                                    box + (uint32_t)((c ^ (rr & 7)) << 4));
+                                v[h][2 * qq] = u.x;
+                                v[h][2 * qq + 1] = u.y;
+                            }
+                        } else {
+                            // box [32 k][128 rows]
+                            const double *col = reinterpret_cast<const double *>(raw) +
+                                                (size_t)(dd * kTcStageK + g * 8) * kTcM + rr;
+#pragma unroll
+                            for (int qq = 0; qq < 8; ++qq) v[h][qq] = col[(size_t)qq * kTcM];
                         }
-                    } else {
-                        // box [32 k][128 rows]
-                        const double *col = reinterpret_cast<const double *>(raw) +
-                                            (size_t)(dd * kTcStageK + g * 8) * kTcM + rr;
-#pragma unroll
-                        for (int qq = 0; qq < 8; ++qq) v[qq] = col[(size_t)qq * kTcM];
+                        em[h] = isb ? ebuf_b[rr] : ebuf_a[rr];
+                        if (live) {
+                            dstb[h] = (isb ? bbuf : abuf) + (uint32_t)g * tc_lbo(rows) +
+                                      (uint32_t)(rr >> 3) * 128u + (uint32_t)(rr & 7) * 16u;
+                            pl[h] = tc_plane(rows);
+                        }
                     }
-                    uint4 dg[kTcDigits];
-                    tc_digits8(v, isb ? ebuf_b[rr] : ebuf_a[rr], dg);
-                    uint8_t *base = (isb ? bbuf : abuf) + (uint32_t)g * tc_lbo(rows) +
-                                    (uint32_t)(rr >> 3) * 128u + (uint32_t)(rr & 7) * 16u;
 #pragma unroll
-                    for (int i = 0; i < kTcDigits; ++i)
-                        *reinterpret_cast<uint4 *>(base + (uint32_t)i * tc_plane(rows)) = dg[i];
+                    for (int h = 0; h < 2; ++h) {
+                        if (dstb[h] == nullptr) continue;
+                        uint4 dg[kTcDigits];
+                        tc_digits8(v[h], em[h], dg);
+#pragma unroll
+                        for (int i = 0; i < kTcDigits; ++i)
+                            *reinterpret_cast<uint4 *>(dstb[h] + (uint32_t)i * pl[h]) = dg[i];
+                    }
                 }
                 asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
                 mbar_arrive(&full[s]);
@@ -1075,61 +1118,74 @@ void tc_gram(int n, int m, int w, const double *Q, int ldq, const double *P, int
     count_launch();
 }
 
-size_t tc_lincomb_scratch_bytes(int k, int m) { return tc_bprep_bytes(k, m); }
+size_t tc_lincomb_scratch_bytes(int k, int m) {
+    return tc_bprep_bytes(std::min(k, kTcSuperLincomb), m);
+}
 
 // Y (n x m, ldy) = alpha X C + Y diag(beta) for X n x k (ldx), C k x m (ldc);
-// beta == nullptr overwrites Y; incb == 0 broadcasts beta[0].
+// beta == nullptr overwrites Y; incb == 0 broadcasts beta[0].  Contractions
+// longer than one super-chunk (480) run as several launches, each later one
+// adding its block's product to Y.
 void tc_lincomb(int n, int k, int m, const double *X, int ldx, const double *C, int ldc, double *Y,
                 int ldy, const double *beta_dev, int incb, cudaStream_t st, double alpha,
                 void *scratch, size_t scratch_bytes) {
     if (n <= 0 || m <= 0) return;
     const int bn = tc_bn(m);
     CUtensorMap ma;
-    if (!tc_map(&ma, X, n, k, (size_t)ldx, kTcM, kTcRawK, false)) {
+    if (!tc_map(&ma, X, n, std::min(k, kTcSuperLincomb), (size_t)ldx, kTcM, kTcRawK, false)) {
         lincomb(n, k, m, X, ldx, C, ldc, Y, ldy, beta_dev, incb, st, alpha);
         return;
     }
-    GCGE_REQUIRE(scratch && scratch_bytes >= tc_bprep_bytes(k, m), GCGE_ERR_ARG,
+    GCGE_REQUIRE(scratch && scratch_bytes >= tc_lincomb_scratch_bytes(k, m), GCGE_ERR_ARG,
                  "tc_lincomb: scratch too small");
-    TcArgs a{};
-    a.M = n;
-    a.N = m;
-    a.K = k;
-    a.A = X;
-    a.lda = (size_t)ldx;
-    a.super_k = kTcSuperLincomb;
-    a.mtiles = (n + kTcM - 1) / kTcM;
-    a.ntiles = (m + bn - 1) / bn;
-    a.items = a.mtiles * a.ntiles;
-    a.out = Y;
-    a.ldo = (size_t)ldy;
-    a.beta = beta_dev;
-    a.incb = incb;
-    a.alpha = alpha;
-    a.nstages = (k + kTcStageK - 1) / kTcStageK;
-    a.nsup = (k + kTcSuperLincomb - 1) / kTcSuperLincomb;
-    a.error = tc_error_word();
-    uint8_t *planes = static_cast<uint8_t *>(scratch);
-    const size_t pbytes = (size_t)a.ntiles * a.nstages * tc_tile_bytes(bn);
-    int *bexps = reinterpret_cast<int *>(
-        (reinterpret_cast<uintptr_t>(planes + pbytes) + 255) & ~(uintptr_t)255);
-    const dim3 pg(a.nsup, a.ntiles);
-    switch (bn) {
-        case 16: k_tc_bprep<16><<<pg, 256, 0, st>>>(C, (size_t)ldc, m, k, kTcSuperLincomb, planes, bexps, a.nstages, a.nsup); break;
-        case 32: k_tc_bprep<32><<<pg, 256, 0, st>>>(C, (size_t)ldc, m, k, kTcSuperLincomb, planes, bexps, a.nstages, a.nsup); break;
-        default: k_tc_bprep<48><<<pg, 256, 0, st>>>(C, (size_t)ldc, m, k, kTcSuperLincomb, planes, bexps, a.nstages, a.nsup); break;
+    for (int k0 = 0; k0 < k; k0 += kTcSuperLincomb) {
+        const int kb = std::min(kTcSuperLincomb, k - k0);
+        const double *Xb = X + (size_t)k0 * ldx;
+        // (the first block's map was made above; Xb keeps its 16-byte alignment)
+        if (k0 > 0 && !tc_map(&ma, Xb, n, kb, (size_t)ldx, kTcM, kTcRawK, false))
+            throw CudaError{GCGE_ERR_ARG, "tc_lincomb: operand layout"};
+        TcArgs a{};
+        a.M = n;
+        a.N = m;
+        a.K = kb;
+        a.A = Xb;
+        a.lda = (size_t)ldx;
+        a.super_k = kTcSuperLincomb;
+        a.mtiles = (n + kTcM - 1) / kTcM;
+        a.ntiles = (m + bn - 1) / bn;
+        a.items = a.mtiles * a.ntiles;
+        a.out = Y;
+        a.ldo = (size_t)ldy;
+        a.beta = beta_dev;
+        a.incb = incb;
+        a.alpha = alpha;
+        a.accumulate = k0 > 0 ? 1 : 0;
+        a.nstages = (kb + kTcStageK - 1) / kTcStageK;
+        a.nsup = 1;
+        a.error = tc_error_word();
+        uint8_t *planes = static_cast<uint8_t *>(scratch);
+        const size_t pbytes = (size_t)a.ntiles * a.nstages * tc_tile_bytes(bn);
+        int *bexps = reinterpret_cast<int *>(
+            (reinterpret_cast<uintptr_t>(planes + pbytes) + 255) & ~(uintptr_t)255);
+        const dim3 pg(1, a.ntiles);
+        const double *Cb = C + k0;
+        switch (bn) {
+            case 16: k_tc_bprep<16><<<pg, 256, 0, st>>>(Cb, (size_t)ldc, m, kb, kTcSuperLincomb, planes, bexps, a.nstages, 1); break;
+            case 32: k_tc_bprep<32><<<pg, 256, 0, st>>>(Cb, (size_t)ldc, m, kb, kTcSuperLincomb, planes, bexps, a.nstages, 1); break;
+            default: k_tc_bprep<48><<<pg, 256, 0, st>>>(Cb, (size_t)ldc, m, kb, kTcSuperLincomb, planes, bexps, a.nstages, 1); break;
+        }
+        // exponent fields of the rows of X over the block's columns
+        DevBuf<int> &eb = slot_stage().tc_exps;
+        eb.alloc((size_t)n);
+        k_tc_exprows<<<dim3((n + 255) / 256, 1), 256, 0, st>>>(Xb, (size_t)ldx, n, kb,
+                                                             kTcSuperLincomb, eb.p);
+        GCGE_CHECK_LAUNCH();
+        count_launch(2);
+        a.bplanes = planes;
+        a.eA = eb.p;
+        a.eB = bexps;
+        launch_tc_bn<false>(ma, ma, a, bn, std::min(a.items, device_sms()), st);
     }
-    // exponent fields of the rows of X per super-chunk of its columns
-    DevBuf<int> &eb = slot_stage().tc_exps;
-    eb.alloc((size_t)a.nsup * n);
-    k_tc_exprows<<<dim3((n + 255) / 256, a.nsup), 256, 0, st>>>(X, (size_t)ldx, n, k,
-                                                              kTcSuperLincomb, eb.p);
-    GCGE_CHECK_LAUNCH();
-    count_launch(2);
-    a.bplanes = planes;
-    a.eA = eb.p;
-    a.eB = bexps;
-    launch_tc_bn<false>(ma, ma, a, bn, std::min(a.items, device_sms()), st);
 }
 
 }  // namespace gcge
