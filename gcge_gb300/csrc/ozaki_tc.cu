@@ -97,7 +97,9 @@ struct TcLayout {
     static constexpr uint32_t b_bytes = tc_tile_bytes(BN);
     static constexpr uint32_t a_box = GRAM ? 16u * kTcM * 8u : (uint32_t)kTcRawK * kTcM * 8u;
     static constexpr uint32_t b_box = GRAM ? 16u * BN * 8u : b_bytes;  // lincomb: planes
-    static constexpr uint32_t raw_bytes = tc_round(a_box + 2 * b_box, 1024);
+    // gram: two A boxes and two B boxes; lincomb: one A box and two planes
+    static constexpr uint32_t raw_bytes =
+        GRAM ? 2 * (a_box + b_box) : tc_round(a_box + 2 * b_box, 1024);
     static constexpr uint32_t raw_off = 0;  // [2] raw stages
     static constexpr uint32_t stage_bytes = a_bytes + b_bytes;
     static constexpr uint32_t dig_off = tc_round(raw_off + 2 * raw_bytes, 1024);  // [2] digit stages
