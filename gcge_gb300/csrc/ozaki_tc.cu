@@ -112,6 +112,11 @@ struct TcLayout {
     static constexpr uint32_t misc_off = bar_off + nbars * 8;  // tmem slot, abort flag
     static constexpr uint32_t bytes = misc_off + 16;
     static constexpr uint32_t alloc_bytes = bytes + 1024;  // room to align the base
+    // what the bulk copies of one raw stage write fits the stage
+    static_assert((GRAM ? 2 * (a_box + b_box) : a_box + 2 * b_box) <= raw_bytes,
+                  "raw stage too small for its bulk copies");
+    static_assert(raw_off + 2 * raw_bytes <= dig_off, "raw stages overlap the digit stages");
+    static_assert(alloc_bytes <= 232448, "shared memory beyond the per-CTA limit");
 };
 
 struct TcArgs {
