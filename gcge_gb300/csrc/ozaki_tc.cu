@@ -84,6 +84,15 @@ __host__ __device__ constexpr uint32_t tc_tile_bytes(int rows) {
     return kTcDigits * tc_plane(rows);
 }
 __host__ __device__ constexpr uint32_t tc_round(uint32_t x, uint32_t a) { return (x + a - 1) / a * a; }
+// The right operand's 7 digit planes form ONE tile of 7 BN rows (plane j at
+// rows [j BN, (j + 1) BN)), so that a single MMA with N = (7 - i) BN
+// multiplies left plane i by right planes 0 .. 6 - i and adds each product
+// into its level's accumulator columns (level l = i + j at columns l BN):
+// k-group g, row r at g * lbo_b + (r / 8) * 128 + (r % 8) * 16.
+__host__ __device__ constexpr uint32_t tc_lbo_b(int bn) {
+    return (uint32_t)kTcDigits * bn * 16u + 16u;
+}
+__host__ __device__ constexpr uint32_t tc_tile_b_bytes(int bn) { return kTcKGroups * tc_lbo_b(bn); }
 
 // Shared memory (offsets from a 1024-byte aligned base).  Raw stage of a
 // Gram: A boxes [2][128 rows][16 k] and B boxes [2][BN rows][16 k] of FP64 in
@@ -94,7 +103,7 @@ __host__ __device__ constexpr uint32_t tc_round(uint32_t x, uint32_t a) { return
 template <int BN, bool GRAM>
 struct TcLayout {
     static constexpr uint32_t a_bytes = tc_tile_bytes(kTcM);
-    static constexpr uint32_t b_bytes = tc_tile_bytes(BN);
+    static constexpr uint32_t b_bytes = tc_tile_b_bytes(BN);
     static constexpr uint32_t a_box = GRAM ? 16u * kTcM * 8u : (uint32_t)kTcRawK * kTcM * 8u;
     static constexpr uint32_t b_box = GRAM ? 16u * BN * 8u : b_bytes;  // lincomb: planes
     // gram: two A boxes and two B boxes; lincomb: one A box and two planes
@@ -471,7 +480,6 @@ __global__ void __launch_bounds__(kTcThreads, 1)
 
     if (warp == 0) {
         // ------------------------------------------------------------ MMA issuer
-        constexpr uint32_t idesc = tc_idesc(kTcM, BN);
         uint32_t t = 0, d = 0;  // digit stages and drain chunks issued so far
         bool ok = true;
         for (int it = blockIdx.x; it < a.items && ok; it += gridDim.x) {
@@ -493,18 +501,21 @@ __global__ void __launch_bounds__(kTcThreads, 1)
                     if (lane == 0) {
                         const uint32_t abase = sbase + L::dig_off + s * L::stage_bytes;
                         const uint32_t bbase = abase + L::a_bytes;
+                        // left plane i times right planes j = 0 .. 6 - i, into
+                        // levels l = i + j, in MMAs of at most kLvl levels (N <= 256)
+                        constexpr int kLvl = 256 / BN < kTcDigits ? 256 / BN : kTcDigits;
 #pragma unroll
                         for (int i = 0; i < kTcDigits; ++i) {
                             const uint64_t ad =
                                 smem_desc(abase + i * tc_plane(kTcM), tc_lbo(kTcM), 128);
 #pragma unroll
-                            for (int j = 0; j + i < kTcDigits; ++j) {
-                                const uint64_t bd =
-                                    smem_desc(bbase + j * tc_plane(BN), tc_lbo(BN), 128);
-                                const int l = i + j;
+                            for (int l0 = i; l0 < kTcDigits; l0 += kLvl) {
+                                const int nl = min(kLvl, kTcDigits - l0);
+                                const uint64_t bd = smem_desc(
+                                    bbase + (uint32_t)((l0 - i) * BN / 8) * 128u, tc_lbo_b(BN), 128);
                                 // the first product into a level in a drain chunk
                                 // overwrites it (level l first meets i = 0)
-                                tc_mma(tmem + (uint32_t)(l * BN), ad, bd, idesc,
+                                tc_mma(tmem + (uint32_t)(l0 * BN), ad, bd, tc_idesc(kTcM, nl * BN),
                                        (st > 0 || i > 0) ? 1u : 0u);
                             }
                         }
@@ -787,9 +798,10 @@ __global__ void __launch_bounds__(kTcThreads, 1)
                         }
                         em[h] = isb ? ebuf_b[rr] : ebuf_a[rr];
                         if (live) {
-                            dstb[h] = (isb ? bbuf : abuf) + (uint32_t)g * tc_lbo(rows) +
+                            dstb[h] = (isb ? bbuf : abuf) +
+                                      (uint32_t)g * (isb ? tc_lbo_b(BN) : tc_lbo(kTcM)) +
                                       (uint32_t)(rr >> 3) * 128u + (uint32_t)(rr & 7) * 16u;
-                            pl[h] = tc_plane(rows);
+                            pl[h] = isb ? (uint32_t)BN * 16u : tc_plane(kTcM);
                         }
                     }
 #pragma unroll
@@ -892,7 +904,7 @@ template <int BN>
 __global__ void __launch_bounds__(256) k_tc_bprep(const double *__restrict__ C, size_t ldc, int N,
                                                   int K, int super_k, uint8_t *__restrict__ planes,
                                                   int *__restrict__ exps, int nstages, int nsup) {
-    constexpr uint32_t bb = tc_tile_bytes(BN);
+    constexpr uint32_t bb = tc_tile_b_bytes(BN);
     __shared__ int em_s[BN];
     const int sidx = blockIdx.x, nt = blockIdx.y;
     const int sk = sidx * super_k, ske = min(K, sk + super_k);
@@ -920,11 +932,11 @@ __global__ void __launch_bounds__(256) k_tc_bprep(const double *__restrict__ C, 
                 v[q] = (gc < N && k + q < ske) ? C[k + q + (size_t)gc * ldc] : 0.0;
             uint4 dg[kTcDigits];
             tc_digits8(v, em_s[c], dg);
-            uint8_t *base = dst + (uint32_t)g * tc_lbo(BN) + (uint32_t)(c >> 3) * 128u +
+            uint8_t *base = dst + (uint32_t)g * tc_lbo_b(BN) + (uint32_t)(c >> 3) * 128u +
                             (uint32_t)(c & 7) * 16u;
 #pragma unroll
             for (int i = 0; i < kTcDigits; ++i)
-                *reinterpret_cast<uint4 *>(base + (uint32_t)i * tc_plane(BN)) = dg[i];
+                *reinterpret_cast<uint4 *>(base + (uint32_t)i * BN * 16u) = dg[i];
         }
     }
 }
@@ -1037,7 +1049,7 @@ size_t tc_bprep_bytes(int k, int m) {
     const size_t nt = (size_t)(m + bn - 1) / bn;
     const size_t nst = (size_t)(k + kTcStageK - 1) / kTcStageK;
     const size_t nsup = (size_t)(k + kTcSuperLincomb - 1) / kTcSuperLincomb;
-    const size_t bb = tc_tile_bytes(bn);
+    const size_t bb = tc_tile_b_bytes(bn);
     return nt * nst * bb + 256 + nt * nsup * bn * sizeof(int) + 256;
 }
 
@@ -1171,7 +1183,7 @@ void tc_lincomb(int n, int k, int m, const double *X, int ldx, const double *C, 
         a.nsup = 1;
         a.error = tc_error_word();
         uint8_t *planes = static_cast<uint8_t *>(scratch);
-        const size_t pbytes = (size_t)a.ntiles * a.nstages * tc_tile_bytes(bn);
+        const size_t pbytes = (size_t)a.ntiles * a.nstages * tc_tile_b_bytes(bn);
         int *bexps = reinterpret_cast<int *>(
             (reinterpret_cast<uintptr_t>(planes + pbytes) + 255) & ~(uintptr_t)255);
         const dim3 pg(1, a.ntiles);
