@@ -5,42 +5,44 @@
 // MultiVecLinearComb (app/app_lapack.c:64-183, :463-534).
 //
 // Method (error-free digit splitting, the Ozaki scheme), as in ozaki.cu:
-// within a super-chunk of consecutive k every row of the left operand and
-// every column of the right operand gets an exponent e with |x| < 2^e, |x|
-// becomes the 56-bit fixed-point integer X = |x| 2^(56-e) (truncated), written
-// as 7 digits of 8 bits with x's sign: the leading digit in [0, 256], the
-// others balanced in [-128, 127].  Digits are exact in FP16, the 28 digit
+// within an exponent window of consecutive k every row of the left operand
+// and every column of the right operand gets an exponent e with |x| < 2^e,
+// |x| becomes the 56-bit fixed-point integer X = |x| 2^(56-e) (truncated),
+// written as 7 digits of 8 bits with x's sign: the leading digit in [0, 256],
+// the others balanced in [-128, 127].  Digits are exact in FP16, the 28 digit
 // pairs with i + j <= 6 are multiplied on the tensor cores and summed into 7
 // level accumulators L_l = sum_{i+j=l} d_i d'_j, which are exact FP32 integers
 // as long as |L_l| < 2^24: 96 consecutive k at most (|L_6| <= 96 (2 * 256 *
 // 128 + 5 * 128^2) < 2^23.8).  Every 96 k ("drain") the levels are read out of
-// tensor memory and folded into two exact int64 words; every super-chunk the
-// words are converted to FP64 with the super-chunk's scale and added.  Error:
-// below 2^-55 of the super-chunk's largest |x| |y| per product.
+// tensor memory into one exact 96-bit integer per output; at the end of a
+// window it is converted to FP64 (integer instructions, round to nearest) with
+// the window's scale.  A Gram work item has one window over its whole k range
+// (error below 2^-54 sqrt(K) |x| |y| per entry, under the FP64 dot product's
+// bound K 2^-53 |x| |y|); a linear combination has one per 480 k.
 //
-// Data path, per CTA (one per SM, persistent over work items):
+// Data path, per CTA (one per SM, persistent over work items, 16 warps):
 //  * exponent fields come from a streaming pre-pass (k_tc_expcols /
-//    k_tc_exprows: per column of the Gram operands over each 384-row
-//    super-chunk, per row of the linear combination's left operand over each
-//    480-column super-chunk);
-//  * one producer thread issues bulk tensor copies (cp.async.bulk.tensor.2d,
-//    TMA) of the raw FP64 tiles of each 32-k raw stage, two raw stages ahead,
-//    into shared memory (Gram tiles: 16 k x rows boxes with the 128-byte
-//    swizzle, so that a lane per row reads them without bank conflicts);
-//  * 7 producer warps turn each 16-k half of a raw stage into the 7 FP16
-//    digit planes of a digit stage (two digit stages, K-major core-matrix
-//    layout: 8 rows x 16 bytes per core matrix); the right operand of a linear
-//    combination is prepared once per call (k_tc_bprep) and copied into each
-//    digit stage with cp.async.bulk;
-//  * one thread of warp 0 issues the 28 MMAs of each digit stage (M = 128 rows,
-//    N = BN, K = 16, f16 x f16 -> f32 into 7 level accumulators in tensor
-//    memory, 7 x BN of its 512 columns) and commits each stage to an mbarrier;
-//  * 12 drain warps read the levels of each 96-k chunk from tensor memory
-//    (warp w reads lanes 32 (w % 4) .. + 31), fold them into int64 registers,
-//    and at each super-chunk end into FP64 accumulators in shared memory; at
-//    the end of a work item they write the result.
+//    k_tc_exprows: per column of the Gram operands over each window, per row
+//    of the linear combination's left operand);
+//  * bulk tensor copies (cp.async.bulk.tensor.2d, TMA) bring the raw FP64
+//    tiles of each 32-k raw stage into shared memory two raw stages ahead
+//    (Gram tiles: 16 k x rows boxes with the 128-byte swizzle, so that lanes
+//    reading rows hit distinct banks); the right operand of a linear
+//    combination is prepared once per call (k_tc_bprep) and copied in with
+//    cp.async.bulk;
+//  * every warp turns its core matrices (8 rows x 8 k) of each 16-k half of a
+//    raw stage into the 7 FP16 digit planes of a digit stage (two digit
+//    stages, K-major core-matrix layout);
+//  * the last warp to finish a digit stage issues its MMAs (M = 128 rows,
+//    N = up to 256, K = 16, f16 x f16 -> f32 into the 7 level accumulators,
+//    7 x BN of the 512 tensor-memory columns) and commits them to an
+//    mbarrier; the last warp to finish reading a raw stage issues the bulk
+//    copies of the raw stage two ahead;
+//  * every warp drains its slice of the levels after each 96-k chunk (warp w
+//    reads lanes 32 (w % 4) .. + 31, BN / 4 columns) and folds it at the end
+//    of each window.
 // Every wait on an mbarrier is bounded; a wait that runs out sets the error
-// word and every role stops at its next wait, so the kernel always returns.
+// word and every warp stops at its next wait, so the kernel always returns.
 #include <cuda.h>
 #include <cudaTypedefs.h>
 
@@ -59,19 +61,15 @@ constexpr int kTcRawK = 32;    // k per raw (TMA) stage: two digit stages
 constexpr int kTcDrainStages = 6;
 constexpr int kTcDrainK = kTcStageK * kTcDrainStages;  // 96: exact FP32 level sums
 constexpr int kTcKGroups = kTcStageK / 8;              // core matrices along k per stage
-constexpr int kTcProdWarps = 7, kTcDrainWarps = 12;
-constexpr int kTcWarps = 1 + kTcProdWarps + kTcDrainWarps;
-constexpr int kTcThreads = kTcWarps * 32;  // 640
-constexpr int kTcProdThreads = kTcProdWarps * 32;
-constexpr int kTcDrainThreads = kTcDrainWarps * 32;
+constexpr int kTcWarps = 16;  // every warp converts digits and drains
+constexpr int kTcThreads = kTcWarps * 32;
 constexpr uint32_t kTcTmemCols = 512;
 // bounded mbarrier waits: 4 s of device clock, or this many suspended tests
 constexpr unsigned long long kTcWaitNs = 4000000000ull;
 constexpr long long kTcWaitPolls = 1LL << 22;
-// exponent-field slots: the producers fill super-chunk j + 1's while the
-// drain folds super-chunk j - 1 with its own
-constexpr int kTcExpSlots = 3;
-constexpr int kTcSuperGram = 4 * kTcDrainK;     // 384 rows of the Gram operands
+// A Gram work item shares one exponent per column over its whole k range
+// (at most this many rows: the 96-bit level sums stay below 2^85)
+constexpr int kTcSuperGramMax = 16384 * kTcDrainK;
 constexpr int kTcSuperLincomb = 5 * kTcDrainK;  // 480: K up to 480 in one super-chunk
 
 // Byte layout of one operand tile of R rows in a digit stage: plane i
@@ -113,13 +111,14 @@ struct TcLayout {
     static constexpr uint32_t stage_bytes = a_bytes + b_bytes;
     static constexpr uint32_t dig_off = tc_round(raw_off + 2 * raw_bytes, 1024);  // [2] digit stages
     static constexpr uint32_t acc_off = dig_off + 2 * stage_bytes;  // double acc[BN][kTcM]
-    static constexpr uint32_t ea_off = acc_off + (GRAM ? (uint32_t)BN * kTcM * 8 : 0u);  // int ea[3][kTcM]
-    static constexpr uint32_t eb_off = ea_off + kTcExpSlots * kTcM * 4;     // int eb[3][BN]
-    static constexpr uint32_t bar_off = tc_round(eb_off + kTcExpSlots * BN * 4, 16);
-    // full[2] empty[2] rfull[2] accf tfree exfull[3] exfree[3] final
-    static constexpr int nbars = 9 + 2 * kTcExpSlots;
-    static constexpr uint32_t misc_off = bar_off + nbars * 8;  // tmem slot, abort flag
-    static constexpr uint32_t bytes = misc_off + 16;
+    static constexpr uint32_t bar_off =
+        tc_round(acc_off + (GRAM ? (uint32_t)BN * kTcM * 8 : 0u), 16);
+    // mbarriers empty[2] rfull[2] accf
+    static constexpr int nbars = 5;
+    // tmem slot, abort flag, arrival counters full[2] and rempty[2], digit
+    // stages issued, drain chunks committed, raw stages issued
+    static constexpr uint32_t misc_off = bar_off + nbars * 8;
+    static constexpr uint32_t bytes = misc_off + 48;
     static constexpr uint32_t alloc_bytes = bytes + 1024;  // room to align the base
     // what the bulk copies of one raw stage write fits the stage
     static_assert((GRAM ? 2 * (a_box + b_box) : a_box + 2 * b_box) <= raw_bytes,
@@ -219,6 +218,17 @@ __device__ __forceinline__ bool mbar_wait_warp(uint64_t *b, uint32_t parity,
     return ok != 0;
 }
 
+// Arrival on a shared-memory counter (release and acquire at CTA scope);
+// returns the count before it.
+__device__ __forceinline__ uint32_t smem_arrive(uint32_t *ctr) {
+    uint32_t old;
+    asm volatile("atom.acq_rel.cta.shared::cta.add.u32 %0, [%1], 1;"
+                 : "=r"(old)
+                 : "r"(su32(ctr))
+                 : "memory");
+    return old;
+}
+
 // ---------------------------------------------------------------- tcgen05
 __device__ __forceinline__ uint64_t smem_desc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
     // start address, leading (k-direction) and stride (8-row) byte offsets in
@@ -251,12 +261,10 @@ __device__ __forceinline__ void tc_fence_before() {
 __device__ __forceinline__ void tc_fence_after() {
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
 }
-__device__ __forceinline__ void tc_ld8(uint32_t taddr, uint32_t (&r)[8]) {
-    asm volatile(
-        "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
-        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
-          "=r"(r[7])
-        : "r"(taddr));
+__device__ __forceinline__ void tc_ld4(uint32_t taddr, uint32_t (&r)[4]) {
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x4.b32 {%0,%1,%2,%3}, [%4];"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
+                 : "r"(taddr));
 }
 __device__ __forceinline__ void tc_wait_ld() {
     asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
@@ -305,29 +313,30 @@ __device__ __forceinline__ uint32_t tc_hsub2(uint32_t a, uint32_t b) {
 // sign.  A digit is formed for two values at once: the FP16 pattern
 // sign | 0x6400 | field is +-(1024 + field) exactly (ulp 1 on [1024, 2048)),
 // and subtracting +-1024 (digit 0) or +-(1024 + 128) leaves +-d exactly.
-__device__ __forceinline__ void tc_digits8(const double (&v)[8], int emax, uint4 (&out)[kTcDigits]) {
-    uint32_t w[kTcDigits][4];
-#pragma unroll
-    for (int e = 0; e < 8; e += 2) {
-        uint32_t yh0, yl0, s0, yh1, yl1, s1;
-        tc_fixed56(v[e], (uint32_t)emax, yh0, yl0, s0);
-        tc_fixed56(v[e + 1], (uint32_t)emax, yh1, yl1, s1);
-        const uint32_t M = 0x64006400u | (s0 >> 16) | s1;  // +-1024 in each half
-        const uint32_t Mb = M | 0x00800080u;                // +-(1024 + 128)
-        w[0][e / 2] = tc_hsub2((yh0 >> 16) | (yh1 & 0xFFFF0000u) | M, M);
-        // byte 6 - i of Y: bytes 4, 5 in the high word, 0..3 in the low word;
-        // the permutation puts value 0's byte in half 0 and value 1's in half 1
-        w[1][e / 2] = tc_hsub2((__byte_perm(yh0, yh1, 0x0501) & 0x00FF00FFu) | M, Mb);
-        w[2][e / 2] = tc_hsub2((__byte_perm(yh0, yh1, 0x0400) & 0x00FF00FFu) | M, Mb);
-        w[3][e / 2] = tc_hsub2((__byte_perm(yl0, yl1, 0x0703) & 0x00FF00FFu) | M, Mb);
-        w[4][e / 2] = tc_hsub2((__byte_perm(yl0, yl1, 0x0602) & 0x00FF00FFu) | M, Mb);
-        w[5][e / 2] = tc_hsub2((__byte_perm(yl0, yl1, 0x0501) & 0x00FF00FFu) | M, Mb);
-        w[6][e / 2] = tc_hsub2((__byte_perm(yl0, yl1, 0x0400) & 0x00FF00FFu) | M, Mb);
-    }
-#pragma unroll
-    for (int i = 0; i < kTcDigits; ++i) out[i] = make_uint4(w[i][0], w[i][1], w[i][2], w[i][3]);
+__device__ __forceinline__ void tc_digit_pair(double x0, double x1, uint32_t emax,
+                                              uint32_t (&w)[kTcDigits]) {
+    uint32_t yh0, yl0, s0, yh1, yl1, s1;
+    tc_fixed56(x0, emax, yh0, yl0, s0);
+    tc_fixed56(x1, emax, yh1, yl1, s1);
+    const uint32_t M = 0x64006400u | (s0 >> 16) | s1;  // +-1024 in each half
+    const uint32_t Mb = M | 0x00800080u;                // +-(1024 + 128)
+    w[0] = tc_hsub2((yh0 >> 16) | (yh1 & 0xFFFF0000u) | M, M);
+    // byte 6 - i of Y: bytes 4, 5 in the high word, 0..3 in the low word; the
+    // permutation puts value 0's byte in half 0 and value 1's in half 1
+    w[1] = tc_hsub2((__byte_perm(yh0, yh1, 0x0501) & 0x00FF00FFu) | M, Mb);
+    w[2] = tc_hsub2((__byte_perm(yh0, yh1, 0x0400) & 0x00FF00FFu) | M, Mb);
+    w[3] = tc_hsub2((__byte_perm(yl0, yl1, 0x0703) & 0x00FF00FFu) | M, Mb);
+    w[4] = tc_hsub2((__byte_perm(yl0, yl1, 0x0602) & 0x00FF00FFu) | M, Mb);
+    w[5] = tc_hsub2((__byte_perm(yl0, yl1, 0x0501) & 0x00FF00FFu) | M, Mb);
+    w[6] = tc_hsub2((__byte_perm(yl0, yl1, 0x0400) & 0x00FF00FFu) | M, Mb);
 }
-
+__device__ __forceinline__ void tc_digits8(const double (&v)[8], int emax, uint4 (&out)[kTcDigits]) {
+    uint32_t w[4][kTcDigits];
+#pragma unroll
+    for (int e = 0; e < 4; ++e) tc_digit_pair(v[2 * e], v[2 * e + 1], (uint32_t)emax, w[e]);
+#pragma unroll
+    for (int i = 0; i < kTcDigits; ++i) out[i] = make_uint4(w[0][i], w[1][i], w[2][i], w[3][i]);
+}
 // ---------------------------------------------------------------- bulk copies
 __device__ __forceinline__ void mbar_expect_tx(uint64_t *b, uint32_t bytes) {
     asm volatile("mbarrier.arrive.expect_tx.release.cta.shared::cta.b64 _, [%0], %1;" ::"r"(
@@ -358,6 +367,67 @@ __device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap *map
 // exact int64 -> double for |t| < 2^51
 __device__ __forceinline__ double tc_i64_to_f64(long long t) {
     return __longlong_as_double(t + 0x4338000000000000LL) - 6755399441055744.0;
+}
+
+// (vh 2^64 + vl) 2^e as a double, rounded to nearest (ties to even), with
+// integer instructions only (FP64 arithmetic is a slow pipe on this part).
+// Results below the normal range flush to zero; above it they are +-inf.
+__device__ __forceinline__ double tc_i128_f64(long long vh, unsigned long long vl, int e) {
+    // vh 2^64 + vl, a two's-complement 128-bit integer
+    const bool neg = vh < 0;
+    if (neg) {
+        vl = ~vl + 1ull;
+        vh = ~vh + (vl == 0 ? 1 : 0);
+    }
+    const unsigned long long mh = (unsigned long long)vh;  // magnitude mh 2^64 + vl
+    if ((mh | vl) == 0) return 0.0;
+    // the leading 64 bits th (top bit set) and the rest tl
+    int lz;
+    unsigned long long th, tl;
+    if (mh != 0) {
+        lz = __clzll((long long)mh);
+        th = lz ? (mh << lz) | (vl >> (64 - lz)) : mh;
+        tl = vl << lz;
+    } else {
+        lz = 64 + __clzll((long long)vl);
+        th = vl << (lz - 64);
+        tl = 0;
+    }
+    // 53 bits kept, 11 rounded, tl sticky; the magnitude is mant 2^(75 - lz)
+    const unsigned long long mant = th >> 11, rb = th & 0x7FFull;
+    const bool up = rb > 0x400ull || (rb == 0x400ull && (tl != 0 || (mant & 1ull)));
+    const int field = 1023 + 127 - lz + e;
+    unsigned long long bits;
+    if (field <= 0) {
+        bits = 0;
+    } else if (field >= 2047) {
+        bits = 0x7FF0000000000000ull;
+    } else {
+        // mant holds the hidden bit, so it adds one to field - 1; a carry of
+        // the rounding moves into the exponent
+        bits = ((unsigned long long)(field - 1) << 52) + mant + (up ? 1ull : 0ull);
+        if (bits > 0x7FF0000000000000ull) bits = 0x7FF0000000000000ull;
+    }
+    return __longlong_as_double((long long)(bits | (neg ? 0x8000000000000000ull : 0ull)));
+}
+// A 96-bit two's-complement accumulator (w0 least significant): += (a0, a1, a2)
+__device__ __forceinline__ void tc_acc96(uint32_t &w0, uint32_t &w1, uint32_t &w2, uint32_t a0,
+                                         uint32_t a1, uint32_t a2) {
+    asm("add.cc.u32 %0, %0, %3;\n\taddc.cc.u32 %1, %1, %4;\n\taddc.u32 %2, %2, %5;"
+        : "+r"(w0), "+r"(w1), "+r"(w2)
+        : "r"(a0), "r"(a1), "r"(a2));
+}
+__device__ __forceinline__ void tc_acc64(uint32_t &w1, uint32_t &w2, uint32_t a1, uint32_t a2) {
+    asm("add.cc.u32 %0, %0, %2;\n\taddc.u32 %1, %1, %3;" : "+r"(w1), "+r"(w2) : "r"(a1), "r"(a2));
+}
+// += v 2^(8 (6 - l)) for a level sum v (|v| < 2^31)
+__device__ __forceinline__ void tc_acc_level(uint32_t &w0, uint32_t &w1, uint32_t &w2, int v, int l) {
+    const uint32_t sx = (uint32_t)(v >> 31);
+    const int sh = 8 * (6 - l);
+    if (sh == 0) tc_acc96(w0, w1, w2, (uint32_t)v, sx, sx);
+    else if (sh < 32) tc_acc96(w0, w1, w2, (uint32_t)v << sh, (uint32_t)(v >> (32 - sh)), sx);
+    else if (sh == 32) tc_acc64(w1, w2, (uint32_t)v, sx);
+    else tc_acc64(w1, w2, (uint32_t)v << (sh - 32), (uint32_t)(v >> (64 - sh)));
 }
 
 // Waits, with a bound of its own and regardless of the abort flag, for a
@@ -429,40 +499,53 @@ __device__ __forceinline__ void cur_next(const TcArgs &a, TcCursor &c) {
 }
 
 // ---------------------------------------------------------------- kernel
+// All 16 warps do the same work.  Per digit stage a thread converts one item
+// (4 consecutive k of one row) of the left operand and, for a Gram, the right
+// operand's items of the warps whose turn it is (those rotate over the warps
+// from stage to stage); after each drain chunk it moves its slice of the
+// level accumulators (tensor-memory lane quarter warp % 4, BN / 4 columns)
+// into 64-bit integers, and after a super-chunk it folds them into FP64.
+// The last warp to finish a digit stage issues its MMAs; the last to finish
+// reading a raw stage issues the bulk copies of the raw stage two ahead into
+// its buffer.
+//
+// The waits form no cycle: digit stage t is produced after the MMAs of stage
+// t - 2 completed (a ring of two digit stages); a warp drains the chunk that
+// ends at stage e before it finishes stage e + 1, so the MMAs of stage e + 1,
+// the next chunk's first (which overwrite the accumulators), are issued after
+// every warp drained it.
 template <int BN, bool GRAM>
 __global__ void __launch_bounds__(kTcThreads, 1)
     k_tc_digits(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB,
                 TcArgs a) {
     using L = TcLayout<BN, GRAM>;
+    static_assert(BN % 16 == 0 && BN <= 64, "tile width: a multiple of 16, at most 64");
     extern __shared__ __align__(1024) uint8_t sm_raw[];
     // 1024-byte aligned base (the 128-byte swizzle of the bulk copies needs it)
     uint8_t *sm = sm_raw + ((1024u - (su32(sm_raw) & 1023u)) & 1023u);
     double *acc = reinterpret_cast<double *>(sm + L::acc_off);  // [BN][kTcM]
-    int *ea = reinterpret_cast<int *>(sm + L::ea_off);           // [3][kTcM]
-    int *eb = reinterpret_cast<int *>(sm + L::eb_off);           // [3][BN]
     uint64_t *bars = reinterpret_cast<uint64_t *>(sm + L::bar_off);
-    uint64_t *full = bars, *empty = bars + 2, *rfull = bars + 4, *accf = bars + 6;
-    uint64_t *tfree = bars + 7, *exfull = bars + 8, *exfree = bars + 8 + kTcExpSlots;
-    uint64_t *fin = bars + 8 + 2 * kTcExpSlots;
-    uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(sm + L::misc_off);
-    volatile int *abort_flag = reinterpret_cast<volatile int *>(sm + L::misc_off + 4);
+    uint64_t *empty = bars, *rfull = bars + 2, *accf = bars + 4;
+    uint32_t *misc = reinterpret_cast<uint32_t *>(sm + L::misc_off);
+    uint32_t *tmem_slot = misc;
+    volatile int *abort_flag = reinterpret_cast<volatile int *>(misc + 1);
+    uint32_t *fcnt = misc + 2, *rcnt = misc + 4;
+    int *n_stages = reinterpret_cast<int *>(misc + 6);  // digit stages issued
+    int *n_chunks = reinterpret_cast<int *>(misc + 7);  // drain chunks committed
+    int *n_raw = reinterpret_cast<int *>(misc + 8);     // raw stages issued
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const uint32_t sbase = su32(sm);
+    const int super_k = a.super_k;
 
     if (tid == 0) {
         for (int s = 0; s < 2; ++s) {
-            mbar_init(&full[s], kTcProdThreads);
             mbar_init(&empty[s], 1);
             mbar_init(&rfull[s], 1);
-        }
-        for (int s = 0; s < kTcExpSlots; ++s) {
-            mbar_init(&exfull[s], kTcProdThreads);
-            mbar_init(&exfree[s], kTcDrainThreads);
+            fcnt[s] = rcnt[s] = 0;
         }
         mbar_init(accf, 1);
-        mbar_init(tfree, kTcDrainThreads);
-        mbar_init(fin, 1);
         *abort_flag = 0;
+        *n_stages = *n_chunks = *n_raw = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     if (warp == 0) {
@@ -476,369 +559,323 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     __syncthreads();
     tc_fence_after();
     const uint32_t tmem = *tmem_slot;
-    const int super_k = a.super_k;
 
-    if (warp == 0) {
-        // ------------------------------------------------------------ MMA issuer
-        uint32_t t = 0, d = 0;  // digit stages and drain chunks issued so far
-        bool ok = true;
-        for (int it = blockIdx.x; it < a.items && ok; it += gridDim.x) {
-            const TcItem w = tc_item<GRAM>(a, it);
-            for (int k0 = w.kb; k0 < w.ke && ok; k0 += kTcDrainK, ++d) {
-                if (d > 0 && !mbar_wait_warp(tfree, (d - 1) & 1, abort_flag, a.error)) {
-                    ok = false;
-                    break;
-                }
-                tc_fence_after();
-                const int nst = min(kTcDrainStages, (w.ke - k0 + kTcStageK - 1) / kTcStageK);
-                for (int st = 0; st < nst; ++st, ++t) {
-                    const uint32_t s = t & 1;
-                    if (!mbar_wait_warp(&full[s], (t >> 1) & 1, abort_flag, a.error)) {
-                        ok = false;
-                        break;
-                    }
-                    tc_fence_after();
-                    if (lane == 0) {
-                        const uint32_t abase = sbase + L::dig_off + s * L::stage_bytes;
-                        const uint32_t bbase = abase + L::a_bytes;
-                        // left plane i times right planes j = 0 .. 6 - i, into
-                        // levels l = i + j, in MMAs of at most kLvl levels (N <= 256)
-                        constexpr int kLvl = 256 / BN < kTcDigits ? 256 / BN : kTcDigits;
+    // bulk copies of raw stage q (cursor c) into raw buffer q % 2
+    auto issue_raw = [&](uint32_t q, const TcCursor &c) {
+        const uint32_t r = q & 1;
+        const uint32_t base = sbase + L::raw_off + r * L::raw_bytes;
+        if (GRAM) {
+            mbar_expect_tx(&rfull[r], 2 * (L::a_box + L::b_box));
+            tma_load_2d(base, &mapA, c.k0, c.w.mt0, &rfull[r]);
+            tma_load_2d(base + L::a_box, &mapA, c.k0 + 16, c.w.mt0, &rfull[r]);
+            tma_load_2d(base + 2 * L::a_box, &mapB, c.k0, c.w.nt * BN, &rfull[r]);
+            tma_load_2d(base + 2 * L::a_box + L::b_box, &mapB, c.k0 + 16, c.w.nt * BN, &rfull[r]);
+        } else {
+            // the A box and the prepared planes of the stage's digit stages
+            const int ske = min(c.w.ke, c.sk + super_k);
+            const int nd = min(2, (ske - c.k0 + kTcStageK - 1) / kTcStageK);
+            mbar_expect_tx(&rfull[r], L::a_box + nd * L::b_box);
+            tma_load_2d(base, &mapA, c.w.mt0, c.k0, &rfull[r]);
+            const uint8_t *src =
+                a.bplanes + ((size_t)c.w.nt * a.nstages + (c.k0 - c.w.kb) / kTcStageK) * L::b_bytes;
+            for (int dd = 0; dd < nd; ++dd)
+                bulk_load(base + L::a_box + dd * L::b_box, src + (size_t)dd * L::b_bytes, L::b_bytes,
+                          &rfull[r]);
+        }
+        atomicMax(n_raw, (int)q + 1);
+    };
+    // the MMAs of digit stage t (buffer s, stage st of its drain chunk)
+    auto issue_mma = [&](uint32_t s, int st, bool last_of_chunk) {
+        const uint32_t abase = sbase + L::dig_off + s * L::stage_bytes;
+        const uint32_t bbase = abase + L::a_bytes;
+        // left plane i times right planes j = 0 .. 6 - i, into levels l = i + j,
+        // in MMAs of at most kLvl levels (N <= 256)
+        constexpr int kLvl = 256 / BN < kTcDigits ? 256 / BN : kTcDigits;
 #pragma unroll
-                        for (int i = 0; i < kTcDigits; ++i) {
-                            const uint64_t ad =
-                                smem_desc(abase + i * tc_plane(kTcM), tc_lbo(kTcM), 128);
+        for (int i = 0; i < kTcDigits; ++i) {
+            const uint64_t ad = smem_desc(abase + i * tc_plane(kTcM), tc_lbo(kTcM), 128);
 #pragma unroll
-                            for (int l0 = i; l0 < kTcDigits; l0 += kLvl) {
-                                const int nl = min(kLvl, kTcDigits - l0);
-                                const uint64_t bd = smem_desc(
-                                    bbase + (uint32_t)((l0 - i) * BN / 8) * 128u, tc_lbo_b(BN), 128);
-                                // the first product into a level in a drain chunk
-                                // overwrites it (level l first meets i = 0)
-                                tc_mma(tmem + (uint32_t)(l0 * BN), ad, bd, tc_idesc(kTcM, nl * BN),
-                                       (st > 0 || i > 0) ? 1u : 0u);
-                            }
-                        }
-                        tc_commit(&empty[s]);
-                        if (st == nst - 1) tc_commit(accf);
-                    }
-                    __syncwarp();
-                }
+            for (int l0 = i; l0 < kTcDigits; l0 += kLvl) {
+                const int nl = min(kLvl, kTcDigits - l0);
+                const uint64_t bd =
+                    smem_desc(bbase + (uint32_t)((l0 - i) * BN / 8) * 128u, tc_lbo_b(BN), 128);
+                // the first product into a level in a drain chunk overwrites it
+                // (level l first meets i = 0)
+                tc_mma(tmem + (uint32_t)(l0 * BN), ad, bd, tc_idesc(kTcM, nl * BN),
+                       (st > 0 || i > 0) ? 1u : 0u);
             }
         }
-        // all issued MMAs complete before tensor memory is freed
-        if (lane == 0) tc_commit(fin);
-        __syncwarp();
-        mbar_wait_teardown(fin, 0);
-    } else if (warp >= 4 && warp < 4 + kTcDrainWarps) {
-        // ------------------------------------------------------------ drain
-        const int q = warp & 3;             // tensor-memory lane quarter
-        const int third = (warp - 4) >> 2;  // column-group share
-        const int row = q * 32 + lane;      // output row within the tile
-        constexpr int NG = BN / 8;          // 8-column groups
-        constexpr int GPT = (NG + 2) / 3;   // groups per drain thread (at most)
-        long long thi[GPT * 8], tlo[GPT * 8];
-#pragma unroll
-        for (int c = 0; c < GPT * 8; ++c) thi[c] = tlo[c] = 0;
-        uint32_t d = 0, sc = 0;  // drain chunks and super-chunks consumed so far
-        bool ok = true;
-        for (int it = blockIdx.x; it < a.items && ok; it += gridDim.x) {
-            const TcItem w = tc_item<GRAM>(a, it);
-            const int grow = w.mt0 + row;
-            if (GRAM)
-                for (int c = third; c < NG; c += 3)
-                    for (int cc = 0; cc < 8; ++cc) acc[(c * 8 + cc) * kTcM + row] = 0.0;
-            for (int sk = w.kb; sk < w.ke && ok; sk += super_k, ++sc) {
-                const int ske = min(w.ke, sk + super_k);
-                for (int k0 = sk; k0 < ske; k0 += kTcDrainK, ++d) {
-                    if (!mbar_wait_warp(accf, d & 1, abort_flag, a.error)) {
-                        ok = false;
-                        break;
-                    }
-                    tc_fence_after();
-#pragma unroll
-                    for (int l = 0; l < kTcDigits; ++l) {
-#pragma unroll
-                        for (int gi = 0; gi < GPT; ++gi) {
-                            const int g = third + 3 * gi;
-                            if (g >= NG) break;
-                            uint32_t v[8];
-                            tc_ld8(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(l * BN + g * 8),
-                                   v);
-                            tc_wait_ld();
-#pragma unroll
-                            for (int cc = 0; cc < 8; ++cc) {
-                                const long long L =
-                                    (long long)__float2int_rn(__uint_as_float(v[cc]));
-                                // hi: levels 0..3 in units of level 3; lo: 4..6 in units of 6
-                                if (l <= 3) thi[gi * 8 + cc] += L << (8 * (3 - l));
-                                else tlo[gi * 8 + cc] += L << (8 * (6 - l));
-                            }
-                        }
-                    }
-                    tc_fence_before();
-                    mbar_arrive(tfree);
-                }
-                if (!ok) break;
-                // fold the super-chunk: into the FP64 accumulators (Gram), or
-                // straight into Y (a linear combination's single super-chunk)
-                const uint32_t b = sc % kTcExpSlots;
-                if (!mbar_wait_warp(&exfull[b], (sc / kTcExpSlots) & 1, abort_flag, a.error)) {
-                    ok = false;
-                    break;
-                }
-                const int er = ea[b * kTcM + row];
-#pragma unroll
-                for (int gi = 0; gi < GPT; ++gi) {
-                    const int g = third + 3 * gi;
-                    if (g >= NG) break;
-#pragma unroll
-                    for (int cc = 0; cc < 8; ++cc) {
-                        const int c = g * 8 + cc;
-                        const int ec = eb[b * BN + c];
-                        // the super-chunk's sum: v 2^(er + ec - 2108), or NaN
-                        const bool nan = er == 0x7FF || ec == 0x7FF;
-                        const int fld = er + ec - 1085;  // exponent field of the scale
-                        const double sc2 = fld <= 0 ? 0.0
-                                           : fld >= 2047
-                                               ? __longlong_as_double(0x7FF0000000000000LL)
-                                               : __longlong_as_double((long long)fld << 52);
-                        const double v = fma(tc_i64_to_f64(thi[gi * 8 + cc]), 16777216.0,
-                                             tc_i64_to_f64(tlo[gi * 8 + cc]));
-                        thi[gi * 8 + cc] = tlo[gi * 8 + cc] = 0;
-                        if (GRAM) {
-                            double &A = acc[c * kTcM + row];
-                            if (nan) A = __longlong_as_double(0x7FF8000000000000LL);
-                            else if (fld > 0) A = fma(v, sc2, A);
-                        } else {
-                            const double val =
-                                nan ? __longlong_as_double(0x7FF8000000000000LL) : v * sc2;
-                            const int col = w.nt * BN + c;
-                            if (grow < a.M && col < a.N) {
-                                double *dst = a.out + grow + (size_t)col * a.ldo;
-                                double y = a.alpha * val;
-                                if (a.accumulate) {
-                                    y += *dst;
-                                } else if (a.beta != nullptr) {
-                                    const double bb =
-                                        a.beta[a.incb == 0 ? 0 : (size_t)col * a.incb];
-                                    if (bb != 0.0) y = fma(bb, *dst, y);
-                                }
-                                *dst = y;
-                            }
-                        }
-                    }
-                }
-                mbar_arrive(&exfree[b]);
-            }
-            if (!ok) break;
-            // the work item's result (Gram: split-k partials)
-            if (GRAM && grow < a.M) {
-                const int z = it / (a.mtiles * a.ntiles);
-                for (int g = third; g < NG; g += 3) {
-                    for (int cc = 0; cc < 8; ++cc) {
-                        const int col = w.nt * BN + g * 8 + cc;
-                        if (col < a.N)
-                            a.out[(size_t)z * a.M * a.N + grow + (size_t)col * a.M] =
-                                acc[(g * 8 + cc) * kTcM + row];
-                    }
-                }
-            }
+        tc_commit(&empty[s]);
+        if (last_of_chunk) {
+            tc_commit(accf);
+            atomicAdd(n_chunks, 1);
         }
-    } else {
-        // ------------------------------------------------------------ producers
-        const int pw = warp < 4 ? warp - 1 : warp - (4 + kTcDrainWarps) + 3;  // 0..6
-        const int p = pw * 32 + lane;                                          // 0..223
-        auto prod_sync = [] { asm volatile("bar.sync 1, %0;" ::"n"(kTcProdThreads) : "memory"); };
-        // bulk tensor copies of raw stage q (cursor c) into raw buffer q % 2
-        auto issue = [&](uint32_t q, const TcCursor &c) {
-            const uint32_t r = q & 1;
-            const uint32_t base = sbase + L::raw_off + r * L::raw_bytes;
-            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-            if (GRAM) {
-                mbar_expect_tx(&rfull[r], 2 * (L::a_box + L::b_box));
-                tma_load_2d(base, &mapA, c.k0, c.w.mt0, &rfull[r]);
-                tma_load_2d(base + L::a_box, &mapA, c.k0 + 16, c.w.mt0, &rfull[r]);
-                tma_load_2d(base + 2 * L::a_box, &mapB, c.k0, c.w.nt * BN, &rfull[r]);
-                tma_load_2d(base + 2 * L::a_box + L::b_box, &mapB, c.k0 + 16, c.w.nt * BN,
-                            &rfull[r]);
-            } else {
-                // the A box and the prepared planes of the stage's digit stages
-                const int ske = min(c.w.ke, c.sk + super_k);
-                const int nd = min(2, (ske - c.k0 + kTcStageK - 1) / kTcStageK);
-                mbar_expect_tx(&rfull[r], L::a_box + nd * L::b_box);
-                tma_load_2d(base, &mapA, c.w.mt0, c.k0, &rfull[r]);
-                const uint8_t *src =
-                    a.bplanes +
-                    ((size_t)c.w.nt * a.nstages + (c.k0 - c.w.kb) / kTcStageK) * L::b_bytes;
-                for (int dd = 0; dd < nd; ++dd)
-                    bulk_load(base + L::a_box + dd * L::b_box, src + (size_t)dd * L::b_bytes,
-                              L::b_bytes, &rfull[r]);
-            }
-        };
-        // exponent fields of super-chunk (w, sk) into slot b
-        auto load_exps = [&](const TcItem &w, int sk, uint32_t b) {
-            const int sidx = (sk - (GRAM ? 0 : w.kb)) / super_k;
-            for (int r = p; r < kTcM; r += kTcProdThreads) {
-                const int gr = w.mt0 + r;
-                ea[b * kTcM + r] = gr < a.M ? a.eA[(size_t)sidx * a.M + gr] : 1;
-            }
-            for (int c = p; c < BN; c += kTcProdThreads) {
-                const int gc = w.nt * BN + c;
-                if (GRAM) eb[b * BN + c] = gc < a.N ? a.eB[(size_t)sidx * a.N + gc] : 1;
-                else eb[b * BN + c] = a.eB[((size_t)w.nt * a.nsup + sidx) * BN + c];
-            }
-        };
+    };
 
-        TcCursor cons, tma;
-        cur_init<GRAM>(a, cons);
-        tma = cons;
-        uint32_t issued = 0;  // raw stages issued
-        if (p == 0) {
-            for (int i = 0; i < 2 && tma.valid; ++i) {
-                issue(issued++, tma);
-                cur_next<GRAM>(a, tma);
-            }
+    if (tid == 0) {
+        TcCursor c;
+        cur_init<GRAM>(a, c);
+        for (uint32_t q = 0; q < 2 && c.valid; ++q) {
+            issue_raw(q, c);
+            cur_next<GRAM>(a, c);
         }
-        // the first super-chunk's exponent fields
-        load_exps(cons.w, cons.sk, 0);
-        prod_sync();
-        mbar_arrive(&exfull[0]);
-        uint32_t q = 0, t = 0, j = 0;  // raw stages, digit stages, super-chunks consumed
-        bool ok = true;
-        while (ok && cons.valid) {
-            const int ske = min(cons.w.ke, cons.sk + super_k);
-            if (cons.k0 == cons.sk) {
-                // at a super-chunk start: the next super-chunk's exponent fields
-                TcCursor nx = cons;
-                nx.k0 = ske - kTcRawK;  // the super-chunk's last raw stage
-                if (nx.k0 < nx.sk) nx.k0 = nx.sk;
-                cur_next<GRAM>(a, nx);
-                while (nx.valid && nx.k0 != nx.sk) cur_next<GRAM>(a, nx);
-                if (nx.valid) {
-                    const uint32_t b1 = (j + 1) % kTcExpSlots;
-                    // every producer wait is followed by a producer barrier and a
-                    // check of the abort flag, so that all producer warps leave
-                    // together (none is left waiting at a barrier the others skip)
-                    if (j + 1 >= kTcExpSlots)
-                        mbar_wait_warp(&exfree[b1], ((j + 1 - kTcExpSlots) / kTcExpSlots) & 1,
-                                       abort_flag, a.error);
-                    prod_sync();
-                    if (*abort_flag) break;
-                    load_exps(nx.w, nx.sk, b1);
-                    prod_sync();
-                    mbar_arrive(&exfull[b1]);
-                }
-            }
-            const uint32_t r = q & 1;
-            mbar_wait_warp(&rfull[r], (q >> 1) & 1, abort_flag, a.error);
-            const uint8_t *raw = sm + L::raw_off + r * L::raw_bytes;
-            const int *ebuf_a = ea + (j % kTcExpSlots) * kTcM;
-            const int *ebuf_b = eb + (j % kTcExpSlots) * BN;
-            const int nd = min(2, (ske - cons.k0 + kTcStageK - 1) / kTcStageK);
-            for (int dd = 0; dd < nd; ++dd, ++t) {
-                const uint32_t s = t & 1;
-                mbar_wait_warp(&empty[s], ((t >> 1) & 1) ^ 1, abort_flag, a.error);
-                prod_sync();
-                if (*abort_flag) {
-                    ok = false;
-                    break;
-                }
-                uint8_t *abuf = sm + L::dig_off + s * L::stage_bytes;
-                uint8_t *bbuf = abuf + L::a_bytes;
-                if (!GRAM) {
-                    // the right operand's prepared planes of this digit stage, from
-                    // the raw stage (the digit stage's full barrier covers them like
-                    // the producers' own stores)
-                    const uint4 *src =
-                        reinterpret_cast<const uint4 *>(raw + L::a_box + dd * L::b_box);
-                    uint4 *dst = reinterpret_cast<uint4 *>(bbuf);
-                    for (int i = p; i < (int)(L::b_bytes / 16); i += kTcProdThreads)
-                        dst[i] = src[i];
-                }
-                // digit planes of this 16-k half of the raw stage, two items
-                // at a time (independent instruction streams)
-                constexpr int a_items = kTcM * kTcKGroups;
-                constexpr int b_items = GRAM ? BN * kTcKGroups : 0;
-                constexpr int n_items = a_items + b_items;
-                for (int item0 = p; item0 < n_items; item0 += 2 * kTcProdThreads) {
-                    double v[2][8];
-                    int em[2] = {1, 1};
-                    uint8_t *dstb[2] = {nullptr, nullptr};
-                    uint32_t pl[2] = {0, 0};
-#pragma unroll
-                    for (int h = 0; h < 2; ++h) {
-                        const int item = item0 + h * kTcProdThreads;
-                        const bool live = item < n_items;
-                        const int it2 = live ? item : item0;
-                        const bool isb = it2 >= a_items;
-                        const int ii = isb ? it2 - a_items : it2;
-                        const int rows = isb ? BN : kTcM;
-                        const int rr = ii % rows, g = ii / rows;
-                        if (GRAM) {
-                            // box dd of the operand: rr's 16 k as 8 chunks of 16
-                            // bytes, chunk c stored at chunk c ^ (rr % 8)
-                            const uint8_t *box = raw + (isb ? 2 * L::a_box + dd * L::b_box
-                                                            : dd * L::a_box) +
-                                                 (uint32_t)rr * 128u;
-#pragma unroll
-                            for (int qq = 0; qq < 4; ++qq) {
-                                const int c = 4 * g + qq;
-                                const double2 u = *reinterpret_cast<const double2 *>(
-                                    box + (uint32_t)((c ^ (rr & 7)) << 4));
-                                v[h][2 * qq] = u.x;
-                                v[h][2 * qq + 1] = u.y;
-                            }
-                        } else {
-                            // box [32 k][128 rows]
-                            const double *col = reinterpret_cast<const double *>(raw) +
-                                                (size_t)(dd * kTcStageK + g * 8) * kTcM + rr;
-#pragma unroll
-                            for (int qq = 0; qq < 8; ++qq) v[h][qq] = col[(size_t)qq * kTcM];
-                        }
-                        em[h] = isb ? ebuf_b[rr] : ebuf_a[rr];
-                        if (live) {
-                            dstb[h] = (isb ? bbuf : abuf) +
-                                      (uint32_t)g * (isb ? tc_lbo_b(BN) : tc_lbo(kTcM)) +
-                                      (uint32_t)(rr >> 3) * 128u + (uint32_t)(rr & 7) * 16u;
-                            pl[h] = isb ? (uint32_t)BN * 16u : tc_plane(kTcM);
-                        }
-                    }
-#pragma unroll
-                    for (int h = 0; h < 2; ++h) {
-                        if (dstb[h] == nullptr) continue;
-                        uint4 dg[kTcDigits];
-                        tc_digits8(v[h], em[h], dg);
-#pragma unroll
-                        for (int i = 0; i < kTcDigits; ++i)
-                            *reinterpret_cast<uint4 *>(dstb[h] + (uint32_t)i * pl[h]) = dg[i];
-                    }
-                }
-                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-                mbar_arrive(&full[s]);
-            }
-            if (!ok) break;
-            // raw buffer r is read: refill it with raw stage q + 2
-            prod_sync();
-            if (*abort_flag) break;
-            if (p == 0 && tma.valid) {
-                issue(issued++, tma);
-                cur_next<GRAM>(a, tma);
-            }
-            ++q;
-            const int sk_before = cons.sk, it_before = cons.it;
-            cur_next<GRAM>(a, cons);
-            if (cons.valid && (cons.sk != sk_before || cons.it != it_before)) ++j;
-        }
-        // raw stages still in flight (an abort) land before the CTA exits
-        if (pw == 0)
-            for (uint32_t qq = q; qq < issued; ++qq)
-                mbar_wait_teardown(&rfull[qq & 1], (qq >> 1) & 1);
     }
 
+    // Work units of a digit stage: core matrices (8 rows x 8 k), one pair of
+    // consecutive k per lane: lane = 8 pp + r, row r of the core matrix, k
+    // pair pp.  The 4-byte digit stores of a warp fill one 128-byte line,
+    // and the 16-byte reads of a quarter-warp from a swizzled box (row r's
+    // chunk 4 g + pp at (4 g + pp) ^ r) hit distinct banks.  Warp w converts
+    // the left operand's row group w in both k-groups; the right operand's
+    // units (Gram) rotate over the warps from stage to stage.
+    const int r7 = lane & 7, pp = lane >> 3;
+    const int ra = warp * 8 + r7;  // left-operand row of this thread
+    const uint32_t a_dst = (uint32_t)warp * 128u + (uint32_t)r7 * 16u + (uint32_t)pp * 4u;
+    constexpr int BU = BN / 4;  // right-operand units: BN / 8 row groups x 2 k-groups
+    // drain slice: row q 32 + lane, columns [cp CPW, (cp + 1) CPW)
+    constexpr int CPW = BN / 4;
+    const int q = warp & 3, cp = warp >> 2;
+    const int drow = q * 32 + lane;
+    // per column the level sums of the current super-chunk, sum over l of
+    // L_l 2^(8 (6 - l)), as a 96-bit integer (w0 least significant)
+    uint32_t w0[CPW], w1[CPW], w2[CPW];
+#pragma unroll
+    for (int c = 0; c < CPW; ++c) w0[c] = w1[c] = w2[c] = 0;
+
+    // the next chunk to drain: work item, super-chunk start, chunk start,
+    // index of its last digit stage
+    TcItem dw{0, 0, 0, 0};
+    int dit = blockIdx.x, dsk = 0, dk0 = 0, dlast = 0;
+    bool dvalid = dit < a.items;
+    uint32_t dn = 0;  // chunks drained
+    auto dstages = [&]() { return min(kTcDrainStages, (dw.ke - dk0 + kTcStageK - 1) / kTcStageK); };
+    if (dvalid) {
+        dw = tc_item<GRAM>(a, dit);
+        dsk = dk0 = dw.kb;
+        dlast = dstages() - 1;
+    }
+    auto drain = [&]() -> bool {
+        if (!mbar_wait_warp(accf, dn & 1, abort_flag, a.error)) return false;
+        tc_fence_after();
+        const uint32_t tb = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(cp * CPW);
+#pragma unroll
+        for (int l = 0; l < kTcDigits; ++l) {
+            uint32_t v[CPW / 4][4];
+#pragma unroll
+            for (int j = 0; j < CPW / 4; ++j) tc_ld4(tb + (uint32_t)(l * BN + 4 * j), v[j]);
+            tc_wait_ld();
+#pragma unroll
+            for (int c = 0; c < CPW; ++c)
+                tc_acc_level(w0[c], w1[c], w2[c], __float2int_rn(__uint_as_float(v[c >> 2][c & 3])),
+                             l);
+        }
+        ++dn;
+        const int ske = min(dw.ke, dsk + super_k);
+        if (dk0 + kTcDrainK >= ske) {
+            // the super-chunk ends: its sums, w 2^(er + ec - 2108)
+            // converted with integer instructions, go into the work item's
+            // split-k partial (Gram; FP64 accumulators for a work item of
+            // several super-chunks) or straight into Y (a linear combination)
+            const int sidx = (dsk - (GRAM ? 0 : dw.kb)) / super_k;
+            const int grow = dw.mt0 + drow;
+            const int er = grow < a.M ? __ldg(a.eA + (size_t)sidx * a.M + grow) : 1;
+            const bool first = dsk == dw.kb, last = dsk + super_k >= dw.ke;
+            const int z = dit / (a.mtiles * a.ntiles);
+#pragma unroll
+            for (int c = 0; c < CPW; ++c) {
+                const int col = cp * CPW + c, gcol = dw.nt * BN + col;
+                const int ec = GRAM ? (gcol < a.N ? __ldg(a.eB + (size_t)sidx * a.N + gcol) : 1)
+                                    : __ldg(a.eB + ((size_t)dw.nt * a.nsup + sidx) * BN + col);
+                const double val = (er == 0x7FF || ec == 0x7FF)
+                                       ? __longlong_as_double(0x7FF8000000000000LL)
+                                       : tc_i128_f64((long long)(int)w2[c],
+                                                     ((unsigned long long)w1[c] << 32) | w0[c],
+                                                     er + ec - 2108);
+                w0[c] = w1[c] = w2[c] = 0;
+                if (GRAM) {
+                    double r = val;
+                    if (!(first && last)) {
+                        double &A = acc[col * kTcM + drow];
+                        if (!first) r += A;
+                        A = r;
+                    }
+                    if (last && grow < a.M && gcol < a.N)
+                        a.out[(size_t)z * a.M * a.N + grow + (size_t)gcol * a.M] = r;
+                } else if (grow < a.M && gcol < a.N) {
+                    double *dst = a.out + grow + (size_t)gcol * a.ldo;
+                    double y = a.alpha == 1.0 ? val : a.alpha * val;
+                    if (a.accumulate) {
+                        y += *dst;
+                    } else if (a.beta != nullptr) {
+                        const double bb = a.beta[a.incb == 0 ? 0 : (size_t)gcol * a.incb];
+                        if (bb != 0.0) y = fma(bb, *dst, y);
+                    }
+                    *dst = y;
+                }
+            }
+        }
+        // the next chunk
+        const int tnext = dlast + 1;
+        dk0 += kTcDrainK;
+        if (dk0 >= ske) {
+            dsk += super_k;
+            if (dsk >= dw.ke) {
+                dit += gridDim.x;
+                dvalid = dit < a.items;
+                if (dvalid) {
+                    dw = tc_item<GRAM>(a, dit);
+                    dsk = dw.kb;
+                }
+            }
+            dk0 = dsk;
+        }
+        if (dvalid) dlast = tnext + dstages() - 1;
+        return true;
+    };
+
+    // ---- production
+    TcCursor cons;
+    cur_init<GRAM>(a, cons);
+    int t = 0;        // digit stages produced
+    uint32_t qr = 0;  // raw stages read
+    int em_a = 1;
+    bool ok = true;
+    while (ok && cons.valid) {
+        const int ske = min(cons.w.ke, cons.sk + super_k);
+        const int sidx = (cons.sk - (GRAM ? 0 : cons.w.kb)) / super_k;
+        if (cons.k0 == cons.sk) {
+            // a super-chunk starts: the exponent field of this thread's row
+            const int gr = cons.w.mt0 + ra;
+            em_a = gr < a.M ? __ldg(a.eA + (size_t)sidx * a.M + gr) : 1;
+        }
+        const uint32_t r = qr & 1;
+        const uint8_t *raw = sm + L::raw_off + r * L::raw_bytes;
+        const int nd = min(2, (ske - cons.k0 + kTcStageK - 1) / kTcStageK);
+        for (int dd = 0; dd < nd; ++dd, ++t) {
+            const uint32_t s = t & 1;
+            // the right-operand unit of this warp at stage t (Gram): unit b goes
+            // to warp (b + t BU) mod 16
+            const int bu = (warp - (int)(((uint32_t)t * BU) & 15u)) & 15;
+            const bool hasb = GRAM && bu < BU;
+            const int rb = (bu >> 1) * 8 + r7, gb = bu & 1;
+            int emb = 1;
+            if (hasb) {
+                const int gc = cons.w.nt * BN + rb;
+                emb = gc < a.N ? __ldg(a.eB + (size_t)sidx * a.N + gc) : 1;
+            }
+            if (dd == 0 && !mbar_wait_warp(&rfull[r], (qr >> 1) & 1, abort_flag, a.error)) {
+                ok = false;
+                break;
+            }
+            if (t >= 2 && !mbar_wait_warp(&empty[s], ((t >> 1) & 1) ^ 1, abort_flag, a.error)) {
+                ok = false;
+                break;
+            }
+            uint8_t *abuf = sm + L::dig_off + s * L::stage_bytes;
+            uint8_t *bbuf = abuf + L::a_bytes;
+            if (!GRAM) {
+                // the right operand's prepared planes of this digit stage, from
+                // the raw stage
+                const uint4 *src = reinterpret_cast<const uint4 *>(raw + L::a_box + dd * L::b_box);
+                uint4 *dst = reinterpret_cast<uint4 *>(bbuf);
+                for (int i = tid; i < (int)(L::b_bytes / 16); i += kTcThreads) dst[i] = src[i];
+            }
+            // the pairs: left operand k-groups 0 and 1, and the right-operand unit
+            double2 v0, v1, vb = make_double2(0.0, 0.0);
+            if (GRAM) {
+                // box dd: row ra's 16 k as 8 chunks of 16 bytes, chunk c at c ^ (ra % 8)
+                const uint8_t *box = raw + dd * L::a_box + (uint32_t)ra * 128u;
+                v0 = *reinterpret_cast<const double2 *>(box + ((uint32_t)(pp ^ r7) << 4));
+                v1 = *reinterpret_cast<const double2 *>(box + ((uint32_t)((4 + pp) ^ r7) << 4));
+                if (hasb) {
+                    const uint8_t *bx = raw + 2 * L::a_box + dd * L::b_box + (uint32_t)rb * 128u;
+                    vb = *reinterpret_cast<const double2 *>(
+                        bx + ((uint32_t)((4 * gb + pp) ^ r7) << 4));
+                }
+            } else {
+                // box [32 k][128 rows]
+                const double *col = reinterpret_cast<const double *>(raw) +
+                                    (size_t)(dd * kTcStageK + 2 * pp) * kTcM + ra;
+                v0 = make_double2(col[0], col[kTcM]);
+                v1 = make_double2(col[8 * kTcM], col[9 * kTcM]);
+            }
+            // row groups past the operand's last row hold zero digits: the
+            // conversion is skipped (warp-uniform)
+            const bool live_a = cons.w.mt0 + warp * 8 < a.M;
+            const bool live_b = !GRAM || cons.w.nt * BN + (bu >> 1) * 8 < a.N;
+            uint32_t d0[kTcDigits], d1[kTcDigits], db[kTcDigits];
+#pragma unroll
+            for (int i = 0; i < kTcDigits; ++i) d0[i] = d1[i] = db[i] = 0u;
+            if (live_a) {
+                tc_digit_pair(v0.x, v0.y, (uint32_t)em_a, d0);
+                tc_digit_pair(v1.x, v1.y, (uint32_t)em_a, d1);
+            }
+            if (hasb && live_b) tc_digit_pair(vb.x, vb.y, (uint32_t)emb, db);
+#pragma unroll
+            for (int i = 0; i < kTcDigits; ++i) {
+                uint8_t *pa = abuf + (uint32_t)i * tc_plane(kTcM) + a_dst;
+                *reinterpret_cast<uint32_t *>(pa) = d0[i];
+                *reinterpret_cast<uint32_t *>(pa + tc_lbo(kTcM)) = d1[i];
+            }
+            if (hasb) {
+                const uint32_t b_dst = (uint32_t)gb * tc_lbo_b(BN) + (uint32_t)(bu >> 1) * 128u +
+                                       (uint32_t)r7 * 16u + (uint32_t)pp * 4u;
+#pragma unroll
+                for (int i = 0; i < kTcDigits; ++i)
+                    *reinterpret_cast<uint32_t *>(bbuf + b_dst + (uint32_t)i * BN * 16u) = db[i];
+            }
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            // chunks that ended at stage t - 1 or earlier
+            while (dvalid && dlast < t) {
+                if (!drain()) {
+                    ok = false;
+                    break;
+                }
+            }
+            if (!ok) break;
+            // arrival; the last warp issues the stage's MMAs
+            tc_fence_before();
+            __syncwarp();
+            if (lane == 0 && smem_arrive(&fcnt[s]) == kTcWarps - 1) {
+                fcnt[s] = 0;
+                tc_fence_after();
+                const int k = cons.k0 + dd * kTcStageK;
+                const int cs = cons.sk + (k - cons.sk) / kTcDrainK * kTcDrainK;
+                issue_mma(s, (k - cs) / kTcStageK, k + kTcStageK >= min(cs + kTcDrainK, ske));
+                atomicMax(n_stages, t + 1);
+            }
+            __syncwarp();
+        }
+        if (!ok) break;
+        // raw stage qr is read; the last warp copies raw stage qr + 2 into its buffer
+        __syncwarp();
+        if (lane == 0 && smem_arrive(&rcnt[r]) == kTcWarps - 1) {
+            rcnt[r] = 0;
+            TcCursor c2 = cons;
+            cur_next<GRAM>(a, c2);
+            if (c2.valid) cur_next<GRAM>(a, c2);
+            if (c2.valid) issue_raw(qr + 2, c2);
+        }
+        __syncwarp();
+        ++qr;
+        cur_next<GRAM>(a, cons);
+    }
+    // the remaining chunks
+    while (ok && dvalid)
+        if (!drain()) ok = false;
+
+    // teardown: the MMAs and bulk copies still in flight (after an abort, or
+    // the last stages' MMAs nobody waited for) complete before tensor memory
+    // is freed and the CTA exits
     tc_fence_before();
     __syncthreads();
     if (warp == 0) {
+        const int ns = *n_stages, nc = *n_chunks, nr = *n_raw;
+        for (int tt = max(ns - 2, 0); tt < ns; ++tt)
+            mbar_wait_teardown(&empty[tt & 1], (tt >> 1) & 1);
+        if (nc > 0) mbar_wait_teardown(accf, (nc - 1) & 1);
+        for (int qq = max(nr - 2, 0); qq < nr; ++qq)
+            mbar_wait_teardown(&rfull[qq & 1], (qq >> 1) & 1);
         tc_fence_after();
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
                      "r"(kTcTmemCols)
@@ -849,18 +886,26 @@ __global__ void __launch_bounds__(kTcThreads, 1)
 // Exponent fields for the Gram operands: out[s * ncols + c] = the largest
 // exponent field (at least 1) of column c of X (n x ncols, leading dimension
 // ld, 16-byte aligned columns) over rows [s super, (s + 1) super).  One warp
-// per (super-chunk, column), 16-byte loads.
+// per (column, piece of at most kTcExpPiece rows of one window), 16-byte
+// loads, merged with atomicMax into `out`, which starts at 0.
+constexpr int kTcExpPiece = 4096;
 __global__ void __launch_bounds__(256) k_tc_expcols(const double *__restrict__ X, size_t ld,
                                                     int n, int ncols, int super, int nsup,
                                                     int *__restrict__ out) {
     const int lane = threadIdx.x & 31;
+    const int pieces = (super + kTcExpPiece - 1) / kTcExpPiece;  // per window
+    const long long units = (long long)nsup * pieces * ncols;
     const long long nw = (long long)gridDim.x * 8;
-    for (long long wid = (long long)blockIdx.x * 8 + (threadIdx.x >> 5);
-         wid < (long long)nsup * ncols; wid += nw) {
-        const int c = (int)(wid / nsup), s = (int)(wid % nsup);
-        const int r0 = s * super, r1 = min(n, r0 + super);
+    for (long long wid = (long long)blockIdx.x * 8 + (threadIdx.x >> 5); wid < units; wid += nw) {
+        const int c = (int)(wid % ncols);
+        const long long sp = wid / ncols;
+        const int s = (int)(sp / pieces), pc = (int)(sp % pieces);
+        const int r0 = s * super + pc * kTcExpPiece;
+        const int r1 = (int)std::min<long long>(std::min<long long>(n, (long long)(s + 1) * super),
+                                                r0 + kTcExpPiece);
         const double *col = X + (size_t)c * ld;
         int em = 1;
+#pragma unroll 4
         for (int r = r0 + 2 * lane; r < r1; r += 64) {
             if (r + 1 < r1) {
                 const double2 u = __ldg(reinterpret_cast<const double2 *>(col + r));
@@ -870,13 +915,12 @@ __global__ void __launch_bounds__(256) k_tc_expcols(const double *__restrict__ X
             }
         }
         em = (int)__reduce_max_sync(0xffffffffu, (unsigned)em);
-        if (lane == 0) out[(size_t)s * ncols + c] = em;
+        if (lane == 0) {
+            if (pieces == 1) out[(size_t)s * ncols + c] = em;
+            else atomicMax(out + (size_t)s * ncols + c, em);
+        }
     }
 }
-
-// Exponent fields for the left operand of a linear combination:
-// out[s * n + r] = the largest exponent field (at least 1) of row r of X
-// (n x K, leading dimension ld) over columns [s super, (s + 1) super).
 __global__ void __launch_bounds__(256) k_tc_exprows(const double *__restrict__ X, size_t ld,
                                                     int n, int K, int super,
                                                     int *__restrict__ out) {
@@ -1102,30 +1146,38 @@ void tc_gram(int n, int m, int w, const double *Q, int ldq, const double *P, int
     a.K = n;
     a.A = Q;
     a.lda = (size_t)ldq;
-    a.super_k = kTcSuperGram;
     a.mtiles = (m + kTcM - 1) / kTcM;
     a.ntiles = (w + bn - 1) / bn;
     const int mn = a.mtiles * a.ntiles;
     const int sms = device_sms();
-    // exponent fields of both operands per 384-row super-chunk
-    const int nsup = (n + kTcSuperGram - 1) / kTcSuperGram;
+    // one wave of one CTA per SM over all work items (k ranges of a multiple
+    // of the drain chunk), fewer and longer ranges until the partials fit
+    // the scratch
+    int z = std::max(1, sms / mn);
+    long long kc = ((long long)(n + z - 1) / z + kTcDrainK - 1) / kTcDrainK * kTcDrainK;
+    GCGE_REQUIRE((size_t)m * w <= scratch_elems, GCGE_ERR_ARG, "tc_gram: scratch too small");
+    while ((size_t)((n + kc - 1) / kc) * m * w > scratch_elems) kc *= 2;
+    // the exponent window: the whole k range of a work item (one super-chunk),
+    // or super-chunks of the largest window when the range is longer.  One
+    // exponent per column over K rows bounds the error of an entry by
+    // 2^-54 sqrt(K) |x| |y|, below the FP64 dot product's K 2^-53 |x| |y|.
+    if (kc > kTcSuperGramMax) kc = (kc + kTcSuperGramMax - 1) / kTcSuperGramMax * kTcSuperGramMax;
+    const int super_k = (int)std::min<long long>(kc, kTcSuperGramMax);
+    z = (int)((n + kc - 1) / kc);
+    a.super_k = super_k;
+    const int nsup = (n + super_k - 1) / super_k;
     DevBuf<int> &eb = slot_stage().tc_exps;
     eb.alloc((size_t)nsup * (m + w));
     int *eA = eb.p, *eB = eb.p + (size_t)nsup * m;
-    const int gx = std::min<long long>(4 * sms, ((long long)nsup * std::max(m, w) + 7) / 8);
-    k_tc_expcols<<<gx, 256, 0, st>>>(Q, (size_t)ldq, n, m, kTcSuperGram, nsup, eA);
-    k_tc_expcols<<<gx, 256, 0, st>>>(P, (size_t)ldp, n, w, kTcSuperGram, nsup, eB);
+    const long long pieces = (super_k + kTcExpPiece - 1) / kTcExpPiece;
+    if (pieces > 1) GCGE_CUDA(cudaMemsetAsync(eb.p, 0, sizeof(int) * (size_t)nsup * (m + w), st));
+    const int gx = (int)std::min<long long>(8 * sms, (nsup * pieces * std::max(m, w) + 7) / 8);
+    k_tc_expcols<<<gx, 256, 0, st>>>(Q, (size_t)ldq, n, m, super_k, nsup, eA);
+    k_tc_expcols<<<gx, 256, 0, st>>>(P, (size_t)ldp, n, w, super_k, nsup, eB);
     GCGE_CHECK_LAUNCH();
     count_launch(2);
     a.eA = eA;
     a.eB = eB;
-    // one wave of one CTA per SM over all work items
-    int z = std::max(1, sms / mn);
-    long long kc = ((long long)(n + z - 1) / z + kTcSuperGram - 1) / kTcSuperGram * kTcSuperGram;
-    GCGE_REQUIRE((size_t)m * w <= scratch_elems, GCGE_ERR_ARG, "tc_gram: scratch too small");
-    // fewer, longer k ranges until the partials fit the scratch
-    while ((size_t)((n + kc - 1) / kc) * m * w > scratch_elems) kc *= 2;
-    z = (int)((n + kc - 1) / kc);
     a.kchunk = (int)kc;
     a.items = z * mn;
     a.out = scratch;

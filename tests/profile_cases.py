@@ -121,7 +121,9 @@ def eig():
 # long-dimension product shapes of the mixed solves: (kind, n, m, w)
 PROD_SHAPES = [("gram", 262144, 180, 20), ("lincomb", 262144, 180, 20),
                ("gram", 2097152, 360, 40), ("lincomb", 2097152, 360, 40),
-               ("gram", 2097152, 400, 40), ("lincomb", 2097152, 400, 320)]
+               ("gram", 2097152, 400, 40), ("lincomb", 2097152, 400, 320),
+               ("gram", 2097152, 320, 40), ("gram", 2097152, 40, 40),
+               ("lincomb", 2097152, 400, 200), ("lincomb", 2097152, 80, 40)]
 
 
 def prodbench():
