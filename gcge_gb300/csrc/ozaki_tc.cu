@@ -61,8 +61,8 @@ constexpr int kTcRawK = 32;    // k per raw (TMA) stage: two digit stages
 constexpr int kTcDrainStages = 6;
 constexpr int kTcDrainK = kTcStageK * kTcDrainStages;  // 96: exact FP32 level sums
 constexpr int kTcKGroups = kTcStageK / 8;              // core matrices along k per stage
-constexpr int kTcWarps = 16;  // every warp converts digits and drains
-constexpr int kTcThreads = kTcWarps * 32;
+constexpr int kTcWarps = 16;  // worker warps: digit conversion and drain
+constexpr int kTcThreads = (kTcWarps + 1) * 32;  // and one warp issuing the MMAs
 constexpr uint32_t kTcTmemCols = 512;
 // bounded mbarrier waits: 4 s of device clock, or this many suspended tests
 constexpr unsigned long long kTcWaitNs = 4000000000ull;
@@ -113,10 +113,9 @@ struct TcLayout {
     static constexpr uint32_t acc_off = dig_off + 2 * stage_bytes;  // double acc[BN][kTcM]
     static constexpr uint32_t bar_off =
         tc_round(acc_off + (GRAM ? (uint32_t)BN * kTcM * 8 : 0u), 16);
-    // mbarriers empty[2] rfull[2] accf
-    static constexpr int nbars = 5;
-    // tmem slot, abort flag, arrival counters full[2] and rempty[2], digit
-    // stages issued, drain chunks committed, raw stages issued
+    // mbarriers empty[2] rfull[2] accf full[2] fin
+    static constexpr int nbars = 8;
+    // tmem slot, abort flag, arrival counters rempty[2], raw stages issued
     static constexpr uint32_t misc_off = bar_off + nbars * 8;
     static constexpr uint32_t bytes = misc_off + 48;
     static constexpr uint32_t alloc_bytes = bytes + 1024;  // room to align the base
@@ -364,10 +363,6 @@ __device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap *map
         : "memory");
 }
 
-// exact int64 -> double for |t| < 2^51
-__device__ __forceinline__ double tc_i64_to_f64(long long t) {
-    return __longlong_as_double(t + 0x4338000000000000LL) - 6755399441055744.0;
-}
 
 // (vh 2^64 + vl) 2^e as a double, rounded to nearest (ties to even), with
 // integer instructions only (FP64 arithmetic is a slow pipe on this part).
@@ -499,21 +494,23 @@ __device__ __forceinline__ void cur_next(const TcArgs &a, TcCursor &c) {
 }
 
 // ---------------------------------------------------------------- kernel
-// All 16 warps do the same work.  Per digit stage a thread converts one item
-// (4 consecutive k of one row) of the left operand and, for a Gram, the right
-// operand's items of the warps whose turn it is (those rotate over the warps
-// from stage to stage); after each drain chunk it moves its slice of the
-// level accumulators (tensor-memory lane quarter warp % 4, BN / 4 columns)
-// into 64-bit integers, and after a super-chunk it folds them into FP64.
-// The last warp to finish a digit stage issues its MMAs; the last to finish
-// reading a raw stage issues the bulk copies of the raw stage two ahead into
-// its buffer.
+// Warps 0 .. 15 are the workers.  Per digit stage a worker thread converts
+// one pair of consecutive k in each of two core matrices of the left operand
+// and, for a Gram, one of the right operand's when it is its warp's turn (those
+// rotate over the warps from stage to stage); after each drain chunk it moves
+// its slice of the level accumulators (tensor-memory lane quarter warp % 4,
+// BN / 4 columns) into 96-bit integers, and after an exponent window it folds
+// them into FP64.  The last worker to finish reading a raw stage issues the
+// bulk copies of the raw stage two ahead into its buffer.  Warp 16 issues the
+// MMAs of each digit stage once every worker has finished it (a dedicated
+// warp: the issue blocks while the tensor core works through the previous
+// stage, ~700 cycles of MMAs per stage).
 //
 // The waits form no cycle: digit stage t is produced after the MMAs of stage
-// t - 2 completed (a ring of two digit stages); a warp drains the chunk that
+// t - 2 completed (a ring of two digit stages); a worker drains the chunk that
 // ends at stage e before it finishes stage e + 1, so the MMAs of stage e + 1,
 // the next chunk's first (which overwrite the accumulators), are issued after
-// every warp drained it.
+// every worker drained it.
 template <int BN, bool GRAM>
 __global__ void __launch_bounds__(kTcThreads, 1)
     k_tc_digits(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB,
@@ -525,14 +522,13 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     uint8_t *sm = sm_raw + ((1024u - (su32(sm_raw) & 1023u)) & 1023u);
     double *acc = reinterpret_cast<double *>(sm + L::acc_off);  // [BN][kTcM]
     uint64_t *bars = reinterpret_cast<uint64_t *>(sm + L::bar_off);
-    uint64_t *empty = bars, *rfull = bars + 2, *accf = bars + 4;
+    uint64_t *empty = bars, *rfull = bars + 2, *accf = bars + 4, *full = bars + 5;
+    uint64_t *fin = bars + 7;
     uint32_t *misc = reinterpret_cast<uint32_t *>(sm + L::misc_off);
     uint32_t *tmem_slot = misc;
     volatile int *abort_flag = reinterpret_cast<volatile int *>(misc + 1);
-    uint32_t *fcnt = misc + 2, *rcnt = misc + 4;
-    int *n_stages = reinterpret_cast<int *>(misc + 6);  // digit stages issued
-    int *n_chunks = reinterpret_cast<int *>(misc + 7);  // drain chunks committed
-    int *n_raw = reinterpret_cast<int *>(misc + 8);     // raw stages issued
+    uint32_t *rcnt = misc + 2;
+    int *n_raw = reinterpret_cast<int *>(misc + 4);  // raw stages issued
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const uint32_t sbase = su32(sm);
     const int super_k = a.super_k;
@@ -541,11 +537,13 @@ __global__ void __launch_bounds__(kTcThreads, 1)
         for (int s = 0; s < 2; ++s) {
             mbar_init(&empty[s], 1);
             mbar_init(&rfull[s], 1);
-            fcnt[s] = rcnt[s] = 0;
+            mbar_init(&full[s], kTcWarps);
+            rcnt[s] = 0;
         }
         mbar_init(accf, 1);
+        mbar_init(fin, 1);
         *abort_flag = 0;
-        *n_stages = *n_chunks = *n_raw = 0;
+        *n_raw = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     if (warp == 0) {
@@ -606,274 +604,287 @@ __global__ void __launch_bounds__(kTcThreads, 1)
             }
         }
         tc_commit(&empty[s]);
-        if (last_of_chunk) {
-            tc_commit(accf);
-            atomicAdd(n_chunks, 1);
-        }
+        if (last_of_chunk) tc_commit(accf);
     };
 
-    if (tid == 0) {
-        TcCursor c;
-        cur_init<GRAM>(a, c);
-        for (uint32_t q = 0; q < 2 && c.valid; ++q) {
-            issue_raw(q, c);
-            cur_next<GRAM>(a, c);
-        }
-    }
-
-    // Work units of a digit stage: core matrices (8 rows x 8 k), one pair of
-    // consecutive k per lane: lane = 8 pp + r, row r of the core matrix, k
-    // pair pp.  The 4-byte digit stores of a warp fill one 128-byte line,
-    // and the 16-byte reads of a quarter-warp from a swizzled box (row r's
-    // chunk 4 g + pp at (4 g + pp) ^ r) hit distinct banks.  Warp w converts
-    // the left operand's row group w in both k-groups; the right operand's
-    // units (Gram) rotate over the warps from stage to stage.
-    const int r7 = lane & 7, pp = lane >> 3;
-    const int ra = warp * 8 + r7;  // left-operand row of this thread
-    const uint32_t a_dst = (uint32_t)warp * 128u + (uint32_t)r7 * 16u + (uint32_t)pp * 4u;
-    constexpr int BU = BN / 4;  // right-operand units: BN / 8 row groups x 2 k-groups
-    // drain slice: row q 32 + lane, columns [cp CPW, (cp + 1) CPW)
-    constexpr int CPW = BN / 4;
-    const int q = warp & 3, cp = warp >> 2;
-    const int drow = q * 32 + lane;
-    // per column the level sums of the current super-chunk, sum over l of
-    // L_l 2^(8 (6 - l)), as a 96-bit integer (w0 least significant)
-    uint32_t w0[CPW], w1[CPW], w2[CPW];
-#pragma unroll
-    for (int c = 0; c < CPW; ++c) w0[c] = w1[c] = w2[c] = 0;
-
-    // the next chunk to drain: work item, super-chunk start, chunk start,
-    // index of its last digit stage
-    TcItem dw{0, 0, 0, 0};
-    int dit = blockIdx.x, dsk = 0, dk0 = 0, dlast = 0;
-    bool dvalid = dit < a.items;
-    uint32_t dn = 0;  // chunks drained
-    auto dstages = [&]() { return min(kTcDrainStages, (dw.ke - dk0 + kTcStageK - 1) / kTcStageK); };
-    if (dvalid) {
-        dw = tc_item<GRAM>(a, dit);
-        dsk = dk0 = dw.kb;
-        dlast = dstages() - 1;
-    }
-    auto drain = [&]() -> bool {
-        if (!mbar_wait_warp(accf, dn & 1, abort_flag, a.error)) return false;
-        tc_fence_after();
-        const uint32_t tb = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(cp * CPW);
-#pragma unroll
-        for (int l = 0; l < kTcDigits; ++l) {
-            uint32_t v[CPW / 4][4];
-#pragma unroll
-            for (int j = 0; j < CPW / 4; ++j) tc_ld4(tb + (uint32_t)(l * BN + 4 * j), v[j]);
-            tc_wait_ld();
-#pragma unroll
-            for (int c = 0; c < CPW; ++c)
-                tc_acc_level(w0[c], w1[c], w2[c], __float2int_rn(__uint_as_float(v[c >> 2][c & 3])),
-                             l);
-        }
-        ++dn;
-        const int ske = min(dw.ke, dsk + super_k);
-        if (dk0 + kTcDrainK >= ske) {
-            // the super-chunk ends: its sums, w 2^(er + ec - 2108)
-            // converted with integer instructions, go into the work item's
-            // split-k partial (Gram; FP64 accumulators for a work item of
-            // several super-chunks) or straight into Y (a linear combination)
-            const int sidx = (dsk - (GRAM ? 0 : dw.kb)) / super_k;
-            const int grow = dw.mt0 + drow;
-            const int er = grow < a.M ? __ldg(a.eA + (size_t)sidx * a.M + grow) : 1;
-            const bool first = dsk == dw.kb, last = dsk + super_k >= dw.ke;
-            const int z = dit / (a.mtiles * a.ntiles);
-#pragma unroll
-            for (int c = 0; c < CPW; ++c) {
-                const int col = cp * CPW + c, gcol = dw.nt * BN + col;
-                const int ec = GRAM ? (gcol < a.N ? __ldg(a.eB + (size_t)sidx * a.N + gcol) : 1)
-                                    : __ldg(a.eB + ((size_t)dw.nt * a.nsup + sidx) * BN + col);
-                const double val = (er == 0x7FF || ec == 0x7FF)
-                                       ? __longlong_as_double(0x7FF8000000000000LL)
-                                       : tc_i128_f64((long long)(int)w2[c],
-                                                     ((unsigned long long)w1[c] << 32) | w0[c],
-                                                     er + ec - 2108);
-                w0[c] = w1[c] = w2[c] = 0;
-                if (GRAM) {
-                    double r = val;
-                    if (!(first && last)) {
-                        double &A = acc[col * kTcM + drow];
-                        if (!first) r += A;
-                        A = r;
+    if (warp == kTcWarps) {
+        // ------------------------------------------------------------ MMA issuer
+        uint32_t t = 0;  // digit stages issued
+        bool ok = true;
+        for (int it = blockIdx.x; it < a.items && ok; it += gridDim.x) {
+            const TcItem w = tc_item<GRAM>(a, it);
+            for (int k0 = w.kb; k0 < w.ke && ok; k0 += kTcDrainK) {
+                const int nst = min(kTcDrainStages, (w.ke - k0 + kTcStageK - 1) / kTcStageK);
+                for (int st = 0; st < nst; ++st, ++t) {
+                    const uint32_t s = t & 1;
+                    // every worker finished the stage (and drained the previous
+                    // chunk before the first stage of this one)
+                    if (!mbar_wait_warp(&full[s], (t >> 1) & 1, abort_flag, a.error)) {
+                        ok = false;
+                        break;
                     }
-                    if (last && grow < a.M && gcol < a.N)
-                        a.out[(size_t)z * a.M * a.N + grow + (size_t)gcol * a.M] = r;
-                } else if (grow < a.M && gcol < a.N) {
-                    double *dst = a.out + grow + (size_t)gcol * a.ldo;
-                    double y = a.alpha == 1.0 ? val : a.alpha * val;
-                    if (a.accumulate) {
-                        y += *dst;
-                    } else if (a.beta != nullptr) {
-                        const double bb = a.beta[a.incb == 0 ? 0 : (size_t)gcol * a.incb];
-                        if (bb != 0.0) y = fma(bb, *dst, y);
-                    }
-                    *dst = y;
+                    tc_fence_after();
+                    if (lane == 0) issue_mma(s, st, st == nst - 1);
+                    __syncwarp();
                 }
             }
         }
-        // the next chunk
-        const int tnext = dlast + 1;
-        dk0 += kTcDrainK;
-        if (dk0 >= ske) {
-            dsk += super_k;
-            if (dsk >= dw.ke) {
-                dit += gridDim.x;
-                dvalid = dit < a.items;
-                if (dvalid) {
-                    dw = tc_item<GRAM>(a, dit);
-                    dsk = dw.kb;
+        // all issued MMAs complete before tensor memory is freed
+        if (lane == 0) tc_commit(fin);
+        __syncwarp();
+        mbar_wait_teardown(fin, 0);
+    } else {
+        if (tid == 0) {
+            TcCursor c;
+            cur_init<GRAM>(a, c);
+            for (uint32_t q = 0; q < 2 && c.valid; ++q) {
+                issue_raw(q, c);
+                cur_next<GRAM>(a, c);
+            }
+        }
+
+        // Work units of a digit stage: core matrices (8 rows x 8 k), one pair of
+        // consecutive k per lane: lane = 8 pp + r, row r of the core matrix, k
+        // pair pp.  The 4-byte digit stores of a warp fill one 128-byte line,
+        // and the 16-byte reads of a quarter-warp from a swizzled box (row r's
+        // chunk 4 g + pp at (4 g + pp) ^ r) hit distinct banks.  Warp w converts
+        // the left operand's row group w in both k-groups; the right operand's
+        // units (Gram) rotate over the warps from stage to stage.
+        const int r7 = lane & 7, pp = lane >> 3;
+        const int ra = warp * 8 + r7;  // left-operand row of this thread
+        const uint32_t a_dst = (uint32_t)warp * 128u + (uint32_t)r7 * 16u + (uint32_t)pp * 4u;
+        constexpr int BU = BN / 4;  // right-operand units: BN / 8 row groups x 2 k-groups
+        // drain slice: row q 32 + lane, columns [cp CPW, (cp + 1) CPW)
+        constexpr int CPW = BN / 4;
+        const int q = warp & 3, cp = warp >> 2;
+        const int drow = q * 32 + lane;
+        // per column the level sums of the current super-chunk, sum over l of
+        // L_l 2^(8 (6 - l)), as a 96-bit integer (w0 least significant)
+        uint32_t w0[CPW], w1[CPW], w2[CPW];
+#pragma unroll
+        for (int c = 0; c < CPW; ++c) w0[c] = w1[c] = w2[c] = 0;
+
+        // the next chunk to drain: work item, super-chunk start, chunk start,
+        // index of its last digit stage
+        TcItem dw{0, 0, 0, 0};
+        int dit = blockIdx.x, dsk = 0, dk0 = 0, dlast = 0;
+        bool dvalid = dit < a.items;
+        uint32_t dn = 0;  // chunks drained
+        auto dstages = [&]() { return min(kTcDrainStages, (dw.ke - dk0 + kTcStageK - 1) / kTcStageK); };
+        if (dvalid) {
+            dw = tc_item<GRAM>(a, dit);
+            dsk = dk0 = dw.kb;
+            dlast = dstages() - 1;
+        }
+        auto drain = [&]() -> bool {
+            if (!mbar_wait_warp(accf, dn & 1, abort_flag, a.error)) return false;
+            tc_fence_after();
+            const uint32_t tb = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(cp * CPW);
+#pragma unroll
+            for (int l = 0; l < kTcDigits; ++l) {
+                uint32_t v[CPW / 4][4];
+#pragma unroll
+                for (int j = 0; j < CPW / 4; ++j) tc_ld4(tb + (uint32_t)(l * BN + 4 * j), v[j]);
+                tc_wait_ld();
+#pragma unroll
+                for (int c = 0; c < CPW; ++c)
+                    tc_acc_level(w0[c], w1[c], w2[c], __float2int_rn(__uint_as_float(v[c >> 2][c & 3])),
+                                 l);
+            }
+            ++dn;
+            const int ske = min(dw.ke, dsk + super_k);
+            if (dk0 + kTcDrainK >= ske) {
+                // the super-chunk ends: its sums, w 2^(er + ec - 2108)
+                // converted with integer instructions, go into the work item's
+                // split-k partial (Gram; FP64 accumulators for a work item of
+                // several super-chunks) or straight into Y (a linear combination)
+                const int sidx = (dsk - (GRAM ? 0 : dw.kb)) / super_k;
+                const int grow = dw.mt0 + drow;
+                const int er = grow < a.M ? __ldg(a.eA + (size_t)sidx * a.M + grow) : 1;
+                const bool first = dsk == dw.kb, last = dsk + super_k >= dw.ke;
+                const int z = dit / (a.mtiles * a.ntiles);
+#pragma unroll
+                for (int c = 0; c < CPW; ++c) {
+                    const int col = cp * CPW + c, gcol = dw.nt * BN + col;
+                    const int ec = GRAM ? (gcol < a.N ? __ldg(a.eB + (size_t)sidx * a.N + gcol) : 1)
+                                        : __ldg(a.eB + ((size_t)dw.nt * a.nsup + sidx) * BN + col);
+                    const double val = (er == 0x7FF || ec == 0x7FF)
+                                           ? __longlong_as_double(0x7FF8000000000000LL)
+                                           : tc_i128_f64((long long)(int)w2[c],
+                                                         ((unsigned long long)w1[c] << 32) | w0[c],
+                                                         er + ec - 2108);
+                    w0[c] = w1[c] = w2[c] = 0;
+                    if (GRAM) {
+                        double r = val;
+                        if (!(first && last)) {
+                            double &A = acc[col * kTcM + drow];
+                            if (!first) r += A;
+                            A = r;
+                        }
+                        if (last && grow < a.M && gcol < a.N)
+                            a.out[(size_t)z * a.M * a.N + grow + (size_t)gcol * a.M] = r;
+                    } else if (grow < a.M && gcol < a.N) {
+                        double *dst = a.out + grow + (size_t)gcol * a.ldo;
+                        double y = a.alpha == 1.0 ? val : a.alpha * val;
+                        if (a.accumulate) {
+                            y += *dst;
+                        } else if (a.beta != nullptr) {
+                            const double bb = a.beta[a.incb == 0 ? 0 : (size_t)gcol * a.incb];
+                            if (bb != 0.0) y = fma(bb, *dst, y);
+                        }
+                        *dst = y;
+                    }
                 }
             }
-            dk0 = dsk;
-        }
-        if (dvalid) dlast = tnext + dstages() - 1;
-        return true;
-    };
+            // the next chunk
+            const int tnext = dlast + 1;
+            dk0 += kTcDrainK;
+            if (dk0 >= ske) {
+                dsk += super_k;
+                if (dsk >= dw.ke) {
+                    dit += gridDim.x;
+                    dvalid = dit < a.items;
+                    if (dvalid) {
+                        dw = tc_item<GRAM>(a, dit);
+                        dsk = dw.kb;
+                    }
+                }
+                dk0 = dsk;
+            }
+            if (dvalid) dlast = tnext + dstages() - 1;
+            return true;
+        };
 
-    // ---- production
-    TcCursor cons;
-    cur_init<GRAM>(a, cons);
-    int t = 0;        // digit stages produced
-    uint32_t qr = 0;  // raw stages read
-    int em_a = 1;
-    bool ok = true;
-    while (ok && cons.valid) {
-        const int ske = min(cons.w.ke, cons.sk + super_k);
-        const int sidx = (cons.sk - (GRAM ? 0 : cons.w.kb)) / super_k;
-        if (cons.k0 == cons.sk) {
-            // a super-chunk starts: the exponent field of this thread's row
-            const int gr = cons.w.mt0 + ra;
-            em_a = gr < a.M ? __ldg(a.eA + (size_t)sidx * a.M + gr) : 1;
-        }
-        const uint32_t r = qr & 1;
-        const uint8_t *raw = sm + L::raw_off + r * L::raw_bytes;
-        const int nd = min(2, (ske - cons.k0 + kTcStageK - 1) / kTcStageK);
-        for (int dd = 0; dd < nd; ++dd, ++t) {
-            const uint32_t s = t & 1;
-            // the right-operand unit of this warp at stage t (Gram): unit b goes
-            // to warp (b + t BU) mod 16
-            const int bu = (warp - (int)(((uint32_t)t * BU) & 15u)) & 15;
-            const bool hasb = GRAM && bu < BU;
-            const int rb = (bu >> 1) * 8 + r7, gb = bu & 1;
-            int emb = 1;
-            if (hasb) {
-                const int gc = cons.w.nt * BN + rb;
-                emb = gc < a.N ? __ldg(a.eB + (size_t)sidx * a.N + gc) : 1;
+        // ---- production
+        TcCursor cons;
+        cur_init<GRAM>(a, cons);
+        int t = 0;        // digit stages produced
+        uint32_t qr = 0;  // raw stages read
+        int em_a = 1;
+        bool ok = true;
+        while (ok && cons.valid) {
+            const int ske = min(cons.w.ke, cons.sk + super_k);
+            const int sidx = (cons.sk - (GRAM ? 0 : cons.w.kb)) / super_k;
+            if (cons.k0 == cons.sk) {
+                // a super-chunk starts: the exponent field of this thread's row
+                const int gr = cons.w.mt0 + ra;
+                em_a = gr < a.M ? __ldg(a.eA + (size_t)sidx * a.M + gr) : 1;
             }
-            if (dd == 0 && !mbar_wait_warp(&rfull[r], (qr >> 1) & 1, abort_flag, a.error)) {
-                ok = false;
-                break;
-            }
-            if (t >= 2 && !mbar_wait_warp(&empty[s], ((t >> 1) & 1) ^ 1, abort_flag, a.error)) {
-                ok = false;
-                break;
-            }
-            uint8_t *abuf = sm + L::dig_off + s * L::stage_bytes;
-            uint8_t *bbuf = abuf + L::a_bytes;
-            if (!GRAM) {
-                // the right operand's prepared planes of this digit stage, from
-                // the raw stage
-                const uint4 *src = reinterpret_cast<const uint4 *>(raw + L::a_box + dd * L::b_box);
-                uint4 *dst = reinterpret_cast<uint4 *>(bbuf);
-                for (int i = tid; i < (int)(L::b_bytes / 16); i += kTcThreads) dst[i] = src[i];
-            }
-            // the pairs: left operand k-groups 0 and 1, and the right-operand unit
-            double2 v0, v1, vb = make_double2(0.0, 0.0);
-            if (GRAM) {
-                // box dd: row ra's 16 k as 8 chunks of 16 bytes, chunk c at c ^ (ra % 8)
-                const uint8_t *box = raw + dd * L::a_box + (uint32_t)ra * 128u;
-                v0 = *reinterpret_cast<const double2 *>(box + ((uint32_t)(pp ^ r7) << 4));
-                v1 = *reinterpret_cast<const double2 *>(box + ((uint32_t)((4 + pp) ^ r7) << 4));
+            const uint32_t r = qr & 1;
+            const uint8_t *raw = sm + L::raw_off + r * L::raw_bytes;
+            const int nd = min(2, (ske - cons.k0 + kTcStageK - 1) / kTcStageK);
+            for (int dd = 0; dd < nd; ++dd, ++t) {
+                const uint32_t s = t & 1;
+                // the right-operand unit of this warp at stage t (Gram): unit b goes
+                // to warp (b + t BU) mod 16
+                const int bu = (warp - (int)(((uint32_t)t * BU) & 15u)) & 15;
+                const bool hasb = GRAM && bu < BU;
+                const int rb = (bu >> 1) * 8 + r7, gb = bu & 1;
+                int emb = 1;
                 if (hasb) {
-                    const uint8_t *bx = raw + 2 * L::a_box + dd * L::b_box + (uint32_t)rb * 128u;
-                    vb = *reinterpret_cast<const double2 *>(
-                        bx + ((uint32_t)((4 * gb + pp) ^ r7) << 4));
+                    const int gc = cons.w.nt * BN + rb;
+                    emb = gc < a.N ? __ldg(a.eB + (size_t)sidx * a.N + gc) : 1;
                 }
-            } else {
-                // box [32 k][128 rows]
-                const double *col = reinterpret_cast<const double *>(raw) +
-                                    (size_t)(dd * kTcStageK + 2 * pp) * kTcM + ra;
-                v0 = make_double2(col[0], col[kTcM]);
-                v1 = make_double2(col[8 * kTcM], col[9 * kTcM]);
-            }
-            // row groups past the operand's last row hold zero digits: the
-            // conversion is skipped (warp-uniform)
-            const bool live_a = cons.w.mt0 + warp * 8 < a.M;
-            const bool live_b = !GRAM || cons.w.nt * BN + (bu >> 1) * 8 < a.N;
-            uint32_t d0[kTcDigits], d1[kTcDigits], db[kTcDigits];
-#pragma unroll
-            for (int i = 0; i < kTcDigits; ++i) d0[i] = d1[i] = db[i] = 0u;
-            if (live_a) {
-                tc_digit_pair(v0.x, v0.y, (uint32_t)em_a, d0);
-                tc_digit_pair(v1.x, v1.y, (uint32_t)em_a, d1);
-            }
-            if (hasb && live_b) tc_digit_pair(vb.x, vb.y, (uint32_t)emb, db);
-#pragma unroll
-            for (int i = 0; i < kTcDigits; ++i) {
-                uint8_t *pa = abuf + (uint32_t)i * tc_plane(kTcM) + a_dst;
-                *reinterpret_cast<uint32_t *>(pa) = d0[i];
-                *reinterpret_cast<uint32_t *>(pa + tc_lbo(kTcM)) = d1[i];
-            }
-            if (hasb) {
-                const uint32_t b_dst = (uint32_t)gb * tc_lbo_b(BN) + (uint32_t)(bu >> 1) * 128u +
-                                       (uint32_t)r7 * 16u + (uint32_t)pp * 4u;
-#pragma unroll
-                for (int i = 0; i < kTcDigits; ++i)
-                    *reinterpret_cast<uint32_t *>(bbuf + b_dst + (uint32_t)i * BN * 16u) = db[i];
-            }
-            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-            // chunks that ended at stage t - 1 or earlier
-            while (dvalid && dlast < t) {
-                if (!drain()) {
+                if (dd == 0 && !mbar_wait_warp(&rfull[r], (qr >> 1) & 1, abort_flag, a.error)) {
                     ok = false;
                     break;
                 }
+                if (t >= 2 && !mbar_wait_warp(&empty[s], ((t >> 1) & 1) ^ 1, abort_flag, a.error)) {
+                    ok = false;
+                    break;
+                }
+                uint8_t *abuf = sm + L::dig_off + s * L::stage_bytes;
+                uint8_t *bbuf = abuf + L::a_bytes;
+                if (!GRAM) {
+                    // the right operand's prepared planes of this digit stage, from
+                    // the raw stage
+                    const uint4 *src = reinterpret_cast<const uint4 *>(raw + L::a_box + dd * L::b_box);
+                    uint4 *dst = reinterpret_cast<uint4 *>(bbuf);
+                    for (int i = tid; i < (int)(L::b_bytes / 16); i += kTcWarps * 32) dst[i] = src[i];
+                }
+                // the pairs: left operand k-groups 0 and 1, and the right-operand unit
+                double2 v0, v1, vb = make_double2(0.0, 0.0);
+                if (GRAM) {
+                    // box dd: row ra's 16 k as 8 chunks of 16 bytes, chunk c at c ^ (ra % 8)
+                    const uint8_t *box = raw + dd * L::a_box + (uint32_t)ra * 128u;
+                    v0 = *reinterpret_cast<const double2 *>(box + ((uint32_t)(pp ^ r7) << 4));
+                    v1 = *reinterpret_cast<const double2 *>(box + ((uint32_t)((4 + pp) ^ r7) << 4));
+                    if (hasb) {
+                        const uint8_t *bx = raw + 2 * L::a_box + dd * L::b_box + (uint32_t)rb * 128u;
+                        vb = *reinterpret_cast<const double2 *>(
+                            bx + ((uint32_t)((4 * gb + pp) ^ r7) << 4));
+                    }
+                } else {
+                    // box [32 k][128 rows]
+                    const double *col = reinterpret_cast<const double *>(raw) +
+                                        (size_t)(dd * kTcStageK + 2 * pp) * kTcM + ra;
+                    v0 = make_double2(col[0], col[kTcM]);
+                    v1 = make_double2(col[8 * kTcM], col[9 * kTcM]);
+                }
+                // row groups past the operand's last row hold zero digits: the
+                // conversion is skipped (warp-uniform)
+                const bool live_a = cons.w.mt0 + warp * 8 < a.M;
+                const bool live_b = !GRAM || cons.w.nt * BN + (bu >> 1) * 8 < a.N;
+                uint32_t d0[kTcDigits], d1[kTcDigits], db[kTcDigits];
+#pragma unroll
+                for (int i = 0; i < kTcDigits; ++i) d0[i] = d1[i] = db[i] = 0u;
+                if (live_a) {
+                    tc_digit_pair(v0.x, v0.y, (uint32_t)em_a, d0);
+                    tc_digit_pair(v1.x, v1.y, (uint32_t)em_a, d1);
+                }
+                if (hasb && live_b) tc_digit_pair(vb.x, vb.y, (uint32_t)emb, db);
+#pragma unroll
+                for (int i = 0; i < kTcDigits; ++i) {
+                    uint8_t *pa = abuf + (uint32_t)i * tc_plane(kTcM) + a_dst;
+                    *reinterpret_cast<uint32_t *>(pa) = d0[i];
+                    *reinterpret_cast<uint32_t *>(pa + tc_lbo(kTcM)) = d1[i];
+                }
+                if (hasb) {
+                    const uint32_t b_dst = (uint32_t)gb * tc_lbo_b(BN) + (uint32_t)(bu >> 1) * 128u +
+                                           (uint32_t)r7 * 16u + (uint32_t)pp * 4u;
+#pragma unroll
+                    for (int i = 0; i < kTcDigits; ++i)
+                        *reinterpret_cast<uint32_t *>(bbuf + b_dst + (uint32_t)i * BN * 16u) = db[i];
+                }
+                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                // chunks that ended at stage t - 1 or earlier
+                while (dvalid && dlast < t) {
+                    if (!drain()) {
+                        ok = false;
+                        break;
+                    }
+                }
+                if (!ok) break;
+                // arrival (release; the stores and drains above come first)
+                tc_fence_before();
+                __syncwarp();
+                if (lane == 0) mbar_arrive(&full[s]);
             }
             if (!ok) break;
-            // arrival; the last warp issues the stage's MMAs
-            tc_fence_before();
+            // raw stage qr is read; the last warp copies raw stage qr + 2 into its buffer
             __syncwarp();
-            if (lane == 0 && smem_arrive(&fcnt[s]) == kTcWarps - 1) {
-                fcnt[s] = 0;
-                tc_fence_after();
-                const int k = cons.k0 + dd * kTcStageK;
-                const int cs = cons.sk + (k - cons.sk) / kTcDrainK * kTcDrainK;
-                issue_mma(s, (k - cs) / kTcStageK, k + kTcStageK >= min(cs + kTcDrainK, ske));
-                atomicMax(n_stages, t + 1);
+            if (lane == 0 && smem_arrive(&rcnt[r]) == kTcWarps - 1) {
+                rcnt[r] = 0;
+                TcCursor c2 = cons;
+                cur_next<GRAM>(a, c2);
+                if (c2.valid) cur_next<GRAM>(a, c2);
+                if (c2.valid) issue_raw(qr + 2, c2);
             }
             __syncwarp();
+            ++qr;
+            cur_next<GRAM>(a, cons);
         }
-        if (!ok) break;
-        // raw stage qr is read; the last warp copies raw stage qr + 2 into its buffer
-        __syncwarp();
-        if (lane == 0 && smem_arrive(&rcnt[r]) == kTcWarps - 1) {
-            rcnt[r] = 0;
-            TcCursor c2 = cons;
-            cur_next<GRAM>(a, c2);
-            if (c2.valid) cur_next<GRAM>(a, c2);
-            if (c2.valid) issue_raw(qr + 2, c2);
-        }
-        __syncwarp();
-        ++qr;
-        cur_next<GRAM>(a, cons);
-    }
-    // the remaining chunks
-    while (ok && dvalid)
-        if (!drain()) ok = false;
+        // the remaining chunks
+        while (ok && dvalid)
+            if (!drain()) ok = false;
 
-    // teardown: the MMAs and bulk copies still in flight (after an abort, or
-    // the last stages' MMAs nobody waited for) complete before tensor memory
-    // is freed and the CTA exits
+    }
+    // teardown: the bulk copies still in flight (after an abort) land before
+    // the CTA exits; the MMA warp waited for its MMAs
     tc_fence_before();
     __syncthreads();
     if (warp == 0) {
-        const int ns = *n_stages, nc = *n_chunks, nr = *n_raw;
-        for (int tt = max(ns - 2, 0); tt < ns; ++tt)
-            mbar_wait_teardown(&empty[tt & 1], (tt >> 1) & 1);
-        if (nc > 0) mbar_wait_teardown(accf, (nc - 1) & 1);
+        const int nr = *n_raw;
         for (int qq = max(nr - 2, 0); qq < nr; ++qq)
             mbar_wait_teardown(&rfull[qq & 1], (qq >> 1) & 1);
         tc_fence_after();
