@@ -7,18 +7,18 @@
 // Method (error-free digit splitting, the Ozaki scheme), as in ozaki.cu:
 // within an exponent window of consecutive k every row of the left operand
 // and every column of the right operand gets an exponent e with |x| < 2^e,
-// |x| becomes the 56-bit fixed-point integer X = |x| 2^(56-e) (truncated),
-// written as 7 digits of 8 bits with x's sign: the leading digit in [0, 256],
+// |x| becomes the 55-bit fixed-point integer X = |x| 2^(55-e) (truncated),
+// written as 7 digits of 8 bits with x's sign: the leading digit in [0, 128],
 // the others balanced in [-128, 127].  Digits are exact in FP16, the 28 digit
 // pairs with i + j <= 6 are multiplied on the tensor cores and summed into 7
 // level accumulators L_l = sum_{i+j=l} d_i d'_j, which are exact FP32 integers
-// as long as |L_l| < 2^24: 96 consecutive k at most (|L_6| <= 96 (2 * 256 *
-// 128 + 5 * 128^2) < 2^23.8).  Every 96 k ("drain") the levels are read out of
-// tensor memory into one exact 96-bit integer per output; at the end of a
-// window it is converted to FP64 (integer instructions, round to nearest) with
-// the window's scale.  A Gram work item has one window over its whole k range
-// (error below 2^-54 sqrt(K) |x| |y| per entry, under the FP64 dot product's
-// bound K 2^-53 |x| |y|); a linear combination has one per 480 k.
+// as long as |L_l| < 2^24: 144 consecutive k at most (|L_6| <= 144 * 7 * 128^2
+// < 2^23.98).  Every 144 k ("drain") the levels are read out of tensor memory
+// into one exact 96-bit integer per output; at the end of a window it is
+// converted to FP64 (integer instructions, round to nearest) with the window's
+// scale.  A Gram work item has one window over its whole k range (error below
+// 2^-53 sqrt(K) |x| |y| per entry, under the FP64 dot product's bound
+// K 2^-53 |x| |y|); a linear combination has one per 432 k.
 //
 // Data path, per CTA (one per SM, persistent over work items, 16 warps):
 //  * exponent fields come from a streaming pre-pass (k_tc_expcols /
@@ -30,17 +30,18 @@
 //    reading rows hit distinct banks); the right operand of a linear
 //    combination is prepared once per call (k_tc_bprep) and copied in with
 //    cp.async.bulk;
-//  * every warp turns its core matrices (8 rows x 8 k) of each 16-k half of a
-//    raw stage into the 7 FP16 digit planes of a digit stage (two digit
-//    stages, K-major core-matrix layout);
-//  * the last warp to finish a digit stage issues its MMAs (M = 128 rows,
-//    N = up to 256, K = 16, f16 x f16 -> f32 into the 7 level accumulators,
-//    7 x BN of the 512 tensor-memory columns) and commits them to an
-//    mbarrier; the last warp to finish reading a raw stage issues the bulk
-//    copies of the raw stage two ahead;
-//  * every warp drains its slice of the levels after each 96-k chunk (warp w
-//    reads lanes 32 (w % 4) .. + 31, BN / 4 columns) and folds it at the end
-//    of each window.
+//  * 16 worker warps turn their core matrices (8 rows x 8 k) of each 16-k
+//    half of a raw stage into the 7 FP16 digit planes of a digit stage (a
+//    ring of two digit stages, K-major core-matrix layout); the last worker
+//    to finish reading a raw stage issues the bulk copies of the raw stage
+//    two ahead;
+//  * one warp issues the MMAs of each digit stage (M = 128 rows, N = up to
+//    256, K = 16, f16 x f16 -> f32 into the 7 level accumulators, 7 x BN of
+//    the 512 tensor-memory columns) and commits them to mbarriers;
+//  * every worker drains its slice of the levels after each 144-k chunk (warp
+//    w reads lanes 32 (w % 4) .. + 31, BN / 4 columns) and folds it at the
+//    end of each window (a Gram work item longer than one window adds its
+//    windows into its split-k partial).
 // Every wait on an mbarrier is bounded; a wait that runs out sets the error
 // word and every warp stops at its next wait, so the kernel always returns.
 #include <cuda.h>
@@ -58,9 +59,10 @@ constexpr int kTcDigits = 7;
 constexpr int kTcM = 128;      // output rows per tile (tensor-memory lanes)
 constexpr int kTcStageK = 16;  // k per digit stage (one MMA step)
 constexpr int kTcRawK = 32;    // k per raw (TMA) stage: two digit stages
-constexpr int kTcDrainStages = 6;
-constexpr int kTcDrainK = kTcStageK * kTcDrainStages;  // 96: exact FP32 level sums
+constexpr int kTcDrainStages = 9;
+constexpr int kTcDrainK = kTcStageK * kTcDrainStages;  // 144: exact FP32 level sums
 constexpr int kTcKGroups = kTcStageK / 8;              // core matrices along k per stage
+constexpr int kTcDigStages = 2;                         // ring of digit stages
 constexpr int kTcWarps = 16;  // worker warps: digit conversion and drain
 constexpr int kTcThreads = (kTcWarps + 1) * 32;  // and one warp issuing the MMAs
 constexpr uint32_t kTcTmemCols = 512;
@@ -68,9 +70,9 @@ constexpr uint32_t kTcTmemCols = 512;
 constexpr unsigned long long kTcWaitNs = 4000000000ull;
 constexpr long long kTcWaitPolls = 1LL << 22;
 // A Gram work item shares one exponent per column over its whole k range
-// (at most this many rows: the 96-bit level sums stay below 2^85)
+// (at most this many rows: the 96-bit level sums stay below 2^86)
 constexpr int kTcSuperGramMax = 16384 * kTcDrainK;
-constexpr int kTcSuperLincomb = 5 * kTcDrainK;  // 480: K up to 480 in one super-chunk
+constexpr int kTcSuperLincomb = 3 * kTcDrainK;  // 432: K up to 432 in one window
 
 // Byte layout of one operand tile of R rows in a digit stage: plane i
 // (digit), k-group g (8 consecutive k), row r: i * plane + g * lbo +
@@ -95,9 +97,8 @@ __host__ __device__ constexpr uint32_t tc_tile_b_bytes(int bn) { return kTcKGrou
 // Shared memory (offsets from a 1024-byte aligned base).  Raw stage of a
 // Gram: A boxes [2][128 rows][16 k] and B boxes [2][BN rows][16 k] of FP64 in
 // the 128-byte swizzle; of a linear combination: A box [32 k][128 rows] and
-// the right operand's prepared digit planes of its two digit stages.  A
-// linear combination covers at most one super-chunk per work item (the host
-// splits longer contractions), so only the Gram keeps FP64 accumulators.
+// the right operand's prepared digit planes of its two digit stages.  The
+// digit stages form a ring of kTcDigStages.
 template <int BN, bool GRAM>
 struct TcLayout {
     static constexpr uint32_t a_bytes = tc_tile_bytes(kTcM);
@@ -109,12 +110,10 @@ struct TcLayout {
         GRAM ? 2 * (a_box + b_box) : tc_round(a_box + 2 * b_box, 1024);
     static constexpr uint32_t raw_off = 0;  // [2] raw stages
     static constexpr uint32_t stage_bytes = a_bytes + b_bytes;
-    static constexpr uint32_t dig_off = tc_round(raw_off + 2 * raw_bytes, 1024);  // [2] digit stages
-    static constexpr uint32_t acc_off = dig_off + 2 * stage_bytes;  // double acc[BN][kTcM]
-    static constexpr uint32_t bar_off =
-        tc_round(acc_off + (GRAM ? (uint32_t)BN * kTcM * 8 : 0u), 16);
-    // mbarriers empty[2] rfull[2] accf full[2] fin
-    static constexpr int nbars = 8;
+    static constexpr uint32_t dig_off = tc_round(raw_off + 2 * raw_bytes, 1024);
+    static constexpr uint32_t bar_off = tc_round(dig_off + kTcDigStages * stage_bytes, 16);
+    // mbarriers empty[3] full[3] rfull[2] accf fin
+    static constexpr int nbars = 2 * kTcDigStages + 4;
     // tmem slot, abort flag, arrival counters rempty[2], raw stages issued
     static constexpr uint32_t misc_off = bar_off + nbars * 8;
     static constexpr uint32_t bytes = misc_off + 48;
@@ -274,27 +273,28 @@ __device__ __forceinline__ int tc_exp_field(double x) {
     return max((int)(((unsigned)__double2hiint(x) >> 20) & 0x7FFu), 1);
 }
 
-// X = |x| 2^(1078 - emax) as a 56-bit fixed-point integer (truncated; the
+// X = |x| 2^(1077 - emax) as a 55-bit fixed-point integer (truncated; the
 // caller guarantees emax >= the exponent field of x), plus 0x808080808080,
-// as two words: the 53-bit significand shifted left by 3, then right by
-// emax - field with clamped funnel shifts (no branches).  sgn = x's sign bit.
-__device__ __forceinline__ void tc_fixed56(double x, uint32_t emax, uint32_t &yh, uint32_t &yl,
-                                           uint32_t &sgn) {
-    const uint32_t hi = (uint32_t)__double2hiint(x), lo = (uint32_t)__double2loint(x);
-    const uint32_t ef = (hi >> 20) & 0x7FFu;
-    const uint32_t mhi = (hi & 0xFFFFFu) | (min(ef, 1u) << 20);
-    uint32_t xh = __funnelshift_l(lo, mhi, 3);
-    uint32_t xl = lo << 3;
-    const uint32_t r = emax - max(ef, 1u);
-    const uint32_t r1 = min(r, 32u), r2 = min(r - r1, 32u);
-    xl = __funnelshift_rc(xl, xh, r1);
-    xh = __funnelshift_rc(xh, 0u, r1);
-    xl = __funnelshift_rc(xl, xh, r2);
-    xh = __funnelshift_rc(xh, 0u, r2);
+// as two words: the 53-bit significand shifted left by 2, then right by
+// r = emax - field (at most 63: everything past 55 bits is gone), a 64-bit
+// shift made of one wrapping and one clamping funnel shift.  hi = x's high
+// word (its sign bit is the sign).
+__device__ __forceinline__ void tc_fixed55(double x, uint32_t emax, uint32_t &yh, uint32_t &yl,
+                                           uint32_t &hi) {
+    hi = (uint32_t)__double2hiint(x);
+    const uint32_t lo = (uint32_t)__double2loint(x);
+    const uint32_t eb = hi & 0x7FF00000u;  // exponent field << 20
+    // the hidden bit, absent for zeros and subnormals (which count as field 1)
+    const uint32_t mhi = (hi & 0x000FFFFFu) | min(eb, 0x00100000u);
+    const uint32_t xh = __funnelshift_l(lo, mhi, 2);
+    const uint32_t xl = lo << 2;
+    const uint32_t r = min(emax - (max(eb, 0x00100000u) >> 20), 63u);
+    const bool big = r >= 32u;
+    const uint32_t sl = __funnelshift_r(big ? xh : xl, big ? 0u : xh, r);  // shift r mod 32
+    const uint32_t sh = __funnelshift_rc(xh, 0u, r);                       // 0 for r >= 32
     asm("add.cc.u32 %0, %2, 0x80808080;\n\taddc.u32 %1, %3, 0x8080;"
         : "=r"(yl), "=r"(yh)
-        : "r"(xl), "r"(xh));
-    sgn = hi & 0x80000000u;
+        : "r"(sl), "r"(sh));
 }
 
 // (a - b) on two packed FP16 values
@@ -306,18 +306,19 @@ __device__ __forceinline__ uint32_t tc_hsub2(uint32_t a, uint32_t b) {
 
 // The 7 FP16 digits of 8 values (one row, 8 consecutive k) relative to the
 // exponent field emax: out[i] holds digit i of the 8 values, two per word
-// (lower k in the low half).  With Y = X + 0x808080808080 (tc_fixed56),
-// digit 0 is Y >> 48 (in [0, 256]) and digit i >= 1 is byte 6 - i of Y less
+// (lower k in the low half).  With Y = X + 0x808080808080 (tc_fixed55),
+// digit 0 is Y >> 48 (in [0, 128]) and digit i >= 1 is byte 6 - i of Y less
 // 128 (in [-128, 127]), so that X = sum_i d_i 2^(8 (6 - i)); each carries x's
 // sign.  A digit is formed for two values at once: the FP16 pattern
 // sign | 0x6400 | field is +-(1024 + field) exactly (ulp 1 on [1024, 2048)),
 // and subtracting +-1024 (digit 0) or +-(1024 + 128) leaves +-d exactly.
 __device__ __forceinline__ void tc_digit_pair(double x0, double x1, uint32_t emax,
                                               uint32_t (&w)[kTcDigits]) {
-    uint32_t yh0, yl0, s0, yh1, yl1, s1;
-    tc_fixed56(x0, emax, yh0, yl0, s0);
-    tc_fixed56(x1, emax, yh1, yl1, s1);
-    const uint32_t M = 0x64006400u | (s0 >> 16) | s1;  // +-1024 in each half
+    uint32_t yh0, yl0, h0, yh1, yl1, h1;
+    tc_fixed55(x0, emax, yh0, yl0, h0);
+    tc_fixed55(x1, emax, yh1, yl1, h1);
+    // +-1024 in each half: the sign bits of the two values at bits 15 and 31
+    const uint32_t M = (__byte_perm(h0, h1, 0x7030) & 0x80008000u) | 0x64006400u;
     const uint32_t Mb = M | 0x00800080u;                // +-(1024 + 128)
     w[0] = tc_hsub2((yh0 >> 16) | (yh1 & 0xFFFF0000u) | M, M);
     // byte 6 - i of Y: bytes 4, 5 in the high word, 0..3 in the low word; the
@@ -520,10 +521,9 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     extern __shared__ __align__(1024) uint8_t sm_raw[];
     // 1024-byte aligned base (the 128-byte swizzle of the bulk copies needs it)
     uint8_t *sm = sm_raw + ((1024u - (su32(sm_raw) & 1023u)) & 1023u);
-    double *acc = reinterpret_cast<double *>(sm + L::acc_off);  // [BN][kTcM]
     uint64_t *bars = reinterpret_cast<uint64_t *>(sm + L::bar_off);
-    uint64_t *empty = bars, *rfull = bars + 2, *accf = bars + 4, *full = bars + 5;
-    uint64_t *fin = bars + 7;
+    uint64_t *empty = bars, *full = bars + kTcDigStages, *rfull = bars + 2 * kTcDigStages;
+    uint64_t *accf = rfull + 2, *fin = rfull + 3;
     uint32_t *misc = reinterpret_cast<uint32_t *>(sm + L::misc_off);
     uint32_t *tmem_slot = misc;
     volatile int *abort_flag = reinterpret_cast<volatile int *>(misc + 1);
@@ -534,10 +534,12 @@ __global__ void __launch_bounds__(kTcThreads, 1)
     const int super_k = a.super_k;
 
     if (tid == 0) {
-        for (int s = 0; s < 2; ++s) {
+        for (int s = 0; s < kTcDigStages; ++s) {
             mbar_init(&empty[s], 1);
-            mbar_init(&rfull[s], 1);
             mbar_init(&full[s], kTcWarps);
+        }
+        for (int s = 0; s < 2; ++s) {
+            mbar_init(&rfull[s], 1);
             rcnt[s] = 0;
         }
         mbar_init(accf, 1);
@@ -609,23 +611,23 @@ __global__ void __launch_bounds__(kTcThreads, 1)
 
     if (warp == kTcWarps) {
         // ------------------------------------------------------------ MMA issuer
-        uint32_t t = 0;  // digit stages issued
+        uint32_t s = 0, ph = 0;  // ring position and phase of the next digit stage
         bool ok = true;
         for (int it = blockIdx.x; it < a.items && ok; it += gridDim.x) {
             const TcItem w = tc_item<GRAM>(a, it);
             for (int k0 = w.kb; k0 < w.ke && ok; k0 += kTcDrainK) {
                 const int nst = min(kTcDrainStages, (w.ke - k0 + kTcStageK - 1) / kTcStageK);
-                for (int st = 0; st < nst; ++st, ++t) {
-                    const uint32_t s = t & 1;
+                for (int st = 0; st < nst; ++st) {
                     // every worker finished the stage (and drained the previous
                     // chunk before the first stage of this one)
-                    if (!mbar_wait_warp(&full[s], (t >> 1) & 1, abort_flag, a.error)) {
+                    if (!mbar_wait_warp(&full[s], ph, abort_flag, a.error)) {
                         ok = false;
                         break;
                     }
                     tc_fence_after();
                     if (lane == 0) issue_mma(s, st, st == nst - 1);
                     __syncwarp();
+                    if (++s == kTcDigStages) s = 0, ph ^= 1;
                 }
             }
         }
@@ -680,28 +682,44 @@ __global__ void __launch_bounds__(kTcThreads, 1)
             if (!mbar_wait_warp(accf, dn & 1, abort_flag, a.error)) return false;
             tc_fence_after();
             const uint32_t tb = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(cp * CPW);
+            // levels 0 and 1, 2 and 3 pair up exactly in 32 bits (|L_0 2^8 + L_1|
+            // < 2^30.2, |L_2 2^8 + L_3| < 2^30.9): each pair is read with one
+            // wait and added once; levels 4, 5 and 6 are added alone
+            auto f2i = [](uint32_t u) { return __float2int_rn(__uint_as_float(u)); };
 #pragma unroll
-            for (int l = 0; l < kTcDigits; ++l) {
-                uint32_t v[CPW / 4][4];
+            for (int l = 0; l < 4; l += 2) {
+                uint32_t u[CPW / 4][4], v[CPW / 4][4];
 #pragma unroll
-                for (int j = 0; j < CPW / 4; ++j) tc_ld4(tb + (uint32_t)(l * BN + 4 * j), v[j]);
+                for (int j = 0; j < CPW / 4; ++j) {
+                    tc_ld4(tb + (uint32_t)(l * BN + 4 * j), u[j]);
+                    tc_ld4(tb + (uint32_t)((l + 1) * BN + 4 * j), v[j]);
+                }
                 tc_wait_ld();
 #pragma unroll
                 for (int c = 0; c < CPW; ++c)
-                    tc_acc_level(w0[c], w1[c], w2[c], __float2int_rn(__uint_as_float(v[c >> 2][c & 3])),
-                                 l);
+                    tc_acc_level(w0[c], w1[c], w2[c],
+                                 f2i(u[c >> 2][c & 3]) * 256 + f2i(v[c >> 2][c & 3]), l + 1);
+            }
+#pragma unroll
+            for (int l = 4; l < kTcDigits; ++l) {
+                uint32_t u[CPW / 4][4];
+#pragma unroll
+                for (int j = 0; j < CPW / 4; ++j) tc_ld4(tb + (uint32_t)(l * BN + 4 * j), u[j]);
+                tc_wait_ld();
+#pragma unroll
+                for (int c = 0; c < CPW; ++c) tc_acc_level(w0[c], w1[c], w2[c], f2i(u[c >> 2][c & 3]), l);
             }
             ++dn;
             const int ske = min(dw.ke, dsk + super_k);
             if (dk0 + kTcDrainK >= ske) {
-                // the super-chunk ends: its sums, w 2^(er + ec - 2108)
+                // the super-chunk ends: its sums, w 2^(er + ec - 2106)
                 // converted with integer instructions, go into the work item's
                 // split-k partial (Gram; FP64 accumulators for a work item of
                 // several super-chunks) or straight into Y (a linear combination)
                 const int sidx = (dsk - (GRAM ? 0 : dw.kb)) / super_k;
                 const int grow = dw.mt0 + drow;
                 const int er = grow < a.M ? __ldg(a.eA + (size_t)sidx * a.M + grow) : 1;
-                const bool first = dsk == dw.kb, last = dsk + super_k >= dw.ke;
+                const bool first = dsk == dw.kb;
                 const int z = dit / (a.mtiles * a.ntiles);
 #pragma unroll
                 for (int c = 0; c < CPW; ++c) {
@@ -712,17 +730,15 @@ __global__ void __launch_bounds__(kTcThreads, 1)
                                            ? __longlong_as_double(0x7FF8000000000000LL)
                                            : tc_i128_f64((long long)(int)w2[c],
                                                          ((unsigned long long)w1[c] << 32) | w0[c],
-                                                         er + ec - 2108);
+                                                         er + ec - 2106);
                     w0[c] = w1[c] = w2[c] = 0;
                     if (GRAM) {
-                        double r = val;
-                        if (!(first && last)) {
-                            double &A = acc[col * kTcM + drow];
-                            if (!first) r += A;
-                            A = r;
+                        // the work item's split-k partial: its first window
+                        // writes it, later windows add to it
+                        if (grow < a.M && gcol < a.N) {
+                            double *dst = a.out + (size_t)z * a.M * a.N + grow + (size_t)gcol * a.M;
+                            *dst = first ? val : *dst + val;
                         }
-                        if (last && grow < a.M && gcol < a.N)
-                            a.out[(size_t)z * a.M * a.N + grow + (size_t)gcol * a.M] = r;
                     } else if (grow < a.M && gcol < a.N) {
                         double *dst = a.out + grow + (size_t)gcol * a.ldo;
                         double y = a.alpha == 1.0 ? val : a.alpha * val;
@@ -759,6 +775,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
         TcCursor cons;
         cur_init<GRAM>(a, cons);
         int t = 0;        // digit stages produced
+        uint32_t s = 0, ph = 0;  // ring position and phase of stage t
         uint32_t qr = 0;  // raw stages read
         int em_a = 1;
         bool ok = true;
@@ -774,7 +791,6 @@ __global__ void __launch_bounds__(kTcThreads, 1)
             const uint8_t *raw = sm + L::raw_off + r * L::raw_bytes;
             const int nd = min(2, (ske - cons.k0 + kTcStageK - 1) / kTcStageK);
             for (int dd = 0; dd < nd; ++dd, ++t) {
-                const uint32_t s = t & 1;
                 // the right-operand unit of this warp at stage t (Gram): unit b goes
                 // to warp (b + t BU) mod 16
                 const int bu = (warp - (int)(((uint32_t)t * BU) & 15u)) & 15;
@@ -789,7 +805,8 @@ __global__ void __launch_bounds__(kTcThreads, 1)
                     ok = false;
                     break;
                 }
-                if (t >= 2 && !mbar_wait_warp(&empty[s], ((t >> 1) & 1) ^ 1, abort_flag, a.error)) {
+                // the MMAs of stage t - kTcDigStages read this buffer
+                if (t >= kTcDigStages && !mbar_wait_warp(&empty[s], ph ^ 1, abort_flag, a.error)) {
                     ok = false;
                     break;
                 }
@@ -859,6 +876,7 @@ __global__ void __launch_bounds__(kTcThreads, 1)
                 tc_fence_before();
                 __syncwarp();
                 if (lane == 0) mbar_arrive(&full[s]);
+                if (++s == kTcDigStages) s = 0, ph ^= 1;
             }
             if (!ok) break;
             // raw stage qr is read; the last warp copies raw stage qr + 2 into its buffer
@@ -1206,7 +1224,7 @@ size_t tc_lincomb_scratch_bytes(int k, int m) {
 
 // Y (n x m, ldy) = alpha X C + Y diag(beta) for X n x k (ldx), C k x m (ldc);
 // beta == nullptr overwrites Y; incb == 0 broadcasts beta[0].  Contractions
-// longer than one super-chunk (480) run as several launches, each later one
+// longer than one window (432) run as several launches, each later one
 // adding its block's product to Y.
 void tc_lincomb(int n, int k, int m, const double *X, int ldx, const double *C, int ldc, double *Y,
                 int ldy, const double *beta_dev, int incb, cudaStream_t st, double alpha,

@@ -89,7 +89,8 @@ def test_gram_digits_nan_propagates(gpu_lib):
 @pytest.mark.parametrize("n,k,m,mode", [(20011, 180, 20, "minus_one"), (5000, 37, 160, "none"),
                                         (1000, 3, 5, "vector"), (70001, 52, 24, "none"),
                                         (64, 64, 8, "vector"), (333, 200, 17, "minus_one"),
-                                        (3001, 1000, 24, "minus_one"), (5000, 481, 50, "vector")])
+                                        (3001, 1000, 24, "minus_one"), (5000, 481, 50, "vector"),
+                                        (4000, 433, 40, "none"), (2000, 145, 33, "vector")])
 def test_lincomb_digits_match_fp64(gpu_lib, n, k, m, mode):
     G = gpu_lib
     rng = np.random.default_rng(n + k + m)
