@@ -8,6 +8,7 @@ columns, blocks of bs = 20).
     python tests/profile_cases.py pcg       # FP32 block PCG, 20 columns, 30 steps
     python tests/profile_cases.py eig       # dense eigensolver, s = 200
     python tests/profile_cases.py pcgsmall  # FP32 block PCG, 2D n = 4160 (cluster form)
+    python tests/profile_cases.py pcg128    # FP32 block PCG, 128^3 variable coefficient, 40 columns
 
 Each case runs the FP64-accurate digit-plane product once after one warm-up
 call, through the same C-ABI entry points the parity tests use
@@ -81,6 +82,23 @@ def pcg():
     red = float(np.max(np.linalg.norm(b - S @ x, axis=0) / np.linalg.norm(b, axis=0)))
     print(f"pcg n={A.n} k={W} steps={it}: max relative residual {red:.2e}")
     return it == 30 and red < 0.5
+
+
+def pcg128():
+    """The W-step PCG of the benchmark solve's shape: the variable-coefficient
+    128^3 operator with its lumped diagonal mass, 40 right-hand sides, 30
+    FP32 steps without early stop (k_block_pcg<float, 40>)."""
+    from gcge_gb300 import problems as Pr
+    A, B = Pr.vardiff3d(128)
+    b = np.random.default_rng(4).standard_normal((A.n, 40))
+    x0 = np.zeros_like(b)
+    sigma = 1.0
+    G.block_pcg(A, B, sigma, b, x0, max_iter=30, rate=1e-30, tol=1e-30, fp32=True)
+    x, it = G.block_pcg(A, B, sigma, b, x0, max_iter=30, rate=1e-30, tol=1e-30, fp32=True)
+    S = A.to_scipy() + sigma * B.to_scipy()
+    red = float(np.max(np.linalg.norm(b - S @ x, axis=0) / np.linalg.norm(b, axis=0)))
+    print(f"pcg n={A.n} k=40 steps={it}: max relative residual {red:.2e}")
+    return it == 30 and red < 1.0
 
 
 def pcgsmall():
@@ -173,6 +191,8 @@ def main(argv):
         ok &= eig()
     if what == "pcgsmall":
         ok &= pcgsmall()
+    if what == "pcg128":
+        ok &= pcg128()
     return 0 if ok else 1
 
 
