@@ -241,14 +241,33 @@ void lincomb(int n, int k, int m, const double *X, int ldx, const double *C, int
 void gram(int n, int m, int w, const double *Q, int ldq, const double *P, int ldp, double *C,
           int ldc, double *scratch, size_t scratch_elems, cudaStream_t st);
 size_t gram_scratch_elems(int n, int m, int w);
+// Exponent fields of one digit-product operand (the Gram's left operand over
+// its row windows, or a linear combination's rows over its columns), kept
+// across calls that pass the same unchanged operand with the same shape.  The
+// caller owns the scope: it must drop the cache (or let it go out of scope)
+// before the operand's values change.
+struct TcExpCache {
+    const double *ptr = nullptr;
+    size_t ld = 0;
+    int rows = 0, cols = 0, window = 0, kind = -1;
+    DevBuf<int> e;
+    bool matches(const double *p, size_t l, int r, int c, int w, int k) const {
+        return kind == k && ptr == p && ld == l && rows == r && cols == c && window == w;
+    }
+    void set(const double *p, size_t l, int r, int c, int w, int k) {
+        ptr = p, ld = l, rows = r, cols = c, window = w, kind = k;
+    }
+};
 // FP64-accurate products on the bf16 tensor cores (ozaki.cu): same arguments
-// and results as gram / lincomb, to FP64 accuracy.
+// and results as gram / lincomb, to FP64 accuracy.  `cache` (optional) keeps
+// the exponent fields of Q (Gram) or X (linear combination) between calls.
 void oz_gram(int n, int m, int w, const double *Q, int ldq, const double *P, int ldp, double *C,
-             int ldc, double *scratch, size_t scratch_elems, cudaStream_t st);
+             int ldc, double *scratch, size_t scratch_elems, cudaStream_t st,
+             TcExpCache *cache = nullptr);
 void oz_lincomb(int n, int k, int m, const double *X, int ldx, const double *C, int ldc,
                 double *Y, int ldy, const double *beta_dev, int incb, cudaStream_t st,
                 double alpha,
-                void *scratch, size_t scratch_bytes);
+                void *scratch, size_t scratch_bytes, TcExpCache *cache = nullptr);
 // Scratch bytes oz_lincomb needs for k terms and m columns.
 size_t oz_lincomb_scratch_bytes(int k, int m);
 // The same products on the 5th-generation tensor cores (ozaki_tc.cu:
@@ -256,10 +275,11 @@ size_t oz_lincomb_scratch_bytes(int k, int m);
 // results; oz_gram / oz_lincomb use them where tc_digits_available().
 bool tc_digits_available();
 void tc_gram(int n, int m, int w, const double *Q, int ldq, const double *P, int ldp, double *C,
-             int ldc, double *scratch, size_t scratch_elems, cudaStream_t st);
+             int ldc, double *scratch, size_t scratch_elems, cudaStream_t st,
+             TcExpCache *cache = nullptr);
 void tc_lincomb(int n, int k, int m, const double *X, int ldx, const double *C, int ldc,
                 double *Y, int ldy, const double *beta_dev, int incb, cudaStream_t st,
-                double alpha, void *scratch, size_t scratch_bytes);
+                double alpha, void *scratch, size_t scratch_bytes, TcExpCache *cache = nullptr);
 size_t tc_lincomb_scratch_bytes(int k, int m);
 // Throws GCGE_ERR_CUDA (and clears the flag) if a tensor-core product's
 // bounded wait ran out since the last check (synchronises the stream).

@@ -150,17 +150,18 @@ constexpr int kDigitMinRows = 1024;
 
 static void dgram(const SolverCtx &c, int n, int m, int w, const double *Q, int ldq,
                   const double *P, int ldp, double *C, int ldc, double *scratch, size_t elems,
-                  cudaStream_t st) {
+                  cudaStream_t st, TcExpCache *qcache = nullptr) {
     if (c.precision == GCGE_PREC_MIXED && !c.escalated && n >= kDigitMinRows)
-        oz_gram(n, m, w, Q, ldq, P, ldp, C, ldc, scratch, elems, st);
+        oz_gram(n, m, w, Q, ldq, P, ldp, C, ldc, scratch, elems, st, qcache);
     else
         gram(n, m, w, Q, ldq, P, ldp, C, ldc, scratch, elems, st);
 }
 static void dlincomb(const SolverCtx &c, int n, int k, int m, const double *X, int ldx,
                      const double *C, int ldc, double *Y, int ldy, const double *beta, int incb,
-                     cudaStream_t st, double alpha = 1.0) {
+                     cudaStream_t st, double alpha = 1.0, TcExpCache *xcache = nullptr) {
     if (c.precision == GCGE_PREC_MIXED && !c.escalated && n >= kDigitMinRows)
-        oz_lincomb(n, k, m, X, ldx, C, ldc, Y, ldy, beta, incb, st, alpha, c.ozb.p, c.ozb.n);
+        oz_lincomb(n, k, m, X, ldx, C, ldc, Y, ldy, beta, incb, st, alpha, c.ozb.p, c.ozb.n,
+                   xcache);
     else
         lincomb(n, k, m, X, ldx, C, ldc, Y, ldy, beta, incb, st, alpha);
 }
@@ -192,6 +193,9 @@ int borth(SolverCtx &c, SparseMat *B, double *x, int ldx, int nrows, int start, 
     double *X1 = x + (size_t)start * ldx;
     bool upload_pending = false;  // a Cholesky-QR coefficient upload from hbuf in flight
     const double reorth_tol = 50.0 * 2.220446049250313e-16;  // src/ops_orth.c:404
+    // the prefix x[:, 0:start) does not change here: the exponent fields of
+    // its digit products are computed once for all projection passes
+    TcExpCache qcache, xcache;
     // Two rounds at most.  Cholesky-QR multiplies the block by R^-1, which
     // scales the rounding-level remainder of the prefix components by up to
     // kappa(R); when the first factor of a round was ill-conditioned
@@ -213,8 +217,9 @@ int borth(SolverCtx &c, SparseMat *B, double *x, int ldx, int nrows, int start, 
                     BX1 = c.T2.p;
                 }
                 dgram(c, nrows, start, k, x, ldx, BX1, useB ? ld : ldx, c.dC.p, start, c.gscr.p,
-                      c.gscr.n, st);
-                dlincomb(c, nrows, start, k, x, ldx, c.dC.p, start, X1, ldx, c.one.p, 0, st, -1.0);
+                      c.gscr.n, st, &qcache);
+                dlincomb(c, nrows, start, k, x, ldx, c.dC.p, start, X1, ldx, c.one.p, 0, st, -1.0,
+                         &xcache);
                 if (pass >= 1 || max_reorth == 0) {
                     if (device_absmax(start, k, c.dC.p, start) < reorth_tol) {
                         bx1_kept = useB;
@@ -352,9 +357,12 @@ struct BgsOrth {
             BX0 = c.T2.p;
             ldb = c.ld;
         }
+        TcExpCache qcache, xcache;  // B X0 and X0 stay unchanged over the passes
         for (int pass = 0; pass < 1 + max_reorth; ++pass) {
-            dgram(c, nrows, n0, n1, BX0, ldb, X1, ldx, c.dC.p, n0, c.gscr.p, c.gscr.n, st);
-            dlincomb(c, nrows, n0, n1, X0, ldx, c.dC.p, n0, X1, ldx, c.one.p, 0, st, -1.0);
+            dgram(c, nrows, n0, n1, BX0, ldb, X1, ldx, c.dC.p, n0, c.gscr.p, c.gscr.n, st,
+                  &qcache);
+            dlincomb(c, nrows, n0, n1, X0, ldx, c.dC.p, n0, X1, ldx, c.one.p, 0, st, -1.0,
+                     &xcache);
             if (absmax_dev(n0, n1, c.dC.p, n0) < kReorthTol) break;
         }
     }
@@ -477,6 +485,7 @@ struct BgsOrth {
         if (start > 0) {
             const int k = end - start;
             double *X1 = x + (size_t)start * ldx;
+            TcExpCache qcache, xcache;  // the prefix stays unchanged over the passes
             for (int pass = 0; pass < 1 + max_reorth; ++pass) {
                 const double *BX1 = X1;
                 int ldb = ldx;
@@ -485,8 +494,10 @@ struct BgsOrth {
                     BX1 = c.T2.p;
                     ldb = c.ld;
                 }
-                dgram(c, nrows, start, k, x, ldx, BX1, ldb, c.dC.p, start, c.gscr.p, c.gscr.n, st);
-                dlincomb(c, nrows, start, k, x, ldx, c.dC.p, start, X1, ldx, c.one.p, 0, st, -1.0);
+                dgram(c, nrows, start, k, x, ldx, BX1, ldb, c.dC.p, start, c.gscr.p, c.gscr.n, st,
+                      &qcache);
+                dlincomb(c, nrows, start, k, x, ldx, c.dC.p, start, X1, ldx, c.one.p, 0, st, -1.0,
+                         &xcache);
                 if (absmax_dev(start, k, c.dC.p, start) < kReorthTol) break;
             }
         }

@@ -519,10 +519,11 @@ void launch_oz_bn(const OzArgs &a, int bn, dim3 grid, cudaStream_t st) {
 // C (m x w, ldc) = Q^T P for Q n x m (ldq), P n x w (ldp); scratch holds the
 // split-k partials (scratch_elems doubles).
 void oz_gram(int n, int m, int w, const double *Q, int ldq, const double *P, int ldp, double *C,
-             int ldc, double *scratch, size_t scratch_elems, cudaStream_t st) {
+             int ldc, double *scratch, size_t scratch_elems, cudaStream_t st,
+             TcExpCache *cache) {
     if (m <= 0 || w <= 0) return;
     if (tc_digits_available()) {
-        tc_gram(n, m, w, Q, ldq, P, ldp, C, ldc, scratch, scratch_elems, st);
+        tc_gram(n, m, w, Q, ldq, P, ldp, C, ldc, scratch, scratch_elems, st, cache);
         return;
     }
     if (n <= 0) {
@@ -564,7 +565,7 @@ size_t oz_lincomb_scratch_bytes(int k, int m) {
 
 void oz_lincomb(int n, int k, int m, const double *X, int ldx, const double *C, int ldc,
                 double *Y, int ldy, const double *beta_dev, int incb, cudaStream_t st,
-                double alpha, void *scratch, size_t scratch_bytes) {
+                double alpha, void *scratch, size_t scratch_bytes, TcExpCache *cache) {
     if (n <= 0 || m <= 0) return;
     if (k <= 0) {
         lincomb(n, k, m, X, ldx, C, ldc, Y, ldy, beta_dev, incb, st, alpha);
@@ -572,7 +573,7 @@ void oz_lincomb(int n, int k, int m, const double *X, int ldx, const double *C, 
     }
     if (tc_digits_available()) {
         tc_lincomb(n, k, m, X, ldx, C, ldc, Y, ldy, beta_dev, incb, st, alpha, scratch,
-                   scratch_bytes);
+                   scratch_bytes, cache);
         return;
     }
     const int bn = oz_tile_n(m);

@@ -1156,7 +1156,7 @@ void tc_check_error(cudaStream_t st) {
 // tensor map cannot describe (an odd leading dimension, a base not 16-byte
 // aligned) go through the FP64 kernel.
 void tc_gram(int n, int m, int w, const double *Q, int ldq, const double *P, int ldp, double *C,
-             int ldc, double *scratch, size_t scratch_elems, cudaStream_t st) {
+             int ldc, double *scratch, size_t scratch_elems, cudaStream_t st, TcExpCache *cache) {
     if (m <= 0 || w <= 0) return;
     if (n <= 0) {
         GCGE_CUDA(cudaMemset2DAsync(C, sizeof(double) * ldc, 0, sizeof(double) * m, w, st));
@@ -1195,16 +1195,33 @@ void tc_gram(int n, int m, int w, const double *Q, int ldq, const double *P, int
     z = (int)((n + kc - 1) / kc);
     a.super_k = super_k;
     const int nsup = (n + super_k - 1) / super_k;
-    DevBuf<int> &eb = slot_stage().tc_exps;
-    eb.alloc((size_t)nsup * (m + w));
-    int *eA = eb.p, *eB = eb.p + (size_t)nsup * m;
     const long long pieces = (super_k + kTcExpPiece - 1) / kTcExpPiece;
-    if (pieces > 1) GCGE_CUDA(cudaMemsetAsync(eb.p, 0, sizeof(int) * (size_t)nsup * (m + w), st));
-    const int gx = (int)std::min<long long>(8 * sms, (nsup * pieces * std::max(m, w) + 7) / 8);
-    k_tc_expcols<<<gx, 256, 0, st>>>(Q, (size_t)ldq, n, m, super_k, nsup, eA);
-    k_tc_expcols<<<gx, 256, 0, st>>>(P, (size_t)ldp, n, w, super_k, nsup, eB);
-    GCGE_CHECK_LAUNCH();
-    count_launch(2);
+    auto expcols = [&](const double *X, int ld, int cols, int *out) {
+        if (pieces > 1) GCGE_CUDA(cudaMemsetAsync(out, 0, sizeof(int) * (size_t)nsup * cols, st));
+        const int gx = (int)std::min<long long>(8 * sms, (nsup * pieces * cols + 7) / 8);
+        k_tc_expcols<<<gx, 256, 0, st>>>(X, (size_t)ld, n, cols, super_k, nsup, out);
+        GCGE_CHECK_LAUNCH();
+        count_launch();
+    };
+    DevBuf<int> &eb = slot_stage().tc_exps;
+    int *eA, *eB;
+    if (cache) {
+        // Q's fields from the cache (computed there on first use)
+        if (!cache->matches(Q, (size_t)ldq, n, m, super_k, 0)) {
+            cache->e.alloc((size_t)nsup * m);
+            expcols(Q, ldq, m, cache->e.p);
+            cache->set(Q, (size_t)ldq, n, m, super_k, 0);
+        }
+        eA = cache->e.p;
+        eb.alloc((size_t)nsup * w);
+        eB = eb.p;
+    } else {
+        eb.alloc((size_t)nsup * (m + w));
+        eA = eb.p;
+        eB = eb.p + (size_t)nsup * m;
+        expcols(Q, ldq, m, eA);
+    }
+    expcols(P, ldp, w, eB);
     a.eA = eA;
     a.eB = eB;
     a.kchunk = (int)kc;
@@ -1228,7 +1245,7 @@ size_t tc_lincomb_scratch_bytes(int k, int m) {
 // adding its block's product to Y.
 void tc_lincomb(int n, int k, int m, const double *X, int ldx, const double *C, int ldc, double *Y,
                 int ldy, const double *beta_dev, int incb, cudaStream_t st, double alpha,
-                void *scratch, size_t scratch_bytes) {
+                void *scratch, size_t scratch_bytes, TcExpCache *cache) {
     if (n <= 0 || m <= 0) return;
     const int bn = tc_bn(m);
     CUtensorMap ma;
@@ -1274,13 +1291,19 @@ void tc_lincomb(int n, int k, int m, const double *X, int ldx, const double *C, 
             case 32: k_tc_bprep<32><<<pg, 256, 0, st>>>(Cb, (size_t)ldc, m, kb, kTcSuperLincomb, planes, bexps, a.nstages, 1); break;
             default: k_tc_bprep<48><<<pg, 256, 0, st>>>(Cb, (size_t)ldc, m, kb, kTcSuperLincomb, planes, bexps, a.nstages, 1); break;
         }
-        // exponent fields of the rows of X over the block's columns
-        DevBuf<int> &eb = slot_stage().tc_exps;
-        eb.alloc((size_t)n);
-        k_tc_exprows<<<dim3((n + 255) / 256, 1), 256, 0, st>>>(Xb, (size_t)ldx, n, kb,
-                                                             kTcSuperLincomb, eb.p);
-        GCGE_CHECK_LAUNCH();
-        count_launch(2);
+        // exponent fields of the rows of X over the block's columns (kept in
+        // the cache when the whole contraction is one block)
+        const bool cached = cache != nullptr && k <= kTcSuperLincomb;
+        DevBuf<int> &eb = cached ? cache->e : slot_stage().tc_exps;
+        count_launch();
+        if (!cached || !cache->matches(Xb, (size_t)ldx, n, kb, kTcSuperLincomb, 1)) {
+            eb.alloc((size_t)n);
+            k_tc_exprows<<<dim3((n + 255) / 256, 1), 256, 0, st>>>(Xb, (size_t)ldx, n, kb,
+                                                                 kTcSuperLincomb, eb.p);
+            GCGE_CHECK_LAUNCH();
+            count_launch();
+            if (cached) cache->set(Xb, (size_t)ldx, n, kb, kTcSuperLincomb, 1);
+        }
         a.bplanes = planes;
         a.eA = eb.p;
         a.eB = bexps;
