@@ -139,10 +139,10 @@ enum { PH_CHECK = 0, PH_P, PH_RR, PH_RRW, PH_EIG, PH_RV, PH_W, PH_LINSOL, PH_X, 
 // Products over the long (vector-length) dimension: FP64 FMA kernels in the
 // FP64 solve, FP64-accurate digit products on the tensor cores in the mixed
 // solve (same results to FP64 accuracy).  The digit products' error bound is
-// relative to the largest |x| |y| of each 64-row chunk: FP64-level for the
+// relative to the largest |x| |y| of each exponent window: FP64-level for the
 // n-row blocks, but not for the coefficient vectors of the projected space
 // (ComputeP's orthogonalisation and its P^T A P, contractions over s rows),
-// whose entries mix O(1) and ~1e-8 values in one chunk.  Products over fewer
+// whose entries mix O(1) and ~1e-8 values in one window.  Products over fewer
 // than kDigitMinRows rows - every projected-space product, since s stays
 // below it for nev up to ~300 - therefore stay FP64; they cost next to
 // nothing.
