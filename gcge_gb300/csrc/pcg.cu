@@ -130,6 +130,46 @@ __device__ __forceinline__ void gather_row(const int *__restrict__ col, const T 
     }
 }
 
+// The same sum for the NU column groups [U0, U0 + NU) only (all of them,
+// active or not), two matrix entries at a time (both entries' loads in
+// flight before their FMAs): the SpMM phase of wide blocks gathers a row in
+// two such halves, so that the accumulators of one half leave registers for
+// the second entry's loads (4.87 -> 4.75 s of inner solve per 128^3 solve;
+// four entries at a time: 4.81 s).
+template <typename T, int KP, int U0, int NU, int NE>
+__device__ __forceinline__ void gather_entries(const int *__restrict__ col,
+                                               const T *__restrict__ val, long long e0, int e,
+                                               const T *X, T (&acc)[NU * Pk<T>::L]) {
+    constexpr int L = Pk<T>::L;
+    int j[NE];
+    T v[NE];
+#pragma unroll
+    for (int d = 0; d < NE; ++d) {
+        j[d] = __ldg(col + e0 + 32LL * (e + d));
+        v[d] = __ldg(val + e0 + 32LL * (e + d));
+    }
+    Pk<T> x[NE][NU];
+#pragma unroll
+    for (int d = 0; d < NE; ++d)
+#pragma unroll
+        for (int u = 0; u < NU; ++u) x[d][u] = Pk<T>::ld(X + boff<T, KP>(j[d], U0 + u));
+#pragma unroll
+    for (int d = 0; d < NE; ++d)
+#pragma unroll
+        for (int u = 0; u < NU; ++u)
+#pragma unroll
+            for (int q = 0; q < L; ++q) acc[u * L + q] = fma(v[d], x[d][u].v[q], acc[u * L + q]);
+}
+template <typename T, int KP, int U0, int NU>
+__device__ __forceinline__ void gather_row_part(const int *__restrict__ col,
+                                                const T *__restrict__ val, long long e0,
+                                                int width, const T *X, T (&acc)[NU * Pk<T>::L]) {
+    int e = 0;
+#pragma unroll 1
+    for (; e + 1 < width; e += 2) gather_entries<T, KP, U0, NU, 2>(col, val, e0, e, X, acc);
+    if (e < width) gather_entries<T, KP, U0, NU, 1>(col, val, e0, e, X, acc);
+}
+
 __device__ __forceinline__ unsigned long long ld_acquire(const unsigned long long *p) {
     unsigned long long v;
     asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
@@ -341,6 +381,11 @@ __device__ __forceinline__ void grid_cols_sum(const double *part, double *out, d
     if (t < KP) out[t] = stripe[t];
     __syncthreads();
 }
+
+// Wide blocks (at least 8 column groups, an even number) gather the SpMM
+// phase in two halves of the column groups.
+template <typename T, int KP>
+constexpr bool kSplitGather = (KP / Pk<T>::L) >= 8 && (KP / Pk<T>::L) % 2 == 0;
 
 // Block shape by row width: 512 threads (two resident blocks, <= 64
 // registers) for rows up to 80 bytes, 512 threads (<= 128 registers) up to
@@ -595,37 +640,70 @@ k_block_pcg(PcgArgs<T> a) {
 #pragma unroll
             for (int u = 0; u < G; ++u) ga[u] = s_gact[u] != 0;
             for (int s = s0 + warp; s < s1; s += nwarps) {
-                T acc[KP];
-#pragma unroll
-                for (int c = 0; c < KP; ++c) acc[c] = T(0);
                 const long long beg = a.sp[s], end = a.sp[s + 1];
-                gather_row<T, KP>(a.col, a.val, beg + lane, (int)((end - beg) >> 5), a.P, ga,
-                                  acc);
-                const int row = s * 32 + lane;
-                if (row < n) {
+                const int width = (int)((end - beg) >> 5);
+                if constexpr (kSplitGather<T, KP>) {
+                    // one half of the column groups of a slice's rows: w, then the
+                    // partial sums of p^T w over those columns
+                    auto spmm_half = [&](auto half_tag, int s, int width, long long e0) {
+                        constexpr int H = decltype(half_tag)::value;
+                        constexpr int NU = G / 2, U0 = H * NU;
+                        T acc[NU * L];
 #pragma unroll
-                    for (int u = 0; u < G; ++u) {
-                        if (!ga[u]) continue;
-                        Pk<T> w;
+                        for (int c = 0; c < NU * L; ++c) acc[c] = T(0);
+                        gather_row_part<T, KP, U0, NU>(a.col, a.val, e0, width, a.P, acc);
+                        const int row = s * 32 + lane;
 #pragma unroll
-                        for (int q = 0; q < L; ++q) w.v[q] = acc[u * L + q];
-                        w.st(a.W + boff<T, KP>(row, u));
-                        const Pk<T> p = Pk<T>::ld(a.P + boff<T, KP>(row, u));
+                        for (int u = 0; u < NU; ++u) {
+                            if (!ga[U0 + u] || row >= n) {
 #pragma unroll
-                        for (int q = 0; q < L; ++q)
-                            acc[u * L + q] = s_act[u * L + q] ? p.v[q] * w.v[q] : T(0);
-                    }
+                                for (int q = 0; q < L; ++q) acc[u * L + q] = T(0);
+                                continue;
+                            }
+                            Pk<T> w;
+#pragma unroll
+                            for (int q = 0; q < L; ++q) w.v[q] = acc[u * L + q];
+                            w.st(a.W + boff<T, KP>(row, U0 + u));
+                            const Pk<T> p = Pk<T>::ld(a.P + boff<T, KP>(row, U0 + u));
+#pragma unroll
+                            for (int q = 0; q < L; ++q)
+                                acc[u * L + q] = s_act[(U0 + u) * L + q] ? p.v[q] * w.v[q] : T(0);
+                        }
+                        warp_cols_add<T, NU * L>(acc, wred[warp] + U0 * L, lane);
+                    };
+                    spmm_half(std::integral_constant<int, 0>{}, s, width, beg + lane);
+                    spmm_half(std::integral_constant<int, 1>{}, s, width, beg + lane);
                 } else {
+                    T acc[KP];
 #pragma unroll
                     for (int c = 0; c < KP; ++c) acc[c] = T(0);
-                }
+                    gather_row<T, KP>(a.col, a.val, beg + lane, width, a.P, ga, acc);
+                    const int row = s * 32 + lane;
+                    if (row < n) {
 #pragma unroll
-                for (int u = 0; u < G; ++u)
-                    if (!ga[u]) {
+                        for (int u = 0; u < G; ++u) {
+                            if (!ga[u]) continue;
+                            Pk<T> w;
 #pragma unroll
-                        for (int q = 0; q < L; ++q) acc[u * L + q] = T(0);
+                            for (int q = 0; q < L; ++q) w.v[q] = acc[u * L + q];
+                            w.st(a.W + boff<T, KP>(row, u));
+                            const Pk<T> p = Pk<T>::ld(a.P + boff<T, KP>(row, u));
+#pragma unroll
+                            for (int q = 0; q < L; ++q)
+                                acc[u * L + q] = s_act[u * L + q] ? p.v[q] * w.v[q] : T(0);
+                        }
+                    } else {
+#pragma unroll
+                        for (int c = 0; c < KP; ++c) acc[c] = T(0);
                     }
-                warp_cols_add<T, KP>(acc, wred[warp], lane);
+#pragma unroll
+                    for (int u = 0; u < G; ++u)
+                        if (!ga[u]) {
+#pragma unroll
+                            for (int q = 0; q < L; ++q) acc[u * L + q] = T(0);
+                        }
+                    warp_cols_add<T, KP>(acc, wred[warp], lane);
+                }
             }
             wred_flush(part_base(epoch + 1) + (size_t)blockIdx.x * KP);
         }
