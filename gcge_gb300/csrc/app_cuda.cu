@@ -846,16 +846,53 @@ int CUDA_MultiVecSetFromHost(void **mv, int start, int end, const double *host, 
         }
     });
 }
+// Columns of a device block stored by the GPU straight into page-locked host
+// memory (column c of src, leading dimension lds, into dst with ldd).  The
+// copy engine's first pass over data that kernels have just written runs at
+// a tenth of the link's rate on this part (0.3-0.9 s for the 5.4 GB of a
+// 128^3 solve's eigenvectors, against 28 ms for a repeated copy); stores from
+// a kernel go at the link's rate.
+__global__ void __launch_bounds__(256) k_cols_to_host(const double *__restrict__ src, size_t lds,
+                                                      double *__restrict__ dst, size_t ldd,
+                                                      int rows) {
+    const double *s = src + (size_t)blockIdx.y * lds;
+    double *d = dst + (size_t)blockIdx.y * ldd;
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (((reinterpret_cast<uintptr_t>(s) | reinterpret_cast<uintptr_t>(d)) & 15) == 0) {
+        const size_t h = (size_t)rows / 2;
+        for (; i < h; i += stride)
+            reinterpret_cast<double2 *>(d)[i] = reinterpret_cast<const double2 *>(s)[i];
+        if ((rows & 1) && blockIdx.x == 0 && threadIdx.x == 0) d[rows - 1] = s[rows - 1];
+    } else {
+        for (; i < (size_t)rows; i += stride) d[i] = s[i];
+    }
+}
+
 int CUDA_MultiVecGetToHost(void **mv, int start, int end, double *host, int ldh) {
     GCGE_TRY_RET({
         MultiVec *m = need_mv(mv, "CUDA_MultiVecGetToHost");
         check_range(m, start, end, "CUDA_MultiVecGetToHost");
         GCGE_REQUIRE(ldh >= m->nrows, GCGE_ERR_ARG, "CUDA_MultiVecGetToHost: ldh");
         if (end > start) {
-            GCGE_CUDA(cudaMemcpy2DAsync(host, sizeof(double) * ldh, m->data + (size_t)start * m->ld,
-                                        sizeof(double) * m->ld, sizeof(double) * m->nrows,
-                                        end - start, cudaMemcpyDeviceToHost, lib_stream()));
-            GCGE_CUDA(cudaStreamSynchronize(lib_stream()));
+            cudaStream_t st = lib_stream();
+            const double *src = m->data + (size_t)start * m->ld;
+            cudaPointerAttributes pa{};
+            const bool pinned = cudaPointerGetAttributes(&pa, host) == cudaSuccess &&
+                                pa.type == cudaMemoryTypeHost && pa.devicePointer != nullptr;
+            cudaGetLastError();
+            if (pinned && m->nrows > 0) {
+                const int bx = (int)std::min<long long>(64, ((long long)m->nrows + 511) / 512);
+                k_cols_to_host<<<dim3(bx, end - start), 256, 0, st>>>(
+                    src, m->ld, static_cast<double *>(pa.devicePointer), (size_t)ldh, m->nrows);
+                GCGE_CHECK_LAUNCH();
+                count_launch();
+            } else {
+                GCGE_CUDA(cudaMemcpy2DAsync(host, sizeof(double) * ldh, src,
+                                            sizeof(double) * m->ld, sizeof(double) * m->nrows,
+                                            end - start, cudaMemcpyDeviceToHost, st));
+            }
+            GCGE_CUDA(cudaStreamSynchronize(st));
         }
     });
 }

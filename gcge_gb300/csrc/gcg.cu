@@ -108,28 +108,46 @@ void SolverCtx::reserve(int n_, int nev_max, int nev_init, int bs, int spmm_nblo
 // ---------------------------------------------------------------- phase timer
 struct PhaseTimer {
     enum { kMaxEvents = 4096 };
-    std::vector<cudaEvent_t> ev;
+    // events come from a per-thread pool that lives as long as the thread: a
+    // solve marks ~12 phases per outer iteration, and creating and destroying
+    // thousands of events per solve cost the next synchronising call on the
+    // stream about 5 ms per outer iteration
+    static std::vector<cudaEvent_t> &pool() {
+        static thread_local std::vector<cudaEvent_t> p;
+        return p;
+    }
+    static int &depth() {
+        static thread_local int d = 0;
+        return d;
+    }
+    size_t used = 0;
     std::vector<int> ph;
     cudaStream_t st;
-    explicit PhaseTimer(cudaStream_t s) : st(s) {}
-    ~PhaseTimer() {
-        for (auto e : ev) cudaEventDestroy(e);
-    }
+    bool active;  // a solve started inside another one's callback records nothing
+    explicit PhaseTimer(cudaStream_t s) : st(s), active(depth()++ == 0) {}
+    ~PhaseTimer() { --depth(); }
+    PhaseTimer(const PhaseTimer &) = delete;
+    PhaseTimer &operator=(const PhaseTimer &) = delete;
     void mark(int phase) {
-        if ((int)ev.size() >= kMaxEvents) return;
-        cudaEvent_t e;
-        if (cudaEventCreate(&e) != cudaSuccess) return;
-        cudaEventRecord(e, st);
-        ev.push_back(e);
+        if (!active || (int)used >= kMaxEvents) return;
+        std::vector<cudaEvent_t> &p = pool();
+        if (used == p.size()) {
+            cudaEvent_t e;
+            if (cudaEventCreate(&e) != cudaSuccess) return;
+            p.push_back(e);
+        }
+        cudaEventRecord(p[used], st);
         ph.push_back(phase);
+        ++used;
     }
     void collect(double *out10) {
         for (int i = 0; i < 10; ++i) out10[i] = 0.0;
-        if (ev.size() < 2) return;
-        cudaEventSynchronize(ev.back());
-        for (size_t i = 0; i + 1 < ev.size(); ++i) {
+        if (used < 2) return;
+        const std::vector<cudaEvent_t> &p = pool();
+        cudaEventSynchronize(p[used - 1]);
+        for (size_t i = 0; i + 1 < used; ++i) {
             float ms = 0.f;
-            if (ph[i] >= 0 && ph[i] < 10 && cudaEventElapsedTime(&ms, ev[i], ev[i + 1]) == cudaSuccess)
+            if (ph[i] >= 0 && ph[i] < 10 && cudaEventElapsedTime(&ms, p[i], p[i + 1]) == cudaSuccess)
                 out10[ph[i]] += ms;
         }
     }
