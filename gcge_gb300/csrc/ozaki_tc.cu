@@ -741,7 +741,9 @@ __global__ void __launch_bounds__(kTcThreads, 1)
                         }
                     } else if (grow < a.M && gcol < a.N) {
                         double *dst = a.out + grow + (size_t)gcol * a.ldo;
-                        double y = a.alpha == 1.0 ? val : a.alpha * val;
+                        // alpha = +-1 needs no FP64 multiply (the sign folds
+                        // into the beta fma or the store)
+                        double y = a.alpha == 1.0 ? val : a.alpha == -1.0 ? -val : a.alpha * val;
                         if (a.accumulate) {
                             y += *dst;
                         } else if (a.beta != nullptr) {
@@ -775,15 +777,17 @@ __global__ void __launch_bounds__(kTcThreads, 1)
         TcCursor cons;
         cur_init<GRAM>(a, cons);
         int t = 0;        // digit stages produced
+        int sidx = 0;     // window of the current raw stage
         uint32_t s = 0, ph = 0;  // ring position and phase of stage t
         uint32_t qr = 0;  // raw stages read
         int em_a = 1;
         bool ok = true;
         while (ok && cons.valid) {
             const int ske = min(cons.w.ke, cons.sk + super_k);
-            const int sidx = (cons.sk - (GRAM ? 0 : cons.w.kb)) / super_k;
             if (cons.k0 == cons.sk) {
-                // a super-chunk starts: the exponent field of this thread's row
+                // a window starts: its index and the exponent field of this
+                // thread's row
+                sidx = (cons.sk - (GRAM ? 0 : cons.w.kb)) / super_k;
                 const int gr = cons.w.mt0 + ra;
                 em_a = gr < a.M ? __ldg(a.eA + (size_t)sidx * a.M + gr) : 1;
             }
