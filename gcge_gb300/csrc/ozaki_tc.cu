@@ -77,7 +77,7 @@ constexpr int kTcSuperLincomb = 3 * kTcDrainK;  // 432: K up to 432 in one windo
 // Byte layout of one operand tile of R rows in a digit stage: plane i
 // (digit), k-group g (8 consecutive k), row r: i * plane + g * lbo +
 // (r / 8) * 128 + (r % 8) * 16, with lbo = R * 16 + 16 (the pad keeps the
-// producers' 16-byte stores of the k-groups of a row on different banks).
+// 16-byte core-matrix rows of different k-groups on different banks).
 __host__ __device__ constexpr uint32_t tc_lbo(int rows) { return (uint32_t)rows * 16u + 16u; }
 __host__ __device__ constexpr uint32_t tc_plane(int rows) { return kTcKGroups * tc_lbo(rows); }
 __host__ __device__ constexpr uint32_t tc_tile_bytes(int rows) {
@@ -129,7 +129,7 @@ struct TcArgs {
     int M, N, K;
     const double *A;  // gram: Q (k, r) at A[k + r lda]; lincomb: X (r, k) at A[r + k lda]
     size_t lda;
-    int super_k;      // k per shared exponent (multiple of kTcDrainK)
+    int super_k;      // k per exponent window (multiple of kTcDrainK)
     int kchunk;       // gram: k per work item (multiple of super_k)
     int items;        // work items
     int mtiles, ntiles;
@@ -138,11 +138,11 @@ struct TcArgs {
     const double *beta;
     int incb;
     double alpha;
-    // exponent fields: gram: eA [super][M], eB [super][N]; lincomb: eA
-    // [super][M] (rows of X), eB = the prepared right operand's [ntile][super][BN]
+    // exponent fields: gram: eA [window][M], eB [window][N]; lincomb: eA
+    // [window][M] (rows of X), eB = the prepared right operand's [ntile][window][BN]
     const int *eA, *eB;
     const uint8_t *bplanes;  // lincomb: [ntile][digit stage][b_bytes]
-    int nstages, nsup;       // lincomb: digit stages and super-chunks of K
+    int nstages, nsup;       // lincomb: digit stages and exponent windows of K
     int accumulate;          // lincomb: add to Y (later blocks of a split contraction)
     int *error;
 };
@@ -460,8 +460,8 @@ __device__ __forceinline__ TcItem tc_item(const TcArgs &a, int it) {
     }
     return w;
 }
-// A position in this CTA's sequence of raw stages: work item, super-chunk
-// start, raw stage start.
+// A position in this CTA's sequence of raw stages: work item, window start,
+// raw stage start.
 struct TcCursor {
     TcItem w;
     int it, sk, k0;
@@ -660,13 +660,13 @@ __global__ void __launch_bounds__(kTcThreads, 1)
         constexpr int CPW = BN / 4;
         const int q = warp & 3, cp = warp >> 2;
         const int drow = q * 32 + lane;
-        // per column the level sums of the current super-chunk, sum over l of
+        // per column the level sums of the current window, sum over l of
         // L_l 2^(8 (6 - l)), as a 96-bit integer (w0 least significant)
         uint32_t w0[CPW], w1[CPW], w2[CPW];
 #pragma unroll
         for (int c = 0; c < CPW; ++c) w0[c] = w1[c] = w2[c] = 0;
 
-        // the next chunk to drain: work item, super-chunk start, chunk start,
+        // the next chunk to drain: work item, window start, chunk start,
         // index of its last digit stage
         TcItem dw{0, 0, 0, 0};
         int dit = blockIdx.x, dsk = 0, dk0 = 0, dlast = 0;
@@ -712,10 +712,10 @@ __global__ void __launch_bounds__(kTcThreads, 1)
             ++dn;
             const int ske = min(dw.ke, dsk + super_k);
             if (dk0 + kTcDrainK >= ske) {
-                // the super-chunk ends: its sums, w 2^(er + ec - 2106)
+                // the window ends: its sums, w 2^(er + ec - 2106)
                 // converted with integer instructions, go into the work item's
-                // split-k partial (Gram; FP64 accumulators for a work item of
-                // several super-chunks) or straight into Y (a linear combination)
+                // split-k partial (Gram; a work item of several windows adds
+                // them there) or straight into Y (a linear combination)
                 const int sidx = (dsk - (GRAM ? 0 : dw.kb)) / super_k;
                 const int grow = dw.mt0 + drow;
                 const int er = grow < a.M ? __ldg(a.eA + (size_t)sidx * a.M + grow) : 1;
@@ -974,9 +974,9 @@ __global__ void __launch_bounds__(256) k_tc_exprows(const double *__restrict__ X
 }
 
 // Right operand of a linear combination (C, K x N, element (k, c) at
-// C[k + c ldc]) prepared once per call: block (super-chunk, n tile) writes the
+// C[k + c ldc]) prepared once per call: block (window, n tile) writes the
 // exponent fields of its BN columns and the digit planes of each 16-k digit
-// stage of the super-chunk in the stage layout of the product kernel.
+// stage of the window in the stage layout of the product kernel.
 template <int BN>
 __global__ void __launch_bounds__(256) k_tc_bprep(const double *__restrict__ C, size_t ldc, int N,
                                                   int K, int super_k, uint8_t *__restrict__ planes,
@@ -1190,8 +1190,8 @@ void tc_gram(int n, int m, int w, const double *Q, int ldq, const double *P, int
     long long kc = ((long long)(n + z - 1) / z + kTcDrainK - 1) / kTcDrainK * kTcDrainK;
     GCGE_REQUIRE((size_t)m * w <= scratch_elems, GCGE_ERR_ARG, "tc_gram: scratch too small");
     while ((size_t)((n + kc - 1) / kc) * m * w > scratch_elems) kc *= 2;
-    // the exponent window: the whole k range of a work item (one super-chunk),
-    // or super-chunks of the largest window when the range is longer.  One
+    // the exponent window: the whole k range of a work item, or windows of
+    // the largest size when the range is longer.  One
     // exponent per column over K rows bounds the error of an entry by
     // 2^-54 sqrt(K) |x| |y|, below the FP64 dot product's K 2^-53 |x| |y|.
     if (kc > kTcSuperGramMax) kc = (kc + kTcSuperGramMax - 1) / kTcSuperGramMax * kTcSuperGramMax;
