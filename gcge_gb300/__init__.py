@@ -46,7 +46,7 @@ EXPORTED_SYMBOLS = [
     "MultiVecOrthSetup_ModifiedGramSchmidt", "MultiVecOrthSetup_BinaryGramSchmidt",
     "EigenSolverSetParametersFromCommandLine_GCG", "CUDA_MatAxpby",
     "MultiLinearSolverSetup_BlockPCG", "GCGE_TestBlockPCGBarrierTimeout",
-    "GCGE_BenchDenseProduct",
+    "GCGE_BenchDenseProduct", "GCGE_SetSpMMTuning", "GCGE_SpMMTuneCandidates", "GCGE_SpMMTune",
 ]
 
 _lib = None
@@ -112,7 +112,8 @@ def load(build_if_missing: bool = False) -> ctypes.CDLL:
                  "GCGE_Solve", "GCGE_Prepare", "GCGE_PreparedSolve", "GCGE_SetPrecision",
                  "GCGE_GetSolveInfo", "GCGE_BenchSpMM", "ops_cuda_last_error", "CUDA_MultiVecSize",
                  "CUDA_MatNnz", "GCGE_DenseEig", "GCGE_BlockPCG", "GCGE_BOrth",
-                 "GCGE_TimerStart", "GCGE_GramNoAlloc", "GCGE_DenseGram", "GCGE_DenseLinComb"):
+                 "GCGE_TimerStart", "GCGE_GramNoAlloc", "GCGE_DenseGram", "GCGE_DenseLinComb",
+                 "GCGE_SetSpMMTuning", "GCGE_SpMMTuneCandidates", "GCGE_SpMMTune"):
         getattr(lib, name).restype = ctypes.c_int
     lib.GCGE_TimerStop.restype = ctypes.c_double
     lib.GCGE_HostAlloc.restype = ctypes.c_void_p
@@ -622,6 +623,45 @@ def bench_spmm(A, k: int, fp32: bool, reps: int = 20):
         if st != GCGE_OK:
             raise GCGEError(st, "GCGE_BenchSpMM")
         return ms.value, by.value
+    finally:
+        ops.close()
+
+
+def set_spmm_tuning(on: int):
+    """1: tune the column split of SpMMs; 0: fixed 40-column launches;
+    -1: off, and forget the tuned choices."""
+    st = load().GCGE_SetSpMMTuning(ctypes.c_int(on))
+    if st != GCGE_OK:
+        raise GCGEError(st, "GCGE_SetSpMMTuning")
+
+
+def spmm_tune_candidates(k: int) -> list:
+    """Candidate launch widths of an SpMM of k columns, fewest launches first."""
+    lib = load()
+    buf = (ctypes.c_int * 16)()
+    cnt = ctypes.c_int()
+    st = lib.GCGE_SpMMTuneCandidates(ctypes.c_int(k), buf, ctypes.c_int(16), ctypes.byref(cnt))
+    if st != GCGE_OK:
+        raise GCGEError(st, "GCGE_SpMMTuneCandidates")
+    return list(buf[:min(cnt.value, 16)])
+
+
+def spmm_tune(A, k: int, fp32: bool):
+    """Time every candidate column split of an SpMM of k columns of A; the
+    choice is kept for later SpMMs of A's shape.  Returns (chosen width,
+    {width: ms})."""
+    lib = load()
+    ops = CudaOps()
+    try:
+        h = ops.mat(A)
+        chunk, cnt = ctypes.c_int(), ctypes.c_int()
+        ms = (ctypes.c_double * 16)()
+        st = lib.GCGE_SpMMTune(h, ctypes.c_int(k), ctypes.c_int(1 if fp32 else 0),
+                               ctypes.byref(chunk), ms, ctypes.c_int(16), ctypes.byref(cnt))
+        if st != GCGE_OK:
+            raise GCGEError(st, "GCGE_SpMMTune")
+        widths = spmm_tune_candidates(k)
+        return chunk.value, dict(zip(widths, ms[:min(cnt.value, 16)]))
     finally:
         ops.close()
 

@@ -1248,17 +1248,16 @@ double GCGE_TimerStop(void) {
     }
 }
 
-int GCGE_BenchSpMM(void *mat, int k, int fp32, int reps, double *ms_per_launch,
-                   double *bytes_per_launch) {
-    GCGE_TRY_RET({
-        SparseMat *A = as_mat(mat);
-        GCGE_REQUIRE(A != nullptr, GCGE_ERR_HANDLE, "GCGE_BenchSpMM: not a CUDA matrix");
-        GCGE_REQUIRE(k >= 1 && reps >= 1, GCGE_ERR_ARG, "GCGE_BenchSpMM: k, reps");
-        cudaStream_t st = lib_stream();
-        const int n = A->n, ld = (n + 31) / 32 * 32;
-        const int vs = fp32 ? 4 : 8;
-        DevBuf<double> X, Y, tmp;
-        DevBuf<float> X32, Y32, V32;
+// Device operands of the SpMM measurements: k seeded uniform columns (and
+// their FP32 copy with the matrix's FP32 values when fp32), Y of the same
+// shape, all owned by the call.
+struct SpmmOperands {
+    int n = 0, ld = 0;
+    DevBuf<double> X, Y, tmp;
+    DevBuf<float> X32, Y32, V32;
+    SpmmOperands(const SparseMat *A, int k, bool fp32, cudaStream_t st) {
+        n = A->n;
+        ld = (n + 31) / 32 * 32;
         X.alloc((size_t)ld * k);
         fill_uniform(n, k, X.p, ld, 12345, st);
         if (fp32) {
@@ -1272,7 +1271,59 @@ int GCGE_BenchSpMM(void *mat, int k, int fp32, int reps, double *ms_per_launch,
         } else {
             Y.alloc((size_t)ld * k);
         }
-        // warm-up
+    }
+};
+
+int GCGE_SetSpMMTuning(int on) {
+    set_spmm_tuning(on > 0);
+    if (on < 0) clear_spmm_tuning();
+    return GCGE_OK;
+}
+
+int GCGE_SpMMTuneCandidates(int k, int *chunks, int cap, int *count) {
+    if (k < 1 || count == nullptr || (cap > 0 && chunks == nullptr)) {
+        set_error(GCGE_ERR_ARG, "GCGE_SpMMTuneCandidates: k < 1 or null output");
+        return GCGE_ERR_ARG;
+    }
+    const std::vector<int> p = spmm_split_candidates(k);
+    *count = (int)p.size();
+    for (int i = 0; i < (int)p.size() && i < cap; ++i) chunks[i] = (k + p[i] - 1) / p[i];
+    return GCGE_OK;
+}
+
+int GCGE_SpMMTune(void *mat, int k, int fp32, int *chunk, double *ms, int cap, int *count) {
+    GCGE_TRY_RET({
+        SparseMat *A = as_mat(mat);
+        GCGE_REQUIRE(A != nullptr, GCGE_ERR_HANDLE, "GCGE_SpMMTune: not a CUDA matrix");
+        GCGE_REQUIRE(k >= 1 && chunk != nullptr && count != nullptr && (cap <= 0 || ms != nullptr),
+                     GCGE_ERR_ARG, "GCGE_SpMMTune: k < 1 or null output");
+        cudaStream_t st = lib_stream();
+        SpmmOperands o(A, k, fp32 != 0, st);
+        std::vector<double> t;
+        const int p = fp32 ? spmm_tuned_split<float>(A->pat, o.V32.p, o.X32.p, o.ld, o.Y32.p,
+                                                      o.ld, k, st, &t)
+                           : spmm_tuned_split<double>(A->pat, A->val.p, o.X.p, o.ld, o.Y.p,
+                                                       o.ld, k, st, &t);
+        *chunk = (k + p - 1) / p;
+        *count = (int)t.size();
+        for (int i = 0; i < (int)t.size() && i < cap; ++i) ms[i] = t[i];
+        GCGE_CUDA(cudaStreamSynchronize(st));
+    });
+}
+
+int GCGE_BenchSpMM(void *mat, int k, int fp32, int reps, double *ms_per_launch,
+                   double *bytes_per_launch) {
+    GCGE_TRY_RET({
+        SparseMat *A = as_mat(mat);
+        GCGE_REQUIRE(A != nullptr, GCGE_ERR_HANDLE, "GCGE_BenchSpMM: not a CUDA matrix");
+        GCGE_REQUIRE(k >= 1 && reps >= 1, GCGE_ERR_ARG, "GCGE_BenchSpMM: k, reps");
+        cudaStream_t st = lib_stream();
+        const int vs = fp32 ? 4 : 8;
+        SpmmOperands o(A, k, fp32 != 0, st);
+        const int n = o.n, ld = o.ld;
+        DevBuf<double> &X = o.X, &Y = o.Y;
+        DevBuf<float> &X32 = o.X32, &Y32 = o.Y32, &V32 = o.V32;
+        // warm-up (with tuning on, the first call picks the column split)
         for (int r = 0; r < 3; ++r) {
             if (fp32) spmm<float>(A->pat, V32.p, X32.p, ld, Y32.p, ld, k, st);
             else spmm<double>(A->pat, A->val.p, X.p, ld, Y.p, ld, k, st);

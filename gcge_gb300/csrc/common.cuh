@@ -224,6 +224,17 @@ int residual_norms(const SellPattern &pa, const double *va, const SellPattern *p
                    double *partial, int kmax, cudaStream_t st, double *ax = nullptr,
                    double *bx = nullptr, int ldo = 0);
 int spmm_blocks(const SellPattern &pat);
+// Column-split tuner of spmm (spmm.cu): candidate launch counts p for k
+// columns (each launch ceil(k / p) columns), the switch (initially from the
+// environment variable GCGE_SPMM_TUNE), the cache reset, and the tuned p for
+// a call (timing every candidate when ms_out is given).
+std::vector<int> spmm_split_candidates(int k);
+bool spmm_tuning_on();
+void set_spmm_tuning(bool on);
+void clear_spmm_tuning();
+template <typename T>
+int spmm_tuned_split(const SellPattern &pat, const T *val, const T *X, int ldx, T *Y, int ldy,
+                     int k, cudaStream_t st, std::vector<double> *ms_out);
 // Smallest block-PCG row width >= k (whole 16-byte column groups).
 int rows_width(int k, int elem_bytes);
 

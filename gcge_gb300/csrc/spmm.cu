@@ -10,7 +10,12 @@
 // Every column's accumulator stays in registers, so the matrix is streamed
 // once for all k columns (reference: one column at a time, app/app_ccs.c:120-131).
 #include <algorithm>
+#include <atomic>
+#include <cstdlib>
+#include <limits>
+#include <map>
 #include <numeric>
+#include <tuple>
 
 #include "common.cuh"
 
@@ -141,19 +146,163 @@ k_residual(const long long *__restrict__ sa, const int *__restrict__ ca,
 
 constexpr int kMaxChunk = 40;
 
+// Register width (accumulators per lane) GCGE_K_DISPATCH gives kc columns.
+static int spmm_dispatch_width(int kc) {
+    return kc <= 4 ? 4 : kc <= 8 ? 8 : kc <= 16 ? 16 : kc <= 24 ? 24 : kc <= 32 ? 32 : 40;
+}
+
+// Y = M X in launches of `chunk` columns each (the last one narrower): each
+// launch streams the matrix once and keeps its columns' sums in registers.
+// Every column's sum runs over the same entries in the same order whatever
+// the chunk, so the result does not depend on it.
 template <typename T>
-void spmm(const SellPattern &pat, const T *val, const T *X, int ldx, T *Y, int ldy, int k,
-          cudaStream_t st) {
-    if (k <= 0 || pat.n == 0) return;
+static void spmm_split(const SellPattern &pat, const T *val, const T *X, int ldx, T *Y, int ldy,
+                       int k, int chunk, cudaStream_t st) {
     const int blocks = spmm_blocks(pat);
-    for (int c0 = 0; c0 < k; c0 += kMaxChunk) {
-        const int kc = std::min(kMaxChunk, k - c0);
+    for (int c0 = 0; c0 < k; c0 += chunk) {
+        const int kc = std::min(chunk, k - c0);
         GCGE_K_DISPATCH(kc, (k_spmm<T, KT><<<blocks, kSpmmThreads, 0, st>>>(
                                 pat.slice_ptr.p, pat.col.p, val, pat.n, pat.nslices,
                                 X + (size_t)c0 * ldx, ldx, Y + (size_t)c0 * ldy, ldy, kc)));
         GCGE_CHECK_LAUNCH();
         count_launch();
     }
+}
+
+// ---------------------------------------------------------------- tuning
+// The column split of an SpMM is a trade: wide launches read the matrix fewer
+// times, narrow ones need fewer registers per lane and so keep more warps
+// resident to hide the gathers' latency.  Which wins depends on the matrix
+// (entries per row, locality of its columns) and the device, so the tuner
+// measures it.  Candidates split k columns into p equal launches, p from
+// ceil(k / 40) up while a launch keeps at least 8 columns; of the p that give
+// the same register width only the smallest is kept (more launches of the
+// same width only re-read the matrix).
+std::vector<int> spmm_split_candidates(int k) {
+    std::vector<int> out;
+    if (k <= 0) return out;
+    int last = -1;
+    for (int p = (k + kMaxChunk - 1) / kMaxChunk;; ++p) {
+        const int chunk = (k + p - 1) / p;
+        if (!out.empty() && chunk < 8) break;
+        const int w = spmm_dispatch_width(chunk);
+        if (w != last) {
+            out.push_back(p);
+            last = w;
+        }
+        if (chunk <= 8) break;
+    }
+    return out;
+}
+
+namespace {
+// A tuned split is kept per device, value type, matrix shape (rows and
+// stored entries) and column class (k rounded up to a multiple of 8).
+struct SpmmTuneKey {
+    int dev, elem, n, kclass;
+    long long padded;
+    bool operator<(const SpmmTuneKey &o) const {
+        return std::tie(dev, elem, n, kclass, padded) <
+               std::tie(o.dev, o.elem, o.n, o.kclass, o.padded);
+    }
+};
+std::mutex g_tune_mu;
+std::map<SpmmTuneKey, int> g_tune;  // chosen number of launches p
+// -1: not yet read from the environment (GCGE_SPMM_TUNE), 0 off, 1 on
+std::atomic<int> g_tune_on{-1};
+
+struct EventPair {
+    cudaEvent_t a = nullptr, b = nullptr;
+    EventPair() {
+        GCGE_CUDA(cudaEventCreate(&a));
+        cudaError_t e = cudaEventCreate(&b);
+        if (e != cudaSuccess) {
+            cudaEventDestroy(a);
+            GCGE_CUDA(e);
+        }
+    }
+    ~EventPair() {
+        cudaEventDestroy(a);
+        cudaEventDestroy(b);
+    }
+};
+}  // namespace
+
+bool spmm_tuning_on() {
+    int v = g_tune_on.load(std::memory_order_relaxed);
+    if (v < 0) {
+        const char *e = getenv("GCGE_SPMM_TUNE");
+        int want = (e != nullptr && atoi(e) != 0) ? 1 : 0, expect = -1;
+        g_tune_on.compare_exchange_strong(expect, want);
+        v = g_tune_on.load();
+    }
+    return v == 1;
+}
+
+void set_spmm_tuning(bool on) { g_tune_on.store(on ? 1 : 0); }
+
+void clear_spmm_tuning() {
+    std::lock_guard<std::mutex> g(g_tune_mu);
+    g_tune.clear();
+}
+
+// The number of launches p for an SpMM of k columns: the cached choice for
+// this matrix shape and column class, or, on the first call (and always when
+// ms_out is given), each candidate timed with CUDA events on `st` (one
+// untimed run, then kTuneReps timed runs) on the caller's own X and Y, which
+// hold M X after every run.  A later candidate must beat the best by 2% to
+// replace it, so noise does not pick more launches.  Not tuned while `st` is
+// being captured into a graph (the timing waits on the host).
+template <typename T>
+int spmm_tuned_split(const SellPattern &pat, const T *val, const T *X, int ldx, T *Y, int ldy,
+                     int k, cudaStream_t st, std::vector<double> *ms_out) {
+    constexpr int kTuneReps = 3;
+    const std::vector<int> cand = spmm_split_candidates(k);
+    if (cand.empty()) return 1;
+    if (cand.size() == 1 && ms_out == nullptr) return cand[0];
+    const SpmmTuneKey key{current_device(), (int)sizeof(T), pat.n, (k + 7) / 8, pat.padded};
+    if (ms_out == nullptr) {
+        std::lock_guard<std::mutex> g(g_tune_mu);
+        auto it = g_tune.find(key);
+        if (it != g_tune.end()) return it->second;
+    }
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    GCGE_CUDA(cudaStreamIsCapturing(st, &cs));
+    if (cs != cudaStreamCaptureStatusNone) return cand[0];
+    EventPair ev;
+    double best = std::numeric_limits<double>::infinity();
+    int bestp = cand[0];
+    for (int p : cand) {
+        const int chunk = (k + p - 1) / p;
+        spmm_split(pat, val, X, ldx, Y, ldy, k, chunk, st);
+        GCGE_CUDA(cudaEventRecord(ev.a, st));
+        for (int r = 0; r < kTuneReps; ++r) spmm_split(pat, val, X, ldx, Y, ldy, k, chunk, st);
+        GCGE_CUDA(cudaEventRecord(ev.b, st));
+        GCGE_CUDA(cudaEventSynchronize(ev.b));
+        float ms = 0.f;
+        GCGE_CUDA(cudaEventElapsedTime(&ms, ev.a, ev.b));
+        const double t = (double)ms / kTuneReps;
+        if (ms_out) ms_out->push_back(t);
+        if (t < best * 0.98) {
+            best = t;
+            bestp = p;
+        }
+    }
+    std::lock_guard<std::mutex> g(g_tune_mu);
+    g_tune[key] = bestp;
+    return bestp;
+}
+
+template <typename T>
+void spmm(const SellPattern &pat, const T *val, const T *X, int ldx, T *Y, int ldy, int k,
+          cudaStream_t st) {
+    if (k <= 0 || pat.n == 0) return;
+    int chunk = kMaxChunk;
+    if (k > 8 && spmm_tuning_on()) {
+        const int p = spmm_tuned_split<T>(pat, val, X, ldx, Y, ldy, k, st, nullptr);
+        chunk = (k + p - 1) / p;
+    }
+    spmm_split(pat, val, X, ldx, Y, ldy, k, chunk, st);
 }
 
 int residual_norms(const SellPattern &pa, const double *va, const SellPattern *pb,
@@ -178,6 +327,10 @@ template void spmm<double>(const SellPattern &, const double *, const double *, 
                            int, int, cudaStream_t);
 template void spmm<float>(const SellPattern &, const float *, const float *, int, float *, int,
                           int, cudaStream_t);
+template int spmm_tuned_split<double>(const SellPattern &, const double *, const double *, int,
+                                      double *, int, int, cudaStream_t, std::vector<double> *);
+template int spmm_tuned_split<float>(const SellPattern &, const float *, const float *, int,
+                                     float *, int, int, cudaStream_t, std::vector<double> *);
 }  // namespace gcge
 
 // ==================================================================== widths

@@ -191,6 +191,29 @@ void GCGE_PreparedDestroy(gcge_prepared **prep);
 int GCGE_BenchSpMM(void *mat, int k, int fp32, int reps, double *ms_per_launch,
                    double *bytes_per_launch);
 
+/* ---- SpMM column-split autotuner ----------------------------------------
+ * An SpMM of k columns (MatDotMultiVec and the solver's own products; the
+ * reference's app_ccs multiplies one column at a time, app/app_ccs.c:120-131)
+ * runs as p launches of ceil(k / p) columns: each launch streams the matrix
+ * once and keeps its columns' sums in registers, so few wide launches read
+ * the matrix least and narrow ones keep more warps resident.  With tuning
+ * on, the first SpMM of a matrix shape (rows, stored entries, value type) and
+ * column class (k rounded up to a multiple of 8) on a device times every
+ * candidate split with CUDA events on the calling stream and keeps the
+ * fastest for the process.  Results are bitwise the same for every split.
+ * Off until GCGE_SetSpMMTuning(1) or the environment variable
+ * GCGE_SPMM_TUNE=1 at the first SpMM.  No counterpart in the reference. */
+/* on = 1: tune; 0: fixed 40-column launches; -1: off and forget the choices. */
+int GCGE_SetSpMMTuning(int on);
+/* The candidate launch widths for k columns, fewest launches first:
+ * chunks[0 .. min(*count, cap)).  Host only (needs no device). */
+int GCGE_SpMMTuneCandidates(int k, int *chunks, int cap, int *count);
+/* Time every candidate split of an SpMM of k columns of a CUDA matrix (FP32
+ * values and columns when fp32) on seeded device columns owned by the call,
+ * keep the choice for later SpMMs of that shape, and return the chosen
+ * launch width and each candidate's average ms (ms[0 .. min(*count, cap))). */
+int GCGE_SpMMTune(void *mat, int k, int fp32, int *chunk, double *ms, int cap, int *count);
+
 /* One long-dimension dense product on device data the call generates
  * (seeded uniform values), timed with CUDA events on the library stream
  * after one untimed call: kind 0 = Gram C (m x w) = Q^T P with Q n x m and

@@ -156,3 +156,35 @@ int main(void) {
     py = [ctypes.sizeof(G.Request), G.Request.info.offset, G.Request.status.offset,
           G.Request.t_end.offset, ctypes.sizeof(G.SolveInfo), G.SolveInfo.pcg_kernel_bytes.offset]
     assert c == py
+
+
+def test_spmm_tuner_candidates_without_gpu(lib):
+    """The tuner's candidate splits (host logic of gcge_gb300/csrc/spmm.cu):
+    p launches of ceil(k / p) columns for p from ceil(k / 40) up while a launch
+    keeps 8 columns, one p per register width (4, 8, 16, 24, 32, 40)."""
+    def width(c):
+        return next(w for w in (4, 8, 16, 24, 32, 40) if c <= w)
+
+    def rule(k):
+        out, last, p = [], None, -(-k // 40)
+        while True:
+            c = -(-k // p)
+            if out and c < 8:
+                return out
+            if width(c) != last:
+                out.append(c)
+                last = width(c)
+            if c <= 8:
+                return out
+            p += 1
+
+    for k in list(range(1, 130)) + [200, 320, 400]:
+        got = G.spmm_tune_candidates(k)
+        assert got == rule(k), k
+        assert all(1 <= c <= 40 for c in got) and got == sorted(got, reverse=True)
+        # every split covers the k columns with at most 40 per launch
+        assert -(-k // got[0]) == -(-k // 40)
+    assert G.spmm_tune_candidates(40) == [40, 20, 14, 8]
+    cnt = ctypes.c_int()
+    assert lib.GCGE_SpMMTuneCandidates(0, None, 0, ctypes.byref(cnt)) == G.GCGE_ERR_ARG
+    assert lib.GCGE_SetSpMMTuning(0) == G.GCGE_OK
