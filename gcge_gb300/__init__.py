@@ -47,6 +47,8 @@ EXPORTED_SYMBOLS = [
     "EigenSolverSetParametersFromCommandLine_GCG", "CUDA_MatAxpby",
     "MultiLinearSolverSetup_BlockPCG", "GCGE_TestBlockPCGBarrierTimeout",
     "GCGE_BenchDenseProduct", "GCGE_SetSpMMTuning", "GCGE_SpMMTuneCandidates", "GCGE_SpMMTune",
+    "CUDA_TransferCreateFromCCS", "CUDA_TransferDestroy", "CUDA_MultiVecFromItoJ",
+    "MultiLinearSolverSetup_BlockAMG",
 ]
 
 _lib = None
@@ -468,7 +470,53 @@ _FT = {
                                      _VP),
     "EigenSolver": ctypes.CFUNCTYPE(None, _VP, _VP, ctypes.POINTER(ctypes.c_double), _VP,
                                     ctypes.c_int, ctypes.POINTER(ctypes.c_int), _VP),
+    "MultiVecFromItoJ": ctypes.CFUNCTYPE(None, _VP, ctypes.c_int, ctypes.c_int, _VP, _VP, _I2, _I2,
+                                         _VP, _VP),
 }
+
+
+class BlockAMGSolver(ctypes.Structure):
+    """src/ops_lin_sol.h:41-47 as include/gcge_ops.h declares it."""
+    _fields_ = [("max_iter", _VP), ("rate", _VP), ("tol", _VP), ("tol_type", ctypes.c_char * 8),
+                ("A_array", _VP), ("P_array", _VP), ("num_levels", ctypes.c_int),
+                ("mv_array_ws", _VP * 5), ("dbl_ws", _VP), ("int_ws", _VP), ("pc", _VP),
+                ("niter", ctypes.c_int), ("residual", ctypes.c_double)]
+
+
+class AMGArrays:
+    """The argument arrays of MultiLinearSolverSetup_BlockAMG (the library
+    keeps pointers to them, so they live as long as the solver is used):
+    level matrix handles, transfer handles, per-level workspace handles
+    (ws[i][l], i < 5), iteration caps, rates, tolerances and the BlockPCG
+    double / int workspaces for blocks of up to k columns."""
+
+    def __init__(self, mats, transfers, ws, max_iter, rate, tol, k):
+        L = len(mats)
+        if len(transfers) != L - 1 or len(ws) != 5 or any(len(w) != L for w in ws):
+            raise ValueError("hierarchy: L matrices, L - 1 transfers, 5 x L workspaces")
+        if len(max_iter) != 2 * L or len(rate) != L or len(tol) != L:
+            raise ValueError("max_iter needs 2 L entries, rate and tol L each")
+        self.L = L
+        self.A = (_VP * L)(*[_handle(m) for m in mats])
+        self.P = (_VP * max(1, L - 1))(*[_handle(t) for t in transfers])
+        self.levels = [(_VP * L)(*[_handle(w) for w in row]) for row in ws]
+        self.ws = (_VP * 5)(*[ctypes.addressof(a) for a in self.levels])
+        self.max_iter = (ctypes.c_int * (2 * L))(*[int(v) for v in max_iter])
+        self.rate = (ctypes.c_double * L)(*[float(v) for v in rate])
+        self.tol = (ctypes.c_double * L)(*[float(v) for v in tol])
+        self.dbl = (ctypes.c_double * (8 * k + 64))()
+        self.int = (ctypes.c_int * (4 * k + 64))()
+
+    def setup(self, lib, ops_ptr, tol_type="abs"):
+        """MultiLinearSolverSetup_BlockAMG(max_iter, rate, tol, tol_type,
+        A_array, P_array, L, mv_array_ws, dbl_ws, int_ws, NULL, ops)."""
+        lib.MultiLinearSolverSetup_BlockAMG(self.max_iter, self.rate, self.tol, tol_type.encode(),
+                                            self.A, self.P, ctypes.c_int(self.L), self.ws,
+                                            self.dbl, self.int, None, ops_ptr)
+
+
+def _handle(h):
+    return h.value if isinstance(h, ctypes.c_void_p) else h
 
 
 # ops->MultiLinearSolver (src/ops.h:121-122)
@@ -487,7 +535,7 @@ class CudaOps:
         lib.OPS_Create(ctypes.byref(self.ptr))
         lib.OPS_CUDA_Set(self.ptr)
         lib.OPS_Setup(self.ptr)
-        self._mats, self._mvs = [], []
+        self._mats, self._mvs, self._transfers = [], [], []
 
     def _fn(self, name):
         return ctypes.cast(getattr(self.ptr.contents, name), _FT[name])
@@ -506,6 +554,29 @@ class CudaOps:
             raise GCGEError(st, "CUDA_MatCreateFromCCS")
         self._mats.append(h)
         return h
+
+    def transfer(self, T):
+        """CUDA_TransferCreateFromCCS of a problems.Transfer (P_l: n_l fine rows
+        by n_{l+1} coarse columns), for the P_array of the block AMG solver."""
+        h = ctypes.c_void_p()
+        cp = np.ascontiguousarray(T.colptr, dtype=np.int32)
+        ri = np.ascontiguousarray(T.rowind, dtype=np.int32)
+        va = np.ascontiguousarray(T.data, dtype=np.float64)
+        st = self.lib.CUDA_TransferCreateFromCCS(ctypes.byref(h), ctypes.c_int(T.nrows),
+                                                 ctypes.c_int(T.ncols), _p(cp), _p(ri), _p(va))
+        if st != GCGE_OK:
+            raise GCGEError(st, "CUDA_TransferCreateFromCCS")
+        self._transfers.append(h)
+        return h
+
+    def from_i_to_j(self, P_array, level_i, level_j, x, y, start, end, ws=None):
+        """ops->MultiVecFromItoJ: P_array a sequence of transfer handles, ws
+        (per-level multivector handles) for jumps over several levels."""
+        parr = (_VP * max(1, len(P_array)))(*[h.value for h in P_array])
+        warr = None if ws is None else (_VP * len(ws))(*[w.value if w else None for w in ws])
+        self._fn("MultiVecFromItoJ")(parr, level_i, level_j, x, y, _I2(*start), _I2(*end), warr,
+                                     ctypes.cast(self.ptr, _VP))
+        self.check("MultiVecFromItoJ")
 
     def mat_axpby(self, alpha, X, beta, Y):
         """CUDA_MatAxpby: Y = alpha X + beta Y (the OPS MatAxpby slot)."""
@@ -606,7 +677,9 @@ class CudaOps:
             self._fn("MultiVecDestroy")(ctypes.byref(h), nc, ctypes.cast(self.ptr, _VP))
         for h in self._mats:
             self.lib.CUDA_MatDestroy(ctypes.byref(h))
-        self._mvs, self._mats = [], []
+        for h in self._transfers:
+            self.lib.CUDA_TransferDestroy(ctypes.byref(h))
+        self._mvs, self._mats, self._transfers = [], [], []
         if self.ptr:
             self.lib.OPS_Destroy(ctypes.byref(self.ptr))
 
@@ -623,6 +696,37 @@ def bench_spmm(A, k: int, fp32: bool, reps: int = 20):
         if st != GCGE_OK:
             raise GCGEError(st, "GCGE_BenchSpMM")
         return ms.value, by.value
+    finally:
+        ops.close()
+
+
+def block_amg(A_list, P_list, b, x0, max_iter, rate, tol, tol_type="abs"):
+    """The block AMG solver through the OPS surface: level matrices
+    (problems.CSRMatrix), transfers (problems.Transfer, P_l of n_l x n_{l+1}),
+    MultiLinearSolverSetup_BlockAMG with the reference's parameter arrays
+    (max_iter: cycles, then each level's pre- and post-smoothing caps; rate and
+    tol per level), then ops->MultiLinearSolver on b (n_0 x k) from x0.
+    Returns (x, the solver's residual field, cycles run)."""
+    load()
+    b = np.asfortranarray(b, dtype=np.float64)
+    k = b.shape[1]
+    ops = CudaOps()
+    try:
+        mats = [ops.mat(a) for a in A_list]
+        trans = [ops.transfer(t) for t in P_list]
+        ws = [[ops.multivec(m, k) for m in mats] for _ in range(5)]
+        arr = AMGArrays(mats, trans, ws, max_iter, rate, tol, k)
+        arr.setup(ops.lib, ops.ptr, tol_type)
+        ops.check("MultiLinearSolverSetup_BlockAMG")
+        bv = ops.multivec(mats[0], k, b)
+        xv = ops.multivec(mats[0], k, x0)
+        fn = ctypes.cast(ops.ptr.contents.MultiLinearSolver, _LINSOL)
+        fn(mats[0], bv, xv, _I2(0, 0), _I2(k, k), ctypes.cast(ops.ptr, _VP))
+        ops.check("MultiLinearSolver (BlockAMG)")
+        g = ctypes.cast(ops.ptr.contents.multi_linear_solver_workspace,
+                        ctypes.POINTER(BlockAMGSolver)).contents
+        residual, cycles = g.residual, g.niter
+        return ops.download(xv, 0, k), residual, cycles
     finally:
         ops.close()
 

@@ -19,7 +19,7 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libgcge_cuda.so")
 SOURCES = ["spmm.cu", "format.cu", "dense.cu", "eig.cu", "pcg.cu", "gcg.cu", "app_cuda.cu", "testing.cu",
-           "noalloc.cu", "ozaki.cu", "serve.cu", "linsol.cu", "ozaki_tc.cu"]
+           "noalloc.cu", "ozaki.cu", "serve.cu", "linsol.cu", "ozaki_tc.cu", "amg.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
          "--expt-relaxed-constexpr"]

@@ -691,6 +691,7 @@ void OPS_Destroy(OPS **ops) {
     orth_release(*ops);
     ctx_release(*ops);
     linsol_release(*ops);
+    amg_release(*ops);
     if ((*ops)->lapack_ops) OPS_Destroy(&(*ops)->lapack_ops);
     free(*ops);
     *ops = nullptr;
@@ -743,6 +744,8 @@ void OPS_CUDA_Set(OPS *ops) {
     ops->MatDotMultiVec = CUDA_MatDotMultiVec;
     ops->MatTransDotMultiVec = CUDA_MatDotMultiVec;
     ops->MultiVecQtAP = CUDA_MultiVecQtAP;
+    // level transfers for the block AMG solver (no app_ccs counterpart)
+    ops->MultiVecFromItoJ = CUDA_MultiVecFromItoJ;
 }
 
 int CUDA_MatCreateFromCCS(void **mat, int nrows, int ncols, const int *j_col, const int *i_row,

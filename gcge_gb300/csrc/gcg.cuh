@@ -55,6 +55,9 @@ void ctx_release(OPS *ops);
 // Per-ops state of MultiLinearSolverSetup_BlockPCG (linsol.cu), freed by
 // OPS_Destroy.
 void linsol_release(OPS *ops);
+// Per-ops state of MultiLinearSolverSetup_BlockAMG (amg.cu), freed by
+// OPS_Destroy.
+void amg_release(OPS *ops);
 
 // The GPU GCG installed as ops->EigenSolver.
 void gcg_eigensolver(void *A, void *B, double *eval, void **evec, int nevGiven, int *nevConv,

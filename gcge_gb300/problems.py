@@ -24,6 +24,8 @@ Workloads (no public dataset is involved; all are generated):
 * ``aniso2d(nx, ny, eps)`` - anisotropic 5-point Laplacian, -eps on x faces
   and -1 on y faces; ``batch_problems`` draws the 512-problem batch.
 * ``rgg_laplacian`` - shifted random-geometric-graph Laplacian L + 1e-3 I.
+* ``multigrid_2d`` - a geometric hierarchy (linear interpolation, Galerkin
+  coarse operators) of the 2D Laplacian for the block AMG solver.
 """
 from __future__ import annotations
 
@@ -35,6 +37,7 @@ __all__ = [
     "CSRMatrix", "splitmix_uniform", "splitmix_normal", "laplace2d", "laplace3d",
     "mass3d", "identity_diag", "diag_matrix", "vardiff3d", "aniso2d", "rgg_laplacian",
     "initial_block", "config1", "config2", "config3", "batch_problems", "to_dense",
+    "Transfer", "interpolation_1d", "multigrid_2d",
 ]
 
 
@@ -351,3 +354,65 @@ def serving_requests(count: int = 64, seed: int = 5, rate: float = 8.0, max_n: i
         out.append(dict(name=name, A=A, B=B, nev=nev, block_size=bs, nev_init=ni, nev_max=nm,
                         tol=(1e300, tol), arrival=t))
     return out
+
+
+# --------------------------------------------------------------------------
+# Multigrid hierarchies for the block AMG solver
+# --------------------------------------------------------------------------
+@dataclass
+class Transfer:
+    """Transfer operator P between adjacent levels: nrows fine rows by ncols
+    coarse columns, in CCS (column pointers, row indices, values; int32 and
+    float64), the layout of the reference's app_ccs matrices."""
+    nrows: int
+    ncols: int
+    colptr: np.ndarray
+    rowind: np.ndarray
+    data: np.ndarray
+
+    def to_scipy(self):
+        import scipy.sparse as sp
+        return sp.csc_matrix((self.data, self.rowind, self.colptr), shape=(self.nrows, self.ncols))
+
+    def transpose(self) -> "Transfer":
+        """P^T in CCS (its column pointers are P's row pointers)."""
+        m = self.to_scipy().tocsr()
+        m.sort_indices()
+        return Transfer(self.ncols, self.nrows, m.indptr.astype(np.int32),
+                        m.indices.astype(np.int32), m.data.astype(np.float64))
+
+
+def interpolation_1d(nc: int):
+    """(2 nc + 1) x nc linear interpolation: coarse point j sits on fine point
+    2 j + 1 with weight 1 and spreads 1/2 to fine points 2 j and 2 j + 2 (the
+    weights of the reference's test hierarchy, app/app_lapack.c:863-890)."""
+    import scipy.sparse as sp
+    j = np.arange(nc)
+    rows = np.concatenate([2 * j + 1, 2 * j, 2 * j + 2])
+    cols = np.concatenate([j, j, j])
+    vals = np.concatenate([np.ones(nc), np.full(nc, 0.5), np.full(nc, 0.5)])
+    return sp.csc_matrix((vals, (rows, cols)), shape=(2 * nc + 1, nc))
+
+
+def multigrid_2d(nx: int, ny: int, levels: int):
+    """Geometric hierarchy of the 5-point Laplacian (4, -1) on an nx x ny
+    grid: P_l = interpolation in y (x) interpolation in x, A_{l+1} =
+    P_l^T A_l P_l (Galerkin; the entries are dyadic rationals, so every
+    machine computes the same coarse matrices exactly).  nx and ny must stay
+    odd while halving: nx_{l+1} = (nx_l - 1) / 2.  Returns ([A_0 .. A_{L-1}]
+    as CSRMatrix, [P_0 .. P_{L-2}] as Transfer)."""
+    import scipy.sparse as sp
+    A = [laplace2d(nx, ny)]
+    P = []
+    cx, cy = nx, ny
+    for _ in range(levels - 1):
+        if cx % 2 == 0 or cy % 2 == 0 or cx < 3 or cy < 3:
+            raise ValueError(f"grid {cx} x {cy} cannot be coarsened")
+        cx, cy = (cx - 1) // 2, (cy - 1) // 2
+        p = sp.kron(interpolation_1d(cy), interpolation_1d(cx), format="csc")
+        p.sort_indices()
+        P.append(Transfer(p.shape[0], p.shape[1], p.indptr.astype(np.int32),
+                          p.indices.astype(np.int32), p.data.astype(np.float64)))
+        a = A[-1].to_scipy()
+        A.append(_from_scipy((p.T @ a @ p).tocsr()))
+    return A, P

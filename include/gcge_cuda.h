@@ -72,6 +72,25 @@ int CUDA_MatNnz(void *mat, long long *nnz);
  * function there to provide the slot.  Failures go to ops_cuda_last_error(). */
 void CUDA_MatAxpby(double alpha, void *matX, double beta, void *matY, struct OPS_ *ops);
 
+/* Transfer operator P between adjacent multigrid levels (nrows fine rows x
+ * ncols coarse columns) from host CCS arrays (j_col[ncols+1], i_row[nnz],
+ * data[nnz]), copied to HBM; for P_array of MultiLinearSolverSetup_BlockAMG
+ * and MultiVecFromItoJ.  No counterpart in app_ccs (its matrices are square
+ * operators; the reference's hierarchies come from ops->MultiGridCreate). */
+int CUDA_TransferCreateFromCCS(void **P, int nrows, int ncols, const int *j_col,
+                               const int *i_row, const double *data);
+void CUDA_TransferDestroy(void **P);
+/* The OPS MultiVecFromItoJ slot (src/ops.h:142-144; NULL in every backend
+ * the reference ships, src/ops.c:78): columns [startIJ[0], endIJ[0]) of the
+ * level-i block to [startIJ[1], endIJ[1]) of the level-j block, one level at
+ * a time: restriction x_{l+1} = P_l^T x_l going down, prolongation x_l =
+ * P_l x_{l+1} going up, P_array[l] from CUDA_TransferCreateFromCCS; between
+ * non-adjacent levels through columns [0, k) of multi_vec_ws[l].
+ * OPS_CUDA_Set installs it.  Failures go to ops_cuda_last_error(). */
+void CUDA_MultiVecFromItoJ(void **P_array, int level_i, int level_j, void **multi_vec_i,
+                           void **multi_vec_j, int *startIJ, int *endIJ, void ***multi_vec_ws,
+                           struct OPS_ *ops);
+
 /* Copy columns [start, end) between a device multivector and a host
  * column-major array with leading dimension ldh >= nrows. */
 int CUDA_MultiVecSetFromHost(void **mv, int start, int end, const double *host, int ldh);

@@ -141,6 +141,19 @@ typedef struct BlockPCGSolver_ {
     int niter; double residual;
 } BlockPCGSolver;
 
+/* src/ops_lin_sol.h:41-47: the block AMG parameters that
+ * MultiLinearSolverSetup_BlockAMG stores (pointers to the caller's arrays);
+ * ops->multi_linear_solver_workspace points at one between solves, and the
+ * solve fills in residual (and niter, the cycles run, which the reference
+ * leaves at 0). */
+typedef struct BlockAMGSolver_ {
+    int *max_iter; double *rate; double *tol; char tol_type[8];
+    void **A_array; void **P_array; int num_levels;
+    void ***mv_array_ws[5]; double *dbl_ws; int *int_ws;
+    void *pc;
+    int niter; double residual;
+} BlockAMGSolver;
+
 /* OPS lifetime: src/ops.c:26-149.  OPS_Setup fills Printf/GetWtime/
  * GetOptionFromCommandLine defaults; the GPU GCG needs no lapack_ops. */
 void OPS_Create(OPS **ops);
@@ -187,6 +200,26 @@ void MultiLinearSolverSetup_BlockPCG(int max_iter, double rate, double tol, cons
                                                             int *end, void **z, int s,
                                                             struct OPS_ *ops),
                                      struct OPS_ *ops);
+
+/* Block AMG setup: src/ops_lin_sol.h:48-53, src/ops_lin_sol.c:686-715.
+ * Installs the V-cycle of src/ops_lin_sol.c:466-685 as
+ * ops->MultiLinearSolver(mat, b, x, start, end, ops) over the caller's
+ * hierarchy: A_array[l] CUDA matrices (l < num_levels, A_array[0] the
+ * operator), P_array[l] transfers of n_l x n_{l+1} from
+ * CUDA_TransferCreateFromCCS, and mv_array_ws[i][l] CUDA multivectors of
+ * level l at least as wide as the block (0, 1: the coarse right-hand side and
+ * solution, levels >= 1; 2, 3, 4: the level's residual and smoothing
+ * workspaces).  Each level smooths with MultiLinearSolverSetup_BlockPCG
+ * (max_iter[2l+1] before and max_iter[2l+2] after the coarse correction,
+ * rate[l], tol[l], tol_type); cycles repeat until the residual field of the
+ * last level-0 smoothing is below tol[0] or after max_iter[0] cycles.  The
+ * arrays are read at every solve (the caller keeps them alive).  ops must
+ * provide MultiVecFromItoJ (OPS_CUDA_Set installs CUDA_MultiVecFromItoJ).
+ * Failures go to ops_cuda_last_error(). */
+void MultiLinearSolverSetup_BlockAMG(int *max_iter, double *rate, double *tol,
+                                     const char *tol_type, void **A_array, void **P_array,
+                                     int num_levels, void ***mv_array_ws[5], double *dbl_ws,
+                                     int *int_ws, void *pc, struct OPS_ *ops);
 
 /* GCG entry points: src/ops_eig_sol_gcg.c:1565-1628 (Setup), :1684-1741
  * (SetParameters), :1865-1877 (GCGE_Create), :1878-1918 (GCGE_Setparameters),

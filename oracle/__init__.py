@@ -2,8 +2,9 @@
 
 This package restates, on the CPU and in numpy/scipy, the reference GCGE
 algorithm (GCG outer loop, BlockPCG, modified Gram-Schmidt B-orthogonalisation,
-the OPS default multivector operations and the app_ccs/app_lapack backends),
-citing the reference file:line each function follows.
+the OPS default multivector operations and the app_ccs/app_lapack backends;
+the block AMG V-cycle in ``amg_oracle.py``), citing the reference file:line
+each function follows.
 
 Only ``tests/``, ``__graft_entry__.smoke()`` and ``bench.py``'s CPU-baseline
 and reference legs may import it, and only as the checker or as the timed CPU

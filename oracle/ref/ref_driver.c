@@ -10,7 +10,8 @@
  * sized as in gcge.c:503-510 (= src/ops_eig_sol_gcg.c:1647-1651),
  * EigenSolverSetup_GCG, GCGE_Setparameters, ops->EigenSolver.
  * The backend is app_ccs (app/app_ccs.c:213-249), the reference's sparse CCS
- * operator with int32 indices and FP64 values.
+ * operator with int32 indices and FP64 values.  Besides GCG: one call of the
+ * reference's MultiVecOrth (ref_orth) and of its BlockAMG (ref_block_amg).
  */
 #include <stdlib.h>
 #include <string.h>
@@ -141,6 +142,110 @@ int ref_orth(int n, int m, double *x, int start, int *end, const char *method, i
     ops->MultiVecOrth((void **)&X, start, end, matB, ops);
     free(ws_data);
     free(dbl_ws);
+    OPS_Destroy(&ops);
+    return 0;
+}
+
+#include "ops_lin_sol.h"
+/* A transfer operator between adjacent levels for the app_ccs backend: P
+ * (fine rows x coarse columns) and P^T, both CCS. */
+typedef struct {
+    CCSMAT P, PT;
+} RefTransfer;
+
+/* ops->MultiVecFromItoJ for app_ccs, which leaves the slot NULL
+ * (src/ops.c:78) and ships no implementation (src/ops.c:110-112 is commented
+ * out): level by level from level_i to level_j, restriction x_{l+1} = P_l^T
+ * x_l and prolongation x_l = P_l x_{l+1} with app_ccs's own MatDotMultiVec
+ * (rectangular CCS, app/app_ccs.c:50-139); columns [startIJ[0], endIJ[0]) of
+ * multi_vec_i to [startIJ[1], endIJ[1]) of multi_vec_j, through columns
+ * [0, k) of multi_vec_ws[l] at the levels in between. */
+static void ref_from_i_to_j(void **P_array, int level_i, int level_j, void **mv_i, void **mv_j,
+                            int *startIJ, int *endIJ, void ***mv_ws, struct OPS_ *ops)
+{
+    int k = endIJ[0] - startIJ[0];
+    int step = level_j > level_i ? 1 : -1;
+    void **src = mv_i;
+    int s0 = startIJ[0], l;
+    for (l = level_i; l != level_j; l += step) {
+        int next = l + step;
+        void **dst = next == level_j ? mv_j : mv_ws[next];
+        int d0 = next == level_j ? startIJ[1] : 0;
+        int start[2] = {s0, d0}, end[2] = {s0 + k, d0 + k};
+        RefTransfer *t = (RefTransfer *)P_array[step > 0 ? l : next];
+        ops->MatDotMultiVec(step > 0 ? (void *)&t->PT : (void *)&t->P, src, dst, start, end, ops);
+        src = dst;
+        s0 = d0;
+    }
+}
+
+/* The reference's BlockAMG (MultiLinearSolverSetup_BlockAMG and the solver
+ * it installs, src/ops_lin_sol.c:466-715) on the app_ccs backend: levels
+ * 0..num_levels-1 with A_l (n[l] x n[l], CCS) and transfers P_l
+ * (n[l] x n[l+1]) with their transposes, each given as three arrays per
+ * level; b and x are n[0] x k column-major (x holds the initial guess and
+ * receives the result); max_iter (2 num_levels entries), rate and tol (one
+ * per level) and tol_type as the setup takes them.  *residual_out receives
+ * the solver's residual field. */
+int ref_block_amg(int num_levels, const int *n,
+                  const int **a_colptr, const int **a_rowind, const double **a_val,
+                  const int **p_colptr, const int **p_rowind, const double **p_val,
+                  const int **pt_colptr, const int **pt_rowind, const double **pt_val,
+                  int k, const double *b, double *x,
+                  int *max_iter, double *rate, double *tol, const char *tol_type,
+                  double *residual_out)
+{
+    OPS *ops = NULL;
+    OPS_Create(&ops);
+    OPS_CCS_Set(ops);
+    OPS_Setup(ops);
+    ops->MultiVecFromItoJ = ref_from_i_to_j;
+
+    int L = num_levels, l, i;
+    CCSMAT *A = calloc((size_t)L, sizeof(CCSMAT));
+    RefTransfer *T = calloc((size_t)(L > 1 ? L - 1 : 1), sizeof(RefTransfer));
+    void **A_array = calloc((size_t)L, sizeof(void *));
+    void **P_array = calloc((size_t)(L > 1 ? L - 1 : 1), sizeof(void *));
+    for (l = 0; l < L; ++l) {
+        A[l].data = (double *)a_val[l]; A[l].i_row = (int *)a_rowind[l];
+        A[l].j_col = (int *)a_colptr[l]; A[l].nrows = n[l]; A[l].ncols = n[l];
+        A_array[l] = &A[l];
+    }
+    for (l = 0; l + 1 < L; ++l) {
+        T[l].P.data = (double *)p_val[l]; T[l].P.i_row = (int *)p_rowind[l];
+        T[l].P.j_col = (int *)p_colptr[l]; T[l].P.nrows = n[l]; T[l].P.ncols = n[l + 1];
+        T[l].PT.data = (double *)pt_val[l]; T[l].PT.i_row = (int *)pt_rowind[l];
+        T[l].PT.j_col = (int *)pt_colptr[l]; T[l].PT.nrows = n[l + 1]; T[l].PT.ncols = n[l];
+        P_array[l] = &T[l];
+    }
+    void ***mv_array_ws[5];
+    for (i = 0; i < 5; ++i) {
+        mv_array_ws[i] = calloc((size_t)L, sizeof(void **));
+        for (l = 0; l < L; ++l)
+            ops->MultiVecCreateByMat(&mv_array_ws[i][l], k, &A[l], ops);
+    }
+    void **mv_b = NULL, **mv_x = NULL;
+    ops->MultiVecCreateByMat(&mv_b, k, &A[0], ops);
+    ops->MultiVecCreateByMat(&mv_x, k, &A[0], ops);
+    memcpy(((LAPACKVEC *)mv_b)->data, b, sizeof(double) * (size_t)n[0] * (size_t)k);
+    memcpy(((LAPACKVEC *)mv_x)->data, x, sizeof(double) * (size_t)n[0] * (size_t)k);
+    double *dbl_ws = calloc((size_t)(8 * k + 64), sizeof(double));
+    int *int_ws = calloc((size_t)(4 * k + 64), sizeof(int));
+
+    MultiLinearSolverSetup_BlockAMG(max_iter, rate, tol, tol_type, A_array, P_array, L,
+                                    mv_array_ws, dbl_ws, int_ws, NULL, ops);
+    int start[2] = {0, 0}, end[2] = {k, k};
+    ops->MultiLinearSolver(A_array[0], mv_b, mv_x, start, end, ops);
+    *residual_out = ((BlockAMGSolver *)ops->multi_linear_solver_workspace)->residual;
+    memcpy(x, ((LAPACKVEC *)mv_x)->data, sizeof(double) * (size_t)n[0] * (size_t)k);
+
+    ops->MultiVecDestroy(&mv_b, k, ops);
+    ops->MultiVecDestroy(&mv_x, k, ops);
+    for (i = 0; i < 5; ++i) {
+        for (l = 0; l < L; ++l) ops->MultiVecDestroy(&mv_array_ws[i][l], k, ops);
+        free(mv_array_ws[i]);
+    }
+    free(dbl_ws); free(int_ws); free(A); free(T); free(A_array); free(P_array);
     OPS_Destroy(&ops);
     return 0;
 }

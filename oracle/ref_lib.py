@@ -97,3 +97,42 @@ def ref_orth(x, start, end, method, block_size, B=None, max_reorth=2,
                  ctypes.byref(e), method.encode(), ctypes.c_int(block_size),
                  ctypes.c_int(max_reorth), ctypes.c_double(zero_tol), *[_ptr(a) for a in arrs])
     return x[:, :e.value].copy(), e.value
+
+
+def ref_block_amg(A_list, P_list, b, x0, max_iter, rate, tol, tol_type="abs"):
+    """The reference's BlockAMG (MultiLinearSolverSetup_BlockAMG and the
+    solver it installs, src/ops_lin_sol.c:466-715) on the app_ccs backend,
+    with a MultiVecFromItoJ written for that backend in the driver.  A_list:
+    level matrices (problems.CSRMatrix, symmetric); P_list:
+    problems.Transfer, P_l of n_l x n_{l+1}; b, x0: n_0 x k.  max_iter has
+    2 L entries (cycles, then the pre- and post-smoothing iteration caps of
+    each level; the coarsest level's single solve takes entry 2 L - 1), rate
+    and tol one per level.  Returns (x, the solver's residual field)."""
+    lib = _load()
+    L = len(A_list)
+    assert len(P_list) == L - 1 and len(max_iter) == 2 * L
+    b = np.asfortranarray(b, dtype=np.float64)
+    x = np.array(x0, dtype=np.float64, order="F", copy=True)
+    k = b.shape[1]
+    PT = [p.transpose() for p in P_list]
+    keep = []
+
+    def ptrs(arrs):
+        keep.extend(arrs)
+        return (ctypes.c_void_p * max(1, len(arrs)))(*[a.ctypes.data for a in arrs])
+
+    n = np.array([a.n for a in A_list], dtype=np.int32)
+    mi = np.array(max_iter, dtype=np.int32)
+    ra = np.array(rate, dtype=np.float64)
+    to = np.array(tol, dtype=np.float64)
+    res = ctypes.c_double()
+    lib.ref_block_amg(
+        ctypes.c_int(L), _ptr(n),
+        ptrs([a.indptr for a in A_list]), ptrs([a.indices for a in A_list]),
+        ptrs([a.data for a in A_list]),
+        ptrs([p.colptr for p in P_list]), ptrs([p.rowind for p in P_list]),
+        ptrs([p.data for p in P_list]),
+        ptrs([p.colptr for p in PT]), ptrs([p.rowind for p in PT]), ptrs([p.data for p in PT]),
+        ctypes.c_int(k), _ptr(b), _ptr(x), _ptr(mi), _ptr(ra), _ptr(to), tol_type.encode(),
+        ctypes.byref(res))
+    return x, res.value

@@ -187,4 +187,5 @@ def test_spmm_tuner_candidates_without_gpu(lib):
     assert G.spmm_tune_candidates(40) == [40, 20, 14, 8]
     cnt = ctypes.c_int()
     assert lib.GCGE_SpMMTuneCandidates(0, None, 0, ctypes.byref(cnt)) == G.GCGE_ERR_ARG
+    assert lib.ops_cuda_last_error() == G.GCGE_ERR_ARG
     assert lib.GCGE_SetSpMMTuning(0) == G.GCGE_OK
