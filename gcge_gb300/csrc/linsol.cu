@@ -131,6 +131,18 @@ void solve_persistent(LinSolRecord &r, SparseMat *A, MultiVec *bv, int sb, Multi
     shift_values(c.upat.padded, c.ua.p, c.ub.p, 0.0, c.us64.p, nullptr, st);
     int niter = 0;
     double residual = -1.0;
+    // The reference runs one list of unconverged columns over the whole block
+    // and reports last_res[unconv[0]] (src/ops_lin_sol.c:406-410): the first
+    // column still iterating at the end, else (the list is compacted in place)
+    // the first column that entered the last iteration; init_res[0] when no
+    // iteration ran.  Chunks iterate independently, so each chunk's candidates
+    // are kept until the block's iteration count is known.
+    struct Candidate {
+        int it;
+        double active_res, entered_res, init0;
+        bool active, entered;
+    };
+    std::vector<Candidate> cand;
     for (int c0 = 0; c0 < k; c0 += kChunkCols) {
         const int kc = std::min(kChunkCols, k - c0);
         const int kp = rows_width(kc, 8);
@@ -143,21 +155,40 @@ void solve_persistent(LinSolRecord &r, SparseMat *A, MultiVec *bv, int sb, Multi
         rows_to_col<double, double>(n, kc, kp, c.xr64.p, xv->data + (size_t)(sx + c0) * xv->ld,
                                     xv->ld, false, st);
         const int it = pcg_last_iters(c.pcg, st);
-        // residual of the first column of the chunk that was still iterating
-        // at the end (else of the first column), as the reference reports
         PcgScalars hs;
         GCGE_CUDA(cudaMemcpyAsync(&hs, c.pcg.sc.p, sizeof(PcgScalars), cudaMemcpyDeviceToHost, st));
         GCGE_CUDA(cudaStreamSynchronize(st));
-        if (c0 == 0) {
-            int first = 0;
-            for (int j = 0; j < kc; ++j)
-                if (hs.active[j]) {
-                    first = j;
-                    break;
-                }
-            residual = it > 0 ? hs.last_res[first] : hs.init_res[0];
-        }
+        Candidate cd{it, 0.0, 0.0, hs.init_res[0], false, false};
+        for (int j = 0; j < kc; ++j)
+            if (hs.active[j]) {
+                cd.active = true;
+                cd.active_res = hs.last_res[j];
+                break;
+            }
+        for (int j = 0; j < kc && it > 0; ++j)
+            if (hs.active[j] || hs.left_at[j] == it) {
+                cd.entered = true;
+                cd.entered_res = hs.last_res[j];
+                break;
+            }
+        cand.push_back(cd);
         niter = std::max(niter, it);
+    }
+    if (niter == 0) {
+        residual = cand.empty() ? -1.0 : cand[0].init0;
+    } else {
+        bool found = false;
+        for (const Candidate &cd : cand)
+            if (cd.it == niter && cd.active) {
+                residual = cd.active_res;
+                found = true;
+                break;
+            }
+        for (size_t i = 0; i < cand.size() && !found; ++i)
+            if (cand[i].it == niter && cand[i].entered) {
+                residual = cand[i].entered_res;
+                found = true;
+            }
     }
     p.niter = niter;
     p.residual = residual;

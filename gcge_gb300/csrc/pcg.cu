@@ -598,10 +598,12 @@ k_block_pcg(PcgArgs<T> a) {
                     sc->init_res[c] = sqrt(rr);
                     sc->last_res[c] = sqrt(rr);
                     sc->active[c] = sqrt(rr) > a.tol * nb ? 1 : 0;
+                    sc->left_at[c] = 0;
                     sc->beta[c] = 0.0;
                     sc->alpha[c] = 0.0;
                 } else {
                     sc->active[c] = 0;
+                    sc->left_at[c] = 0;
                 }
             }
             __syncthreads();
@@ -802,8 +804,10 @@ k_block_pcg(PcgArgs<T> a) {
                     const double res = sqrt(rr);
                     sc->last_res[c] = res;
                     sc->beta[c] = rr / sc->rho1[c];
-                    if (!(res > a.rate * sc->init_res[c] && res > a.tol * sc->norm_b[c]))
+                    if (!(res > a.rate * sc->init_res[c] && res > a.tol * sc->norm_b[c])) {
                         sc->active[c] = 0;
+                        sc->left_at[c] = sc->niter + 1;  // niter moves on after the barrier
+                    }
                 }
                 __syncthreads();
                 if (tid == 0) {

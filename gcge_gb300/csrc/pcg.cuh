@@ -12,6 +12,10 @@ struct PcgScalars {
     double beta[kPcgMaxCols], init_res[kPcgMaxCols], last_res[kPcgMaxCols];
     double norm_b[kPcgMaxCols];
     int active[kPcgMaxCols];
+    // iteration (1-based) in which a column left, 0 if it never iterated:
+    // with every column gone, the reference's residual field names the first
+    // column that entered the last iteration (src/ops_lin_sol.c:406-410)
+    int left_at[kPcgMaxCols];
     int nactive;
     int niter;
 };

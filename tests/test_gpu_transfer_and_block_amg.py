@@ -2,7 +2,9 @@
 against scipy, and the block AMG solver (MultiLinearSolverSetup_BlockAMG,
 src/ops_lin_sol.c:466-715) through the OPS surface against the reference's
 own BlockAMG run on the same hierarchies (fixtures of
-tests/golden/make_golden_amg.py) and against the CPU restatement."""
+tests/golden/make_golden_amg.py) and against the CPU restatement; and the
+BlockPCG residual field those cycles stop on."""
+import ctypes
 import json
 import os
 
@@ -11,6 +13,7 @@ import pytest
 
 from gcge_gb300 import problems as P
 from oracle.amg_oracle import block_amg as oracle_block_amg
+from oracle.amg_oracle import block_pcg as oracle_block_pcg
 
 pytestmark = pytest.mark.gpu
 
@@ -86,3 +89,56 @@ def test_block_amg_matches_reference(gpu_lib, name):
                                         xo, c["max_iter"], c["rate"], c["tol"], c["tol_type"])
         assert cycles == cyc_o
         assert res == pytest.approx(res_o, rel=1e-3)
+
+
+class _BlockPCGSolver(ctypes.Structure):
+    """src/ops_lin_sol.h:29-40 as include/gcge_ops.h declares it."""
+    _fields_ = [("max_iter", ctypes.c_int), ("rate", ctypes.c_double), ("tol", ctypes.c_double),
+                ("tol_type", ctypes.c_char * 8), ("mv_ws", ctypes.c_void_p * 3),
+                ("dbl_ws", ctypes.c_void_p), ("int_ws", ctypes.c_void_p), ("pc", ctypes.c_void_p),
+                ("MatDotMultiVec", ctypes.c_void_p), ("niter", ctypes.c_int),
+                ("residual", ctypes.c_double)]
+
+
+def test_block_pcg_residual_field_follows_the_reference_list(gpu_lib):
+    """The residual field that BlockAMG's cycles stop on, from the persistent
+    route on 45 columns (two launches): columns 0-39 are Laplacian
+    eigenvectors and leave after one step, columns 40-44 are random and still
+    iterate after 20 steps.  The reference reports the last residual of the
+    first column left in its list (src/ops_lin_sol.c:406-410): column 40's,
+    as the restatement does."""
+    G = gpu_lib
+    nx, k, steps = 40, 45, 20
+    A = P.laplace2d(nx, nx)
+    n = A.n
+
+    def mode(m):
+        return np.sin(np.pi * m * np.arange(1, nx + 1) / (nx + 1))
+
+    B = np.zeros((n, k), order="F")
+    for j in range(40):
+        B[:, j] = np.kron(mode(1 + j // 5), mode(1 + j % 5))
+    B[:, 40:] = (P.splitmix_uniform(9, n * 5, 0) - 0.5).reshape((n, 5), order="F")
+    X0 = np.zeros((n, k), order="F")
+    ops = G.CudaOps()
+    try:
+        h = ops.mat(A)
+        b = ops.multivec(h, k, B)
+        x = ops.multivec(h, k, X0)
+        ops.lib.MultiLinearSolverSetup_BlockPCG(ctypes.c_int(steps), ctypes.c_double(0.0),
+                                                ctypes.c_double(1e-9), b"abs", None, None, None,
+                                                None, None, ops.ptr)
+        ops.check("MultiLinearSolverSetup_BlockPCG")
+        fn = ctypes.cast(ops.ptr.contents.MultiLinearSolver, G._LINSOL)
+        fn(h, b, x, G._I2(0, 0), G._I2(k, k), ctypes.cast(ops.ptr, ctypes.c_void_p))
+        ops.check("MultiLinearSolver")
+        ws = ctypes.cast(ops.ptr.contents.multi_linear_solver_workspace,
+                         ctypes.POINTER(_BlockPCGSolver)).contents
+        niter, residual = ws.niter, ws.residual
+    finally:
+        ops.close()
+    As = A.to_scipy()
+    st = oracle_block_pcg(lambda v: As @ v, B, X0.copy(order="F"), steps, 0.0, 1e-9, "abs")
+    assert niter == st.niter == steps
+    assert residual == pytest.approx(st.residual, rel=1e-6)
+    assert residual > 1e-6          # a random column's, not an eigenvector column's
