@@ -78,9 +78,28 @@ void check_slot(const char *what) {
 }
 
 // Per-ops state: the reference keeps one static BlockAMGSolver per process
-// (src/ops_lin_sol.c:690-693); here every ops has its own.
+// (src/ops_lin_sol.c:690-693); here every ops has its own.  The smoothing
+// solves of each level run on an OPS object of that level: the block-PCG
+// setup keeps its operator (the level matrix on its union pattern) per OPS,
+// so one per level builds each level's operator once instead of at every
+// switch between levels.
 struct AmgRecord {
     BlockAMGSolver pub;  // ops->multi_linear_solver_workspace points here
+    std::vector<OPS *> level_ops;
+    ~AmgRecord() {
+        for (OPS *&o : level_ops) OPS_Destroy(&o);
+    }
+    OPS *level(int l) {
+        while ((int)level_ops.size() <= l) {
+            OPS *o = nullptr;
+            OPS_Create(&o);
+            GCGE_REQUIRE(o != nullptr, GCGE_ERR_ALLOC, "BlockAMG: level solver");
+            OPS_CUDA_Set(o);
+            OPS_Setup(o);
+            level_ops.push_back(o);
+        }
+        return level_ops[l];
+    }
 };
 
 std::mutex g_amg_mu;
@@ -97,20 +116,23 @@ AmgRecord *amg_record(OPS *ops, bool create) {
 }
 
 // One V-cycle from `level` down (src/ops_lin_sol.c:466-642): columns
-// [start_bx[0], end_bx[0]) of b, [start_bx[1], end_bx[1]) of x.
+// [start_bx[0], end_bx[0]) of b, [start_bx[1], end_bx[1]) of x.  The
+// residual, the transfers and the correction go through the caller's slots;
+// the smoothing solves (BlockPCG with the level's parameters) through the
+// level's own OPS object.
 void amg_cycle(AmgRecord &r, int level, void **mv_b, void **mv_x, int *start_bx, int *end_bx,
                OPS *ops) {
     BlockAMGSolver &g = r.pub;
-    auto solver_at_entry = ops->MultiLinearSolver;
+    OPS *lops = r.level(level);
     const int coarsest = g.num_levels - 1;
     const int bs = end_bx[1] - start_bx[1];
     void *A = g.A_array[level];
     void **ws[3] = {g.mv_array_ws[2][level], g.mv_array_ws[3][level], g.mv_array_ws[4][level]};
     // pre-smoothing (the whole solve at the coarsest level), :485-502
     MultiLinearSolverSetup_BlockPCG(g.max_iter[2 * level + 1], g.rate[level], g.tol[level],
-                                    g.tol_type, ws, g.dbl_ws, g.int_ws, nullptr, nullptr, ops);
+                                    g.tol_type, ws, g.dbl_ws, g.int_ws, nullptr, nullptr, lops);
     check_slot("MultiLinearSolverSetup_BlockPCG");
-    ops->MultiLinearSolver(A, mv_b, mv_x, start_bx, end_bx, ops);
+    lops->MultiLinearSolver(A, mv_b, mv_x, start_bx, end_bx, lops);
     check_slot("smoothing");
     if (level < coarsest) {
         int start[2], end[2];
@@ -131,7 +153,6 @@ void amg_cycle(AmgRecord &r, int level, void **mv_b, void **mv_x, int *start_bx,
         check_slot("MultiVecFromItoJ (restriction)");
         ops->MultiVecAxpby(0.0, nullptr, 0.0, coarse_x, start, end, ops);
         check_slot("MultiVecAxpby");
-        ops->multi_linear_solver_workspace = (void *)&g;
         amg_cycle(r, coarse, coarse_b, coarse_x, start, end, ops);
         // prolongation into ws[0] and x += P e, :577-600
         ops->MultiVecFromItoJ(g.P_array, coarse, level, coarse_x, mv_r, start, end,
@@ -143,16 +164,15 @@ void amg_cycle(AmgRecord &r, int level, void **mv_b, void **mv_x, int *start_bx,
         // post-smoothing, :611-627
         MultiLinearSolverSetup_BlockPCG(g.max_iter[2 * level + 2], g.rate[level], g.tol[level],
                                         g.tol_type, ws, g.dbl_ws, g.int_ws, nullptr, nullptr,
-                                        ops);
+                                        lops);
         check_slot("MultiLinearSolverSetup_BlockPCG");
-        ops->MultiLinearSolver(A, mv_b, mv_x, start_bx, end_bx, ops);
+        lops->MultiLinearSolver(A, mv_b, mv_x, start_bx, end_bx, lops);
         check_slot("smoothing");
     }
-    // the residual field of the last smoothing solve, then the AMG solver
-    // back in place, :637-641
-    g.residual = static_cast<BlockPCGSolver *>(ops->multi_linear_solver_workspace)->residual;
-    ops->multi_linear_solver_workspace = (void *)&g;
-    ops->MultiLinearSolver = solver_at_entry;
+    // the residual field of the last smoothing solve, :637; the caller's ops
+    // keeps the AMG solver installed throughout (the reference re-installs
+    // it after each level, :638-641)
+    g.residual = static_cast<BlockPCGSolver *>(lops->multi_linear_solver_workspace)->residual;
 }
 
 // Sizes of the hierarchy and of the workspaces a cycle of bs columns uses,
