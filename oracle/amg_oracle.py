@@ -26,10 +26,12 @@ class PCGState:
         self.residual = -1.0
 
 
-def block_pcg(matvec, b, x, max_iter, rate, tol, tol_type="abs", state=None):
+def block_pcg(matvec, b, x, max_iter, rate, tol, tol_type="abs", state=None, user_norms=None):
     """BlockPCG, src/ops_lin_sol.c:140-437: CG on every column of x (n x k, in
     place) for A x = b, columns leaving when their residual norm falls below
-    rate times its initial value or tol (times |b| for "rel").  Returns the
+    rate times its initial value or tol times the column's norm (1 for "abs",
+    |b| for "rel", |user_norms[i]| for "user", the values the caller leaves in
+    dbl_ws, :186-191).  Returns the
     state with niter and residual as the reference fills them (:406-410): the
     last residual of the column first in the int_ws list of unconverged
     columns after the last iteration (that list is compacted in place, so
@@ -40,6 +42,8 @@ def block_pcg(matvec, b, x, max_iter, rate, tol, tol_type="abs", state=None):
     k = b.shape[1]
     if tol_type == "rel":                                   # :172-185
         norm_b = np.sqrt(np.einsum("ij,ij->j", b, b))
+    elif tol_type == "user":                                # :186-191
+        norm_b = np.abs(np.asarray(user_norms, dtype=np.float64)[:k])
     else:                                                   # :192-197
         norm_b = np.ones(k)
     r = b - matvec(x)                                       # :201-221

@@ -249,3 +249,43 @@ int ref_block_amg(int num_levels, const int *n,
     OPS_Destroy(&ops);
     return 0;
 }
+
+/* One call of the reference's BlockPCG (MultiLinearSolverSetup_BlockPCG +
+ * ops->MultiLinearSolver, src/ops_lin_sol.c:140-465) on the app_ccs backend:
+ * A (n x n CCS) x = b for columns [sb, sb + k) of b (n x mb) into
+ * [sx, sx + k) of x (n x mx, holding the initial guess), with max_iter, rate,
+ * tol and tol_type ("abs", "rel", or "user" with |user_norms[i]| as the
+ * norms).  *niter_out and *residual_out receive the solver record's fields. */
+int ref_block_pcg(int n, const int *a_colptr, const int *a_rowind, const double *a_val,
+                  int mb, double *b, int sb, int mx, double *x, int sx, int k,
+                  int max_iter, double rate, double tol, const char *tol_type,
+                  const double *user_norms, int *niter_out, double *residual_out)
+{
+    OPS *ops = NULL;
+    OPS_Create(&ops);
+    OPS_CCS_Set(ops);
+    OPS_Setup(ops);
+    CCSMAT A;
+    A.data = (double *)a_val; A.i_row = (int *)a_rowind; A.j_col = (int *)a_colptr;
+    A.nrows = n; A.ncols = n;
+    LAPACKVEC B = {b, n, mb, n}, X = {x, n, mx, n};
+    void **ws[3];
+    int i;
+    for (i = 0; i < 3; ++i) ops->MultiVecCreateByMat(&ws[i], k, &A, ops);
+    double *dbl_ws = calloc((size_t)(6 * k + 64), sizeof(double));
+    int *int_ws = calloc((size_t)(2 * k + 64), sizeof(int));
+    if (user_norms != NULL)
+        memcpy(dbl_ws, user_norms, sizeof(double) * (size_t)k);
+    MultiLinearSolverSetup_BlockPCG(max_iter, rate, tol, tol_type, ws, dbl_ws, int_ws, NULL, NULL,
+                                    ops);
+    int start[2] = {sb, sx}, end[2] = {sb + k, sx + k};
+    ops->MultiLinearSolver(&A, (void **)&B, (void **)&X, start, end, ops);
+    BlockPCGSolver *s = (BlockPCGSolver *)ops->multi_linear_solver_workspace;
+    *niter_out = s->niter;
+    *residual_out = s->residual;
+    for (i = 0; i < 3; ++i) ops->MultiVecDestroy(&ws[i], k, ops);
+    free(dbl_ws);
+    free(int_ws);
+    OPS_Destroy(&ops);
+    return 0;
+}

@@ -136,3 +136,20 @@ def ref_block_amg(A_list, P_list, b, x0, max_iter, rate, tol, tol_type="abs"):
         ctypes.c_int(k), _ptr(b), _ptr(x), _ptr(mi), _ptr(ra), _ptr(to), tol_type.encode(),
         ctypes.byref(res))
     return x, res.value
+
+
+def ref_block_pcg(A, b, x0, sb, sx, k, max_iter, rate, tol, tol_type="abs", user_norms=None):
+    """The reference's BlockPCG (src/ops_lin_sol.c:140-465) on the app_ccs
+    backend: columns [sb, sb + k) of b into [sx, sx + k) of a copy of x0.
+    Returns (x, niter, residual) with the solver record's fields."""
+    lib = _load()
+    b = np.array(b, dtype=np.float64, order="F", copy=True)
+    x = np.array(x0, dtype=np.float64, order="F", copy=True)
+    un = None if user_norms is None else np.ascontiguousarray(user_norms, dtype=np.float64)
+    it, res = ctypes.c_int(), ctypes.c_double()
+    lib.ref_block_pcg(ctypes.c_int(A.n), _ptr(A.indptr), _ptr(A.indices), _ptr(A.data),
+                      ctypes.c_int(b.shape[1]), _ptr(b), ctypes.c_int(sb), ctypes.c_int(x.shape[1]),
+                      _ptr(x), ctypes.c_int(sx), ctypes.c_int(k), ctypes.c_int(max_iter),
+                      ctypes.c_double(rate), ctypes.c_double(tol), tol_type.encode(), _ptr(un),
+                      ctypes.byref(it), ctypes.byref(res))
+    return x, it.value, res.value

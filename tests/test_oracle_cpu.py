@@ -138,3 +138,67 @@ def test_oracle_orth_and_w12_solves_match_reference_fixture(case, golden_orth):
     assert r.nconv >= nev
     assert np.max(np.abs(r.eval[:nev] - ref) / np.abs(ref)) < 1e-10
     assert abs(r.niter - g["niter"]) <= max(3, g["niter"] // 5)
+
+
+def _pcg_cases():
+    """(name, A, b, x0, sb, sx, k, max_iter, rate, tol, tol_type, user_norms)."""
+    A = P.laplace2d(40, 30)
+    n = A.n
+    rng = np.random.default_rng(0)
+    B = rng.standard_normal((n, 14))
+    X0 = 0.1 * rng.standard_normal((n, 13))
+    # columns whose right-hand sides are eigenvectors leave after one step
+    sx_ = np.sin(np.pi * np.arange(1, 41) / 41)
+    sy_ = np.sin(np.pi * 2 * np.arange(1, 31) / 31)
+    Be = B.copy()
+    Be[:, 2] = np.kron(sy_, sx_)
+    Be[:, 3] = 3.0 * np.kron(sy_, sx_)
+    Z = np.zeros_like(X0)
+    return [
+        ("abs_ranges", A, B, X0, 2, 1, 6, 30, 1e-2, 1e-6, "abs", None),
+        ("rel_early_leavers", A, Be, Z, 2, 0, 12, 25, 0.0, 1e-10, "rel", None),
+        ("user_norms", A, B, X0, 0, 0, 5, 40, 1e-3, 1e-7, "user",
+         np.array([2.0, -1.0, 0.5, 4.0, 1.0])),
+        ("all_converge", A, B, Z, 1, 3, 7, 400, 0.0, 1e-8, "abs", None),
+        ("no_iteration", A, B, X0, 0, 0, 4, 30, 1e-2, 1e30, "abs", None),
+    ]
+
+
+@pytest.mark.skipif(not ref_lib.available(), reason="reference build (oracle/_ref) not present")
+@pytest.mark.parametrize("idx", range(5))
+def test_block_pcg_restatements_match_live_reference(idx):
+    """Both CPU restatements of BlockPCG (the GCG oracle's, which the GPU
+    linear-solver tests compare with, and the block AMG oracle's, which also
+    keeps the solver record's fields) against the compiled reference's
+    BlockPCG: the solution, the iteration count and the residual field
+    (src/ops_lin_sol.c:406-410), on column ranges, early leavers, "rel" and
+    "user" norms, convergence of every column, and no iteration at all."""
+    from oracle.amg_oracle import block_pcg
+    name, A, B, X0, sb, sx, k, mi, rate, tol, tt, un = _pcg_cases()[idx]
+    xr, itr, resr = ref_lib.ref_block_pcg(A, B, X0, sb, sx, k, mi, rate, tol, tt, un)
+    As = A.to_scipy()
+    b = np.asfortranarray(B[:, sb:sb + k])
+    # the block AMG oracle's BlockPCG
+    x1 = np.array(X0[:, sx:sx + k], order="F", copy=True)
+    st = block_pcg(lambda v: As @ v, b, x1, mi, rate, tol, tt, user_norms=un)
+    assert np.abs(x1 - xr[:, sx:sx + k]).max() <= 1e-12 * max(1.0, np.abs(xr).max())
+    assert st.niter == itr
+    assert st.residual == pytest.approx(resr, rel=1e-6, abs=1e-14 * np.linalg.norm(b))
+    # columns outside the range are untouched
+    keep = [c for c in range(X0.shape[1]) if not sx <= c < sx + k]
+    assert np.array_equal(xr[:, keep], X0[:, keep])
+    # the GCG oracle's BlockPCG
+    if tt != "user":
+        p = GCGParams(nev_init=1, nev_max=1, block_size=1, cg_max_iter=mi, cg_rate=rate,
+                      cg_tol=tol, cg_tol_type=tt)
+        o = GCGOracle(As, None, p)
+        x2 = np.array(X0[:, sx:sx + k], order="F", copy=True)
+        it2 = o.block_pcg(b, x2)
+        assert it2 == itr
+        assert np.abs(x2 - xr[:, sx:sx + k]).max() <= 1e-12 * max(1.0, np.abs(xr).max())
+    if name == "rel_early_leavers":
+        assert itr == mi and resr > 1e-6          # a random column's residual
+    if name == "no_iteration":
+        assert itr == 0
+        r0 = np.linalg.norm(B[:, sb] - As @ X0[:, sx])
+        assert resr == pytest.approx(r0, rel=1e-12)
