@@ -189,3 +189,45 @@ def test_spmm_tuner_candidates_without_gpu(lib):
     assert lib.GCGE_SpMMTuneCandidates(0, None, 0, ctypes.byref(cnt)) == G.GCGE_ERR_ARG
     assert lib.ops_cuda_last_error() == G.GCGE_ERR_ARG
     assert lib.GCGE_SetSpMMTuning(0) == G.GCGE_OK
+
+
+# The C examples of INTEGRATION.md, each compiled as a function body against
+# the headers and linked against the library (not run: no device here).
+_SNIPPET_PRELUDES = {
+    "## 1. Drop-in": "void snippet(int n, int *j_col, int *i_row, double *data, int nevMax, "
+                     "int nevGiven, double *x0, int block_size, int nevInit, double gapMin, "
+                     "int maxit, int nev, double *eval, double *evec_host)",
+    "## 1b.": "void snippet(OPS *ops, int argc, char **argv)",
+    "## 2d.": "void snippet(OPS *ops, int L, int *n, int **a_col, int **a_row, double **a_val, "
+              "int **p_col, int **p_row, double **p_val, int block_size, int *max_iter, "
+              "double *rate, double *tol, double *dbl_ws, int *int_ws, void **b, void **x, "
+              "int *start, int *end)",
+}
+
+
+def _integration_snippets():
+    text = open(os.path.join(ROOT, "INTEGRATION.md")).read()
+    out = {}
+    for head, proto in _SNIPPET_PRELUDES.items():
+        sec = text[text.index(head):]
+        body = sec[sec.index("```c\n") + 5:]
+        body = body[:body.index("```")]
+        out[head] = (proto, "\n".join(l for l in body.splitlines()
+                                      if not l.startswith("#include")))
+    return out
+
+
+@pytest.mark.skipif(shutil.which("gcc") is None, reason="gcc not available")
+@pytest.mark.parametrize("head", list(_SNIPPET_PRELUDES))
+def test_integration_examples_compile_and_link(lib, tmp_path, head):
+    proto, body = _integration_snippets()[head]
+    src = tmp_path / "snippet.c"
+    src.write_text("#include <stdlib.h>\n#include \"gcge_cuda.h\"\n" + proto +
+                   " {\n    int l, i;\n    (void)l; (void)i;\n" + body +
+                   "\n}\nint main(void) { return 0; }\n")
+    libdir = os.path.dirname(G.lib_path())
+    r = subprocess.run(["gcc", "-std=c99", "-Wall", "-Wno-unused-variable",
+                        "-Wno-unused-but-set-variable", "-I" + INC, str(src), "-o",
+                        str(tmp_path / "snippet"), "-L" + libdir, "-lgcge_cuda"],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
